@@ -1,0 +1,172 @@
+"""Solve drivers: ``ebSolve`` / ``ebtSolve`` / ``ebSolveCycles``.
+
+Host sequencing follows ``EllipticBSAM/src/ebSolve.m:22-94`` (and the tree
+copy ``EllipticBSAMTree/src/ebtSolve.m``): set-up, then either geometry-
+driven refinement followed by one solve (``Indicator='fun'``) or
+solve / tag / add level / re-solve.  Every ``ebSolveCycles`` call -- the
+reference's hot path -- runs on the GPU through the C-ABI library
+(``bsam.device``); the set-up ghost fills and the new-level prolongation
+run there too.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import hierarchy as hier
+from .options import ebOptions
+from .tagcluster import tag_cluster
+
+
+class Solution(dict):
+    def __getattr__(self, name):
+        try:
+            return self[name]
+        except KeyError as e:
+            raise AttributeError(name) from e
+
+
+def default_backend(opts):
+    from .device import DeviceBackend
+    return DeviceBackend.get(int(opts.get('Device', 0)))
+
+
+def ebSolveCycles(H, backend=None):
+    """Run V-cycles on H until ``rel <= RelTol`` or ``MaxVCycles``
+    (``EllipticBSAM/src/ebSolveCycles.m:1-80``); appends one stage record."""
+    backend = backend or default_backend(H.opts)
+    it, hist, rel, vis = backend.solve_cycles(H)
+    ncellTot = 0
+    for k in range(H.rootIdx, H.nlev + 1):
+        ncellTot += sum(f.size for f in H.lev[k].F)
+    stage = {
+        'amrLevels': H.nlev - H.rootIdx + 1,
+        'nlev': H.nlev,
+        'vcycles': int(it),
+        'resHist': np.asarray(hist),
+        'finalRel': float(rel),
+        'visibleCells': int(vis),
+        'totalCells': int(ncellTot),
+    }
+    if len(hist) >= 2:
+        stage['avgFactor'] = (hist[-1] / max(hist[0], np.finfo(float).tiny)) ** (1.0 / (len(hist) - 1))
+    else:
+        stage['avgFactor'] = math.nan
+    H.stats['stages'].append(stage)
+    if H.opts.Verbose >= 1:
+        print(f"[ebsam] stage {len(H.stats['stages'])}: {stage['amrLevels']} AMR level(s), {it} V-cycle(s), "
+              f"|r|/|f| = {rel:.2e}, avg factor {stage['avgFactor']:.3f}, {vis} visible cells")
+    return H
+
+
+ebtSolveCycles = ebSolveCycles
+
+
+def build_hierarchy(prob, opts, backend, tree=False):
+    """The geometry-driven ('fun') hierarchy: set-up, then tag/cluster/add
+    level until MaxLevels (``ebSolve.m:30-37``); no solve."""
+    H = hier.setup(prob, opts, backend, tree=tree)
+    while (H.nlev - H.rootIdx + 1) < opts.MaxLevels:
+        boxes = tag_cluster(H)
+        if boxes.shape[0] == 0:
+            break
+        H = hier.add_level(H, boxes, backend)
+    return H
+
+
+def _solve(prob, args, kwargs, tree, backend):
+    if len(args) == 1 and isinstance(args[0], dict) and not kwargs:
+        opts = ebOptions(args[0])
+    else:
+        opts = ebOptions(*args, **kwargs)
+    backend = backend or default_backend(opts)
+    H = hier.setup(prob, opts, backend, tree=tree)
+    if str(opts.Indicator).lower() == 'fun':
+        while (H.nlev - H.rootIdx + 1) < opts.MaxLevels:
+            boxes = tag_cluster(H)
+            if boxes.shape[0] == 0:
+                break
+            H = hier.add_level(H, boxes, backend)
+        H = ebSolveCycles(H, backend)
+    else:
+        H = ebSolveCycles(H, backend)
+        while (H.nlev - H.rootIdx + 1) < opts.MaxLevels:
+            boxes = tag_cluster(H)
+            if boxes.shape[0] == 0:
+                if opts.Verbose >= 1:
+                    print(f'[ebsam] no cells tagged; stopping at {H.nlev - H.rootIdx + 1} AMR level(s)')
+                break
+            H = hier.add_level(H, boxes, backend)
+            H = ebSolveCycles(H, backend)
+    mz = opts.MeanZero
+    if isinstance(mz, str) and mz.lower() == 'auto':
+        mz = H.coarsest['singular']
+    if mz:
+        m, _ = backend.composite_mean(H)
+        for k in range(1, H.nlev + 1):
+            for p in range(H.lev[k].np):
+                H.lev[k].Q[p] = H.lev[k].Q[p] - m
+        H.touch()
+    sol = Solution()
+    sol['H'] = H
+    sol['stats'] = H.stats
+    sol['err'] = error_norms(H) if prob.exact is not None else None
+    sol['mass'] = backend.mass_check(H)
+    levels = []
+    for k in range(H.rootIdx, H.nlev + 1):
+        lev = H.lev[k]
+        d = {'n': lev.n, 'h': lev.h, 'np': lev.np, 'cells': sum(f.size for f in lev.F), 'box': lev.box.copy()}
+        if tree:
+            d['parent'] = lev.parent.copy()
+            d['mbounds'] = lev.mbounds.copy()
+        levels.append(d)
+    sol['levels'] = levels
+    return sol
+
+
+def ebSolve(prob, *args, backend=None, **kwargs):
+    """Adaptive FAS multigrid solve (``EllipticBSAM/src/ebSolve.m``)."""
+    return _solve(prob, args, kwargs, False, backend)
+
+
+def ebtSolve(prob, *args, backend=None, **kwargs):
+    """Tree-form adaptive solve (``EllipticBSAMTree/src/ebtSolve.m``)."""
+    return _solve(prob, args, kwargs, True, backend)
+
+
+def error_norms(H, ufun=None):
+    """``ebErrorNorms`` (``EllipticBSAM/src/ebErrorNorms.m``): composite error
+    of the visible cells against the exact solution; the singular
+    all-Neumann problem is compared modulo its composite mean."""
+    ufun = ufun or H.prob.exact
+    dom = H.prob.domain
+    E = {}
+    for k in range(H.rootIdx, H.nlev + 1):
+        lev = H.lev[k]
+        for p in range(lev.np):
+            b = lev.box[p]
+            xc = dom[0] + (np.arange(b[0], b[1] + 1) - 0.5) * lev.h[0]
+            yc = dom[2] + (np.arange(b[2], b[3] + 1) - 0.5) * lev.h[1]
+            XC, YC = np.meshgrid(xc, yc, indexing='ij')
+            E[(k, p)] = lev.Q[p][1:-1, 1:-1] - ufun(XC, YC)
+    m = 0.0
+    if H.coarsest['singular']:
+        tot = area = 0.0
+        for (k, p), e in E.items():
+            da = H.lev[k].h[0] * H.lev[k].h[1]
+            vis = ~H.lev[k].covered[p]
+            tot += float(np.sum(e[vis])) * da
+            area += np.count_nonzero(vis) * da
+        m = tot / max(area, np.finfo(float).tiny)
+        E = {key: e - m for key, e in E.items()}
+    linf = l2sq = 0.0
+    dof = 0
+    for (k, p), e in E.items():
+        da = H.lev[k].h[0] * H.lev[k].h[1]
+        ev = e[~H.lev[k].covered[p]]
+        if ev.size:
+            linf = max(linf, float(np.max(np.abs(ev))))
+            l2sq += float(np.sum(ev ** 2)) * da
+            dof += ev.size
+    return {'linf': linf, 'l2': math.sqrt(l2sq), 'dof': dof, 'meanShift': m}
