@@ -1,0 +1,307 @@
+"""Benchmark: the diffuse-domain starfish solve (BSAM-in-MATLAB examples/
+demoStarfish.m 'full': 64^2 base refined through 5 AMR levels to 1024^2-
+equivalent spacing, 543,384 stored cells, RelTol 1e-10) on one GB300.
+
+One step = one ebSolveCycles of that hierarchy from its initial state (zero
+initial guess): ghost fill, initial residual, V(3,3)-cycles to relative
+composite residual 1e-10 (10 cycles).
+
+  value   solves/s with the hierarchy resident in HBM (device-side state
+          restore before each solve; L2 flushed between solves by writing a
+          256 MiB buffer, the hierarchy being ~40 MB).
+  e2e     the same solves through the C-ABI with host buffers: per solve the
+          initial guess and source go host->device, the solution and the
+          residual history come back (pinned host memory).
+  roofline  the red-black smoother, algorithmic bytes 48 B per cell per
+          red+black sweep (24 B per colour pass), per-launch CUDA-event times
+          of eagerly launched V-cycles, against the measured HBM copy peak.
+  cpu_baseline  the C oracle (a restatement of the reference's MATLAB path)
+          on the host cores, a bounded sample of whole solves.
+
+`--impl reference` times the reference's CPU path instead: MATLAB is not
+available, so the C oracle restatement runs on all host cores.
+With several ranks (torchrun) every rank solves its own replica; the
+hierarchy does not shard (replicas only).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, 'bsam-in-matlab_gb300'), os.path.join(ROOT, 'oracle')):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = 'solves/s & p50/p99 ms at rel resid 1e-10, mixed vs FP64 GPU; smoother HBM GB/s'
+WORKLOAD = ('starfish diffuse-domain transmission, 64^2 base + 5 AMR levels (1024^2-equivalent), '
+            '543384 stored cells, QC-ring hierarchy, V(3,3), RelTol 1e-10, FP64')
+
+
+def starfish_hierarchy(backend):
+    from bsam import ebOptions
+    from bsam.ddm import starfish_problem, starfish_tag
+    from bsam.solve import build_hierarchy
+    prob, aux, g = starfish_problem()
+    opts = ebOptions('BaseCells', 64, 'MaxLevels', 5, 'Indicator', 'fun', 'TagFunction', starfish_tag(g),
+                     'TagBuffer', 2, 'RelTol', 1e-10, 'MaxVCycles', 100, 'Verbose', 0)
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        H = build_hierarchy(prob, opts, backend)
+    return H, opts
+
+
+def load_peaks():
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d['hbm_gbs']), 'measured'
+    return 6800.0, 'fallback'
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
+             'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+             'clocks_event_reasons.sw_power_cap')
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), f'--query-gpu={q}',
+                                          '--format=csv,noheader,nounits', '-lms', '100'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [s.strip() for s in line.split(',')]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unsampled']}
+        sm = [float(r[0]) for r in self.rows if r[0].replace('.', '').isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == 'active'})
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': max(mx) if mx else None,
+                'reasons': reasons, 'samples': len(self.rows)}
+
+
+def cpu_oracle_rate(H, opts, threads, budget_s):
+    """Solves/s of the C oracle on `threads` host threads (bounded sample)."""
+    os.environ['OMP_NUM_THREADS'] = str(threads)
+    from bsam.flat import flatten
+    from bsam_oracle import OracleHier
+    fl = flatten(H)
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        oh = OracleHier(fl, opts)
+        it, hist, rel, vis = oh.solve_cycles(opts.MaxVCycles + 2)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or n >= 50:
+            break
+    return n / el, n, el, it, rel
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU path (C oracle restatement; MATLAB
+    is not installed) on all host threads, same workload and metric."""
+    if rank != 0:
+        return
+    from bsam_oracle import OracleBackend, build as build_oracle
+    build_oracle()
+    H, opts = starfish_hierarchy(OracleBackend())
+    threads = os.cpu_count() or 1
+    os.environ['OMP_NUM_THREADS'] = str(threads)
+    from bsam.flat import flatten
+    from bsam_oracle import OracleHier
+    fl = flatten(H)
+    times = []
+    for s in range(args.warmup + args.steps):
+        oh = OracleHier(fl, opts)
+        t0 = time.perf_counter()
+        it, hist, rel, vis = oh.solve_cycles(opts.MaxVCycles + 2)
+        dt = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(dt)
+    tot = sum(times)
+    value = len(times) / tot
+    line = {'metric': METRIC, 'value': value, 'unit': 'solves/s', 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': 1e3 * tot / len(times), 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+            'impl': 'reference',
+            'config': {'workload': WORKLOAD, 'vcycles': it, 'final_rel': rel},
+            'cpu_baseline': {'value': value, 'unit': 'solves/s', 'cores': threads, 'kind': 'port',
+                             'sample': f'{len(times)} full starfish solves (MATLAB absent: C oracle restatement)'},
+            'e2e': {'value': value, 'unit': 'solves/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='native', choices=['native', 'reference'])
+    ap.add_argument('--cpu-budget', type=float, default=15.0)
+    args = ap.parse_args()
+    rank = int(os.environ.get('RANK', 0))
+    world = int(os.environ.get('WORLD_SIZE', 1))
+    local = int(os.environ.get('LOCAL_RANK', 0))
+    if args.impl == 'reference':
+        return run_reference(args, rank, world)
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    from bsam.build import build_all
+    build_all()
+    from bsam.device import DeviceBackend, DevHier, BSAM_FIELD_Q, BSAM_FIELD_FTRUE, lib, check
+    from bsam.flat import flatten
+    backend = DeviceBackend.get(local)
+    H, opts = starfish_hierarchy(backend)
+    fl = flatten(H)
+    dh = DevHier(backend.ctx, fl, opts)
+    dh.save_state()
+    stream = torch.cuda.ExternalStream(dh.stream(), device=torch.device('cuda', local))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f'cuda:{local}')
+
+    def one_solve():
+        dh.restore_state()
+        return dh.solve_cycles(opts.MaxVCycles + 2)
+
+    # warm-up (builds the V-cycle graph)
+    for _ in range(args.warmup):
+        it, hist, rel, vis = one_solve()
+    assert rel <= 1e-10, rel
+
+    # ---- device-resident timing ------------------------------------------
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    n0 = dh.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for s in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                starts[s].record(stream)
+            it, hist, rel, vis = one_solve()
+            ends[s].record(stream)
+        torch.cuda.synchronize()
+    launches = dh.launch_count() - n0
+    per = np.array([a.elapsed_time(b) for a, b in zip(starts, ends)])
+    total_ms = float(per.sum())
+    if dist:
+        t = torch.tensor([total_ms], device=f'cuda:{local}')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms / 1e3)
+
+    # ---- end to end through the C-ABI with host buffers ---------------------
+    Q0 = torch.from_numpy(fl.Q.copy()).pin_memory().numpy()
+    F0 = torch.from_numpy(fl.FTrue.copy()).pin_memory().numpy()
+    Qout = torch.empty(fl.Q.size, dtype=torch.float64).pin_memory().numpy()
+    hist_bytes = 8 * (opts.MaxVCycles + 2)
+    import ctypes as C
+    L = lib()
+    e2e_ms = []
+    torch.cuda.synchronize()
+    for s in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dh.restore_state()
+        check(L.bsam_set_field(dh.h, BSAM_FIELD_Q, Q0.ctypes.data, Q0.size))
+        check(L.bsam_set_field(dh.h, BSAM_FIELD_FTRUE, F0.ctypes.data, F0.size))
+        it2, hist2, rel2, _ = dh.solve_cycles(opts.MaxVCycles + 2)
+        check(L.bsam_get_field(dh.h, BSAM_FIELD_Q, Qout.ctypes.data, Qout.size))
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    assert rel2 <= 1e-10
+    e2e_total = sum(e2e_ms)
+    if dist:
+        t = torch.tensor([e2e_total], device=f'cuda:{local}')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = world * args.steps / (e2e_total / 1e3)
+
+    # ---- roofline of the smoother -------------------------------------------
+    prof = dh.profile(3)
+    peak, peak_kind = load_peaks()
+    rl = prof['relax']
+    achieved = rl['bytes'] / (rl['ms'] / 1e3) / 1e9
+    per_kind = {k: {'ms_per_cycle': v['ms'] / 3, 'launches_per_cycle': v['launches'] / 3} for k, v in prof.items()}
+
+    if rank == 0:
+        cpu = None
+        try:
+            from bsam_oracle import build as build_oracle
+            build_oracle()
+            rate, n, el, itc, relc = cpu_oracle_rate(H, opts, 1, args.cpu_budget)
+            cpu = {'value': rate, 'unit': 'solves/s', 'cores': 1, 'kind': 'port',
+                   'sample': f'{n} full starfish solves on 1 host thread in {el:.1f} s (C oracle restatement; '
+                             f'MATLAB not installed)'}
+        except Exception as e:  # report, do not hide
+            cpu = {'value': None, 'unit': 'solves/s', 'cores': 0, 'kind': 'port', 'sample': f'failed: {e}'}
+        line = {
+            'metric': METRIC, 'value': value, 'unit': 'solves/s', 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': total_ms / args.steps, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': WORKLOAD, 'parallelism': 'replicas' if world > 1 else 'single',
+                       'l2': 'flushed between solves (256 MiB write)', 'vcycles_per_solve': it,
+                       'final_rel': rel, 'visible_cells': vis, 'stored_cells': int(fl.F.size - 0),
+                       'p50_ms': float(np.percentile(per, 50)), 'p99_ms': float(np.percentile(per, 99)),
+                       'kernels_per_vcycle': dh.kernels_per_vcycle(), 'per_kernel': per_kind},
+            'e2e': {'value': e2e_value, 'unit': 'solves/s',
+                    'h2d_bytes_per_step': int(8 * (Q0.size + F0.size)),
+                    'd2h_bytes_per_step': int(8 * Qout.size + hist_bytes),
+                    'p50_ms': float(np.percentile(e2e_ms, 50)), 'p99_ms': float(np.percentile(e2e_ms, 99))},
+            'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                         'frac': achieved / peak, 'traffic': None, 'peak_kind': peak_kind,
+                         'kernel': 'k_relax (red-black GS colour pass, all levels)',
+                         'bytes_per_launch': rl['bytes'] / max(rl['launches'], 1),
+                         'avg_launch_us': 1e3 * rl['ms'] / max(rl['launches'], 1)},
+            'cpu_baseline': cpu,
+            'gpu_launches': int(launches),
+            'clocks': clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

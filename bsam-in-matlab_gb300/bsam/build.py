@@ -1,0 +1,59 @@
+"""In-tree build of the package's native libraries.
+
+``libbsam_dev.so``  CUDA kernels + C-ABI (nvcc, sm_103a only)
+``libbsam_host.so`` host set-up helpers (gcc)
+
+Both land in ``bsam-in-matlab_gb300/lib/`` and are rebuilt when a source is
+newer than the library.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(PKG, 'csrc')
+LIBDIR = os.path.join(PKG, 'lib')
+REPO = os.path.dirname(PKG)
+INCLUDE = os.path.join(REPO, 'include')
+
+HOST_LIB = os.path.join(LIBDIR, 'libbsam_host.so')
+DEV_LIB = os.path.join(LIBDIR, 'libbsam_dev.so')
+
+DEV_SOURCES = ['bsam_dev.cu']
+NVCC_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a', '-O3', '-lineinfo', '-std=c++17',
+              '--fmad=false', '-Xcompiler', '-fPIC,-ffp-contract=off', '-shared']
+
+
+def _stale(lib, srcs):
+    if not os.path.exists(lib):
+        return True
+    t = os.path.getmtime(lib)
+    return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def build_host(force=False):
+    os.makedirs(LIBDIR, exist_ok=True)
+    src = os.path.join(CSRC, 'bsam_host.c')
+    if force or _stale(HOST_LIB, [src]):
+        subprocess.check_call(['gcc', '-O2', '-ffp-contract=off', '-fno-fast-math', '-fPIC', '-shared',
+                               '-o', HOST_LIB, src, '-lm'])
+    return HOST_LIB
+
+
+def build_dev(force=False, verbose=False):
+    os.makedirs(LIBDIR, exist_ok=True)
+    srcs = [os.path.join(CSRC, s) for s in DEV_SOURCES]
+    deps = srcs + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(('.cuh', '.h'))] + \
+        [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+    if force or _stale(DEV_LIB, deps):
+        cmd = ['nvcc'] + NVCC_FLAGS + ['-I', INCLUDE, '-o', DEV_LIB] + srcs
+        if verbose:
+            cmd.insert(1, '-Xptxas=-v')
+        subprocess.check_call(cmd)
+    return DEV_LIB
+
+
+def build_all(force=False):
+    build_host(force)
+    build_dev(force)

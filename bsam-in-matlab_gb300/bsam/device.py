@@ -1,0 +1,296 @@
+"""ctypes binding of ``libbsam_dev.so`` (the C-ABI of ``include/bsam_dev.h``).
+
+``DeviceBackend`` is what the host drivers call for every numerical step of
+the solve path: the ghost fills and prolongation of hierarchy set-up and
+``ebSolveCycles``.  A hierarchy is uploaded once per structural change
+(``H.version``) and stays resident; after each call the solution, coarse
+shadows and working force are read back into ``H`` so the host keeps the
+reference's value semantics (``H = ebSolveCycles(H)``).
+
+There is no fallback: if the library cannot be built or loaded, or no
+sm_103 device is present, the calls raise ``DeviceError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build import build_dev
+from .flat import flatten, scatter_field, FIELD_Q, FIELD_F, FIELD_QC
+
+P, I32, I64, D = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+
+BSAM_FIELD_Q, BSAM_FIELD_F, BSAM_FIELD_FTRUE, BSAM_FIELD_QC, BSAM_FIELD_CC, BSAM_FIELD_INVDIAG = range(6)
+NKINDS = 9
+KIND_NAMES = ['relax', 'ghost', 'restrict', 'ring', 'coarse_load', 'corrections', 'prolong', 'coarsest', 'residual']
+ERRNAMES = {1: 'arg', 2: 'cuda', 3: 'nomem', 4: 'state', 5: 'nodev'}
+
+
+class DeviceError(RuntimeError):
+    """A C-ABI call failed; ``ident`` mirrors the MEX error id bsam:device:<code>."""
+
+    def __init__(self, code, msg):
+        self.code = code
+        self.ident = f'bsam:device:{ERRNAMES.get(code, code)}'
+        super().__init__(f'{self.ident}: {msg}')
+
+
+class HierDesc(C.Structure):
+    _fields_ = [('nlev', I32), ('root_idx', I32), ('npatch', I32),
+                ('levels', P), ('hs', P), ('patches', P),
+                ('Q', P), ('F', P), ('FTrue', P), ('QC', P), ('CC', P), ('InvDiagS', P), ('DeW', P), ('DnS', P),
+                ('bcg', P), ('cfd', P), ('pcoef', P), ('covered', P),
+                ('same', P), ('ring', P), ('win', P), ('fp', P), ('corr', P),
+                ('Ainv', P), ('bcRhs', P),
+                ('n_q', I64), ('n_cells', I64), ('n_dew', I64), ('n_dns', I64), ('n_qc', I64), ('n_bcg', I64),
+                ('n_cfd', I64), ('n_pcoef', I64), ('n_same', I64), ('n_ring', I64), ('n_win', I64), ('n_fp', I64),
+                ('n_corr', I64),
+                ('ncoarse', I32), ('singular', I32)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [('npre', I32), ('npost', I32), ('omega', D), ('ghost_interp', I32), ('mass_correction', I32),
+                ('max_vcycles', I32), ('rel_tol', D), ('precision', I32)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_dev()
+        L = C.CDLL(path)
+        L.bsam_last_error.restype = C.c_char_p
+        L.bsam_ctx_create.argtypes = [C.c_int, C.POINTER(P)]
+        L.bsam_ctx_destroy.argtypes = [P]
+        L.bsam_hier_upload.argtypes = [P, C.POINTER(HierDesc), C.POINTER(SolveOpts), C.POINTER(P)]
+        L.bsam_hier_free.argtypes = [P]
+        L.bsam_set_opts.argtypes = [P, C.POINTER(SolveOpts)]
+        L.bsam_set_field.argtypes = [P, C.c_int, P, I64]
+        L.bsam_get_field.argtypes = [P, C.c_int, P, I64]
+        L.bsam_fill_ghosts.argtypes = [P, C.c_int]
+        L.bsam_prolong_level.argtypes = [P, C.c_int]
+        L.bsam_solve_cycles.argtypes = [P, P, C.c_int, C.POINTER(C.c_int), C.POINTER(D), C.POINTER(I64)]
+        L.bsam_vcycle.argtypes = [P]
+        L.bsam_comp_residual.argtypes = [P, P]
+        L.bsam_composite_mean.argtypes = [P, C.POINTER(D), C.POINTER(D)]
+        L.bsam_mass_check.argtypes = [P, P]
+        L.bsam_stream.argtypes = [P, C.POINTER(P)]
+        L.bsam_profile_vcycles.argtypes = [P, C.c_int, P, P, P]
+        L.bsam_kernels_per_vcycle.argtypes = [P, C.POINTER(I64)]
+        L.bsam_save_state.argtypes = [P]
+        L.bsam_restore_state.argtypes = [P]
+        L.bsam_launch_count.argtypes = [P, C.POINTER(I64)]
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != 0:
+        raise DeviceError(rc, lib().bsam_last_error().decode(errors='replace'))
+
+
+def solve_opts(opts):
+    return SolveOpts(int(opts['NPre']), int(opts['NPost']), float(opts['Omega']),
+                     0 if str(opts['GhostInterp']).lower() == 'qif' else 1, int(bool(opts['MassCorrection'])),
+                     int(opts['MaxVCycles']), float(opts['RelTol']),
+                     1 if str(opts.get('Precision', 'fp64')).lower() == 'mixed' else 0)
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None and a.size else None
+
+
+def make_desc(fl, keep):
+    """Fill a HierDesc from a Flat (``keep`` collects arrays to hold alive)."""
+    def arr(a, dt):
+        a = np.ascontiguousarray(a, dtype=dt)
+        keep.append(a)
+        return _ptr(a)
+    d = HierDesc()
+    d.nlev, d.root_idx, d.npatch = fl.nlev, fl.rootIdx, fl.npatch
+    d.levels, d.hs, d.patches = arr(fl.levels, np.int32), arr(fl.hs, np.float64), arr(fl.patches, np.int32)
+    for name in ('Q', 'F', 'FTrue', 'QC', 'CC', 'InvDiagS', 'DeW', 'DnS', 'bcg', 'cfd', 'pcoef'):
+        setattr(d, name, arr(getattr(fl, name), np.float64))
+    d.covered = arr(fl.covered, np.uint8)
+    for name in ('same', 'ring', 'win', 'fp', 'corr'):
+        setattr(d, name, arr(getattr(fl, name), np.int32))
+    d.Ainv, d.bcRhs = arr(fl.Ainv, np.float64), arr(fl.bcRhs, np.float64)
+    d.n_q, d.n_cells, d.n_dew, d.n_dns = fl.Q.size, fl.F.size, fl.DeW.size, fl.DnS.size
+    d.n_qc, d.n_bcg, d.n_cfd, d.n_pcoef = fl.QC.size, fl.bcg.size, fl.cfd.size, fl.pcoef.size
+    d.n_same, d.n_ring, d.n_win = fl.same.shape[0], fl.ring.shape[0], fl.win.size
+    d.n_fp, d.n_corr = fl.fp.shape[0], fl.corr.size
+    d.ncoarse, d.singular = int(fl.bcRhs.size), int(fl.singular)
+    return d
+
+
+class Context:
+    def __init__(self, device=0):
+        self.device = device
+        h = P()
+        check(lib().bsam_ctx_create(int(device), C.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        try:
+            lib().bsam_ctx_destroy(self.h)
+        except Exception:
+            pass
+
+
+class DevHier:
+    """One uploaded hierarchy (device-resident)."""
+
+    def __init__(self, ctx, fl, opts):
+        self.ctx = ctx
+        self.fl = fl
+        keep = []
+        desc = make_desc(fl, keep)
+        self.opts = solve_opts(opts)
+        h = P()
+        check(lib().bsam_hier_upload(ctx.h, C.byref(desc), C.byref(self.opts), C.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        try:
+            lib().bsam_hier_free(self.h)
+        except Exception:
+            pass
+
+    def set_opts(self, opts):
+        self.opts = solve_opts(opts)
+        check(lib().bsam_set_opts(self.h, C.byref(self.opts)))
+
+    def get(self, which, n):
+        out = np.empty(n)
+        check(lib().bsam_get_field(self.h, which, _ptr(out), n))
+        return out
+
+    def set(self, which, arr):
+        arr = np.ascontiguousarray(arr, dtype=np.float64)
+        check(lib().bsam_set_field(self.h, which, _ptr(arr), arr.size))
+
+    def fill(self, k):
+        check(lib().bsam_fill_ghosts(self.h, int(k)))
+
+    def prolong(self, k):
+        check(lib().bsam_prolong_level(self.h, int(k)))
+
+    def solve_cycles(self, hist_cap):
+        hist = np.zeros(max(hist_cap, 1))
+        it = C.c_int(0)
+        rel = D(0)
+        vis = I64(0)
+        check(lib().bsam_solve_cycles(self.h, _ptr(hist), hist.size, C.byref(it), C.byref(rel), C.byref(vis)))
+        return it.value, hist[:it.value + 1].copy(), rel.value, vis.value
+
+    def vcycle(self):
+        check(lib().bsam_vcycle(self.h))
+
+    def residual(self):
+        out = np.zeros(5)
+        check(lib().bsam_comp_residual(self.h, _ptr(out)))
+        return {'linf': out[0], 'l2': out[1], 'fnorm': out[2], 'rel': out[3], 'ncell': int(out[4])}
+
+    def mass_check(self):
+        out = np.zeros(4)
+        check(lib().bsam_mass_check(self.h, _ptr(out)))
+        return {'lhs': out[0], 'flux': out[1], 'defect': out[2], 'rel': out[3]}
+
+    def composite_mean(self):
+        m, a = D(0), D(0)
+        check(lib().bsam_composite_mean(self.h, C.byref(m), C.byref(a)))
+        return m.value, a.value
+
+    def stream(self):
+        s = P()
+        check(lib().bsam_stream(self.h, C.byref(s)))
+        return s.value
+
+    def profile(self, ncycles):
+        ms = np.zeros(NKINDS)
+        nl = np.zeros(NKINDS, dtype=np.int64)
+        by = np.zeros(NKINDS)
+        check(lib().bsam_profile_vcycles(self.h, int(ncycles), _ptr(ms), _ptr(nl), _ptr(by)))
+        return {KIND_NAMES[i]: {'ms': ms[i], 'launches': int(nl[i]), 'bytes': by[i]} for i in range(NKINDS)}
+
+    def save_state(self):
+        check(lib().bsam_save_state(self.h))
+
+    def restore_state(self):
+        check(lib().bsam_restore_state(self.h))
+
+    def launch_count(self):
+        n = I64(0)
+        check(lib().bsam_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def kernels_per_vcycle(self):
+        n = I64(0)
+        check(lib().bsam_kernels_per_vcycle(self.h, C.byref(n)))
+        return n.value
+
+
+class DeviceBackend:
+    """Backend of the host drivers: every numerical step runs on the GPU."""
+
+    name = 'device'
+    _instances = {}
+
+    @classmethod
+    def get(cls, device=0):
+        if device not in cls._instances:
+            cls._instances[device] = cls(device)
+        return cls._instances[device]
+
+    def __init__(self, device=0):
+        self.ctx = Context(device)
+
+    def ensure(self, H):
+        cur = getattr(H, '_dev', None)
+        if cur is not None and cur[0] == H.version and cur[1].ctx is self.ctx:
+            dh = cur[1]
+            dh.set_opts(H.opts)
+            return dh
+        fl = flatten(H)
+        dh = DevHier(self.ctx, fl, H.opts)
+        H._dev = (H.version, dh)
+        return dh
+
+    def _writeback(self, H, dh):
+        fl = dh.fl
+        scatter_field(H, fl, FIELD_Q, dh.get(BSAM_FIELD_Q, fl.Q.size))
+        scatter_field(H, fl, FIELD_QC, dh.get(BSAM_FIELD_QC, fl.QC.size))
+        scatter_field(H, fl, FIELD_F, dh.get(BSAM_FIELD_F, fl.F.size))
+
+    def run(self, H, ops):
+        dh = self.ensure(H)
+        for op in ops:
+            if op[0] == 'fill':
+                dh.fill(op[1])
+            elif op[0] == 'prolong':
+                dh.prolong(op[1])
+            else:
+                raise ValueError(op)
+        self._writeback(H, dh)
+
+    def solve_cycles(self, H):
+        dh = self.ensure(H)
+        out = dh.solve_cycles(int(H.opts.MaxVCycles) + 2)
+        self._writeback(H, dh)
+        return out
+
+    def residual(self, H):
+        dh = self.ensure(H)
+        res = dh.residual()
+        self._writeback(H, dh)
+        return res
+
+    def mass_check(self, H):
+        return self.ensure(H).mass_check()
+
+    def composite_mean(self, H):
+        return self.ensure(H).composite_mean()

@@ -1,0 +1,45 @@
+"""ctypes access to ``libbsam_host.so`` (set-up helpers, see csrc/bsam_host.c)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .build import build_host
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(build_host())
+        P, I64 = C.c_void_p, C.c_int64
+        for fn in ('exp', 'tanh', 'cosh', 'sin', 'cos', 'sqrt'):
+            getattr(L, 'bsam_v' + fn).argtypes = [P, P, I64]
+        L.bsam_vatan2.argtypes = [P, P, P, I64]
+        L.bsam_vhypot.argtypes = [P, P, P, I64]
+        L.bsam_starfish_new.restype = P
+        L.bsam_starfish_new.argtypes = [C.c_int] + [C.c_double] * 5
+        L.bsam_starfish_free.argtypes = [P]
+        L.bsam_starfish_nvert.restype = C.c_int
+        L.bsam_starfish_nvert.argtypes = [P]
+        L.bsam_starfish_vertices.argtypes = [P, P]
+        L.bsam_starfish_distance.argtypes = [P, P, P, P, I64]
+        _lib = L
+    return _lib
+
+
+def _v1(name, x):
+    x = np.asarray(x, dtype=np.float64)
+    xc = np.ascontiguousarray(x.ravel(order='F'))
+    y = np.empty_like(xc)
+    getattr(lib(), 'bsam_v' + name)(xc.ctypes.data, y.ctypes.data, xc.size)
+    return y.reshape(x.shape, order='F') if x.ndim else float(y[0])
+
+
+def exp(x): return _v1('exp', x)
+def tanh(x): return _v1('tanh', x)
+def cosh(x): return _v1('cosh', x)
+def sin(x): return _v1('sin', x)
+def cos(x): return _v1('cos', x)

@@ -1,0 +1,1160 @@
+// bsam_dev.cu -- C-ABI, hierarchy residency and launch sequencing of the
+// GB300 solve path (include/bsam_dev.h).
+//
+// Upload turns the reference-structured flat tables into an execution plan:
+//   * per level, work decompositions over colour cells, cells and coarse
+//     cells (256-item blocks, several small patches per block);
+//   * per level, a ghost program: one final rule per ghost cell resolved from
+//     the three ordered stages of ebFillGhosts, plus the QC ring refresh;
+//   * per fine level, the flux corrections in gather form (CSR over target
+//     coarse cells, contributions in the reference's order);
+//   * residual reduction slots and the coarsest inverse.
+// One V-cycle + fill-down + residual is a fixed launch sequence, captured
+// once into a CUDA graph per hierarchy and replayed each cycle.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "bsam_dev.h"
+#include "kernels.cuh"
+
+using namespace bsam;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(e == cudaErrorMemoryAllocation ? BSAM_ERR_NOMEM : BSAM_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(x)                                     \
+  do {                                            \
+    cudaError_t e_ = (x);                         \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #x); \
+  } while (0)
+
+// flat.py column layouts
+enum { LD_N0, LD_N1, LD_P0, LD_P1, LD_CELL0, LD_CELL1, LD_Q0, LD_Q1, LDN };
+enum {
+  PD_LEVEL, PD_ILO, PD_IHI, PD_JLO, PD_JHI, PD_MX, PD_MY, PD_PAR0,
+  PD_BCW, PD_BCE, PD_BCS, PD_BCN, PD_FIW, PD_FIE, PD_FIS, PD_FIN,
+  PD_CCSW, PD_CCSE, PD_CCNW, PD_CCNE,
+  PD_QOFF, PD_COFF, PD_DEWOFF, PD_DNSOFF, PD_QCOFF, PD_BCGOFF, PD_CFDOFF, PD_PCOFF,
+  PD_SAME0, PD_SAME1, PD_RING0, PD_RING1, PD_WIN0, PD_FP0, PD_CORR0, PD_PARENT, PDN
+};
+
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  int alloc(size_t count) {
+    n = count;
+    if (count == 0) return BSAM_OK;
+    CK(cudaMalloc(&p, sizeof(T) * count));
+    return BSAM_OK;
+  }
+  int upload(const T *h, size_t count, cudaStream_t s) {
+    int rc = alloc(count);
+    if (rc) return rc;
+    if (count) CK(cudaMemcpyAsync(p, h, sizeof(T) * count, cudaMemcpyHostToDevice, s));
+    return BSAM_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+bool is_pow2(double x) {
+  int e;
+  return x > 0 && std::frexp(x, &e) == 0.5;
+}
+
+struct DecompH {
+  int beg_off = 0, blk_off = 0, n = 0, nblocks = 0;
+};
+
+struct LevelPlan {
+  int k = 0, p0 = 0, p1 = 0;  // global patch range
+  double hx = 0, hy = 0;
+  bool pow2 = false;
+  DecompH col, cell, coarse;
+  int g1_off = 0, g1_n = 0, g2_off = 0, g2_n = 0;
+  int ring_off = 0, ring_n = 0;
+  // corrections contributed by this (fine) level, targets in level k-1
+  int ct_off = 0, ct_n = 0;
+  // residual slots of this level (k >= root): main blocks then target blocks
+  int res_slot = 0, res_main_blocks = 0, res_tgt_blocks = 0;
+  int64_t ncells = 0;
+};
+
+}  // namespace
+
+struct bsam_ctx_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+};
+
+struct bsam_hier_s {
+  bsam_ctx ctx = nullptr;
+  cudaStream_t stream = nullptr;
+  int nlev = 0, root = 0, npatch = 0;
+  bsam_solve_opts opts{};
+  std::vector<int32_t> hpatches;  // host copy of the descriptor table
+  std::vector<int32_t> hlevels;
+  std::vector<double> hs;
+  std::vector<LevelPlan> lev;     // index 1..nlev
+  int64_t n_q = 0, n_cells = 0, n_qc = 0;
+  int64_t ncell_visible = 0;
+  int ncoarse = 0, n1 = 0, coarse_c_off = 0, coarse_q_off = 0;
+  // device arrays
+  DBuf<double> Q, F, FTrue, QC, CC, ID, DeW, DnS, bcg, cfd, pcoef, Ainv, bcRhs, slots, area, partials;
+  DBuf<uint8_t> flags;
+  DBuf<int> win, fp, ring, ints, ct_cell, ct_patch, ct_beg, ct_item, ct_j, level_slot0;
+  DBuf<int8_t> g_type;
+  DBuf<int> g_dst, g_a, g_b, g_c, g_d, g_e;
+  DBuf<PatchD> patches;
+  DBuf<ResAcc> acc;
+  ResAcc *acc_host = nullptr;  // pinned
+  int nslots = 0, nres_levels = 0, npartials = 0;
+  // graph of one V-cycle + fill-down + residual
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int64_t kernels_per_cycle = 0;
+  // profiling
+  bool profiling = false;
+  struct Rec { int kind; cudaEvent_t a, b; double bytes; };
+  std::vector<Rec> recs;
+  int64_t launch_count = 0;
+  int64_t graph_launches = 0;
+  DBuf<double> saveQ, saveQC, saveF;
+};
+
+namespace {
+
+Fields fields(bsam_hier h) {
+  Fields f;
+  f.Q = h->Q.p; f.F = h->F.p; f.QC = h->QC.p;
+  f.FTrue = h->FTrue.p; f.CC = h->CC.p; f.ID = h->ID.p; f.DeW = h->DeW.p; f.DnS = h->DnS.p;
+  f.bcg = h->bcg.p; f.cfd = h->cfd.p; f.pcoef = h->pcoef.p; f.flags = h->flags.p;
+  f.win = h->win.p; f.fp = h->fp.p;
+  return f;
+}
+
+LevelD leveld(bsam_hier h, int k) {
+  const LevelPlan &L = h->lev[k];
+  LevelD d;
+  d.patches = h->patches.p + L.p0;
+  d.hx = L.hx; d.hy = L.hy;
+  d.hx2 = L.hx * L.hx; d.hy2 = L.hy * L.hy;
+  d.ihx2 = 1.0 / d.hx2; d.ihy2 = 1.0 / d.hy2;
+  return d;
+}
+
+Decomp decomp(bsam_hier h, const DecompH &D) {
+  Decomp d;
+  d.beg = h->ints.p + D.beg_off;
+  d.blk_p0 = h->ints.p + D.blk_off;
+  d.n = D.n;
+  d.nblocks = D.nblocks;
+  return d;
+}
+
+inline int nblk(int n) { return (n + kBlock - 1) / kBlock; }
+
+// launch bookkeeping: optional per-kernel CUDA events for profiling
+struct Launch {
+  bsam_hier h;
+  int kind;
+  double bytes;
+  cudaEvent_t a = nullptr, b = nullptr;
+  Launch(bsam_hier h_, int kind_, double bytes_) : h(h_), kind(kind_), bytes(bytes_) {
+    h->launch_count++;
+    if (h->profiling) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, h->stream);
+    }
+  }
+  ~Launch() {
+    if (h->profiling) {
+      cudaEventRecord(b, h->stream);
+      h->recs.push_back({kind, a, b, bytes});
+    }
+  }
+};
+
+enum { K_RELAX, K_GHOST, K_RESTRICT, K_RING, K_LOAD, K_CORR, K_PROLONG, K_COARSEST, K_RESID };
+
+// ---------------------------------------------------------------------------
+void launch_fill(bsam_hier h, int k) {
+  const LevelPlan &L = h->lev[k];
+  GhostItems G{h->g_type.p, h->g_dst.p, h->g_a.p, h->g_b.p, h->g_c.p, h->g_d.p, h->g_e.p};
+  if (L.g1_n) {
+    Launch l(h, K_GHOST, 0);
+    k_ghost<<<nblk(L.g1_n), kBlock, 0, h->stream>>>(G, L.g1_off, L.g1_n, h->Q.p, h->QC.p, h->bcg.p, L.hx, L.hy);
+  }
+  if (L.g2_n) {
+    Launch l(h, K_GHOST, 0);
+    k_ghost<<<nblk(L.g2_n), kBlock, 0, h->stream>>>(G, L.g2_off, L.g2_n, h->Q.p, h->QC.p, h->bcg.p, L.hx, L.hy);
+  }
+}
+
+void launch_relax(bsam_hier h, int k, int nsweeps) {
+  const LevelPlan &L = h->lev[k];
+  Fields f = fields(h);
+  LevelD ld = leveld(h, k);
+  Decomp D = decomp(h, L.col);
+  for (int s = 0; s < nsweeps; ++s)
+    for (int m = 0; m < 2; ++m) {
+      {
+        Launch l(h, K_RELAX, 24.0 * (double)L.ncells);
+        if (L.pow2)
+          k_relax<true><<<D.nblocks, kBlock, 0, h->stream>>>(ld, D, f, m, h->opts.omega);
+        else
+          k_relax<false><<<D.nblocks, kBlock, 0, h->stream>>>(ld, D, f, m, h->opts.omega);
+      }
+      launch_fill(h, k);
+    }
+}
+
+void launch_restrict(bsam_hier h, int k, int to_parent) {
+  const LevelPlan &L = h->lev[k];
+  Decomp D = decomp(h, L.coarse);
+  Launch l(h, K_RESTRICT, 12.0 * (double)L.ncells);
+  k_restrict<<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), D, fields(h), to_parent);
+}
+
+void launch_ring(bsam_hier h, int k) {
+  const LevelPlan &L = h->lev[k];
+  if (!L.ring_n) return;
+  Launch l(h, K_RING, 0);
+  k_ring<<<nblk(L.ring_n), kBlock, 0, h->stream>>>(h->ring.p, L.ring_off, L.ring_n, h->Q.p, h->QC.p);
+}
+
+void launch_coarse_load(bsam_hier h, int k) {
+  const LevelPlan &L = h->lev[k];
+  Decomp D = decomp(h, L.coarse);
+  Fields f = fields(h);
+  const bool pow2 = L.pow2 && h->lev[k - 1].pow2;
+  {
+    Launch l(h, K_LOAD, 50.0 * (double)L.ncells);
+    if (pow2)
+      k_coarse_load<true><<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), leveld(h, k - 1), D, f);
+    else
+      k_coarse_load<false><<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), leveld(h, k - 1), D, f);
+  }
+  if (h->opts.mass_correction && L.ct_n) {
+    Launch l(h, K_CORR, 0);
+    const int *tc = h->ct_cell.p + L.ct_off, *tb = h->ct_beg.p + L.ct_off;
+    if (h->lev[k - 1].pow2)
+      k_corr<true><<<nblk(L.ct_n), kBlock, 0, h->stream>>>(leveld(h, k), leveld(h, k - 1), f, tc, tb, h->ct_item.p,
+                                                          h->ct_j.p, L.ct_n);
+    else
+      k_corr<false><<<nblk(L.ct_n), kBlock, 0, h->stream>>>(leveld(h, k), leveld(h, k - 1), f, tc, tb, h->ct_item.p,
+                                                           h->ct_j.p, L.ct_n);
+  }
+}
+
+void launch_prolong(bsam_hier h, int k, int correct) {
+  const LevelPlan &L = h->lev[k];
+  Decomp D = decomp(h, L.coarse);
+  Launch l(h, K_PROLONG, 20.0 * (double)L.ncells);
+  k_prolong<<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), D, fields(h), correct);
+}
+
+void launch_coarsest(bsam_hier h) {
+  {
+    Launch l(h, K_COARSEST, 8.0 * (double)h->ncoarse * h->ncoarse);
+    const int threads = h->ncoarse * 32;
+    k_coarsest<<<nblk(threads), kBlock, 0, h->stream>>>(h->Ainv.p, h->bcRhs.p, fields(h), h->coarse_c_off,
+                                                        h->coarse_q_off, h->n1, h->ncoarse);
+  }
+  launch_fill(h, 1);
+}
+
+void launch_vcycle(bsam_hier h, int k) {
+  if (k == 1) {
+    launch_coarsest(h);
+    return;
+  }
+  launch_relax(h, k, h->opts.npre);
+  launch_restrict(h, k, 1);
+  launch_fill(h, k - 1);
+  launch_ring(h, k);
+  launch_coarse_load(h, k);
+  launch_vcycle(h, k - 1);
+  launch_prolong(h, k, 1);
+  launch_fill(h, k);
+  launch_relax(h, k, h->opts.npost);
+}
+
+void launch_filldown(bsam_hier h) {
+  for (int kk = h->nlev; kk >= 2; --kk) {
+    launch_restrict(h, kk, 1);
+    launch_fill(h, kk - 1);
+  }
+}
+
+void launch_residual(bsam_hier h) {
+  Fields f = fields(h);
+  if (h->opts.mass_correction) {
+    for (int k = std::max(2, h->root + 1); k <= h->nlev; ++k) {
+      launch_ring(h, k);
+      launch_restrict(h, k, 0);
+    }
+  }
+  for (int k = h->root; k <= h->nlev; ++k) {
+    const LevelPlan &L = h->lev[k];
+    Decomp D = decomp(h, L.cell);
+    {
+      Launch l(h, K_RESID, 41.0 * (double)L.ncells);
+      if (L.pow2)
+        k_residual<true><<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), D, f, h->acc.p, h->slots.p + L.res_slot,
+                                                              h->opts.mass_correction);
+      else
+        k_residual<false><<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), D, f, h->acc.p, h->slots.p + L.res_slot,
+                                                               h->opts.mass_correction);
+    }
+    // targets in level k receive the corrections of level k+1
+    if (k < h->nlev && h->opts.mass_correction && h->lev[k + 1].ct_n) {
+      const LevelPlan &Lf = h->lev[k + 1];
+      Launch l(h, K_RESID, 0);
+      double *slot = h->slots.p + L.res_slot + L.res_main_blocks;
+      const int *tc = h->ct_cell.p + Lf.ct_off, *tp = h->ct_patch.p + Lf.ct_off, *tb = h->ct_beg.p + Lf.ct_off;
+      if (L.pow2)
+        k_residual_targets<true><<<nblk(Lf.ct_n), kBlock, 0, h->stream>>>(
+            leveld(h, k + 1), leveld(h, k), h->patches.p + L.p0, f, tc, tp, tb, h->ct_item.p, h->ct_j.p, Lf.ct_n,
+            h->acc.p, slot);
+      else
+        k_residual_targets<false><<<nblk(Lf.ct_n), kBlock, 0, h->stream>>>(
+            leveld(h, k + 1), leveld(h, k), h->patches.p + L.p0, f, tc, tp, tb, h->ct_item.p, h->ct_j.p, Lf.ct_n,
+            h->acc.p, slot);
+    }
+  }
+  {
+    Launch l(h, K_RESID, 0);
+    k_residual_final<<<1, 32, 0, h->stream>>>(h->acc.p, h->slots.p, h->level_slot0.p, h->area.p, h->nres_levels,
+                                               (double)h->ncell_visible);
+  }
+}
+
+// one ebSolveCycles iteration body: F = FTrue, V-cycle, fill-down, residual
+int launch_iteration(bsam_hier h) {
+  CK(cudaMemcpyAsync(h->F.p, h->FTrue.p, sizeof(double) * h->n_cells, cudaMemcpyDeviceToDevice, h->stream));
+  launch_vcycle(h, h->nlev);
+  launch_filldown(h);
+  launch_residual(h);
+  CK(cudaGetLastError());
+  return BSAM_OK;
+}
+
+int build_graph(bsam_hier h) {
+  if (h->gexec) return BSAM_OK;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const int64_t before = h->launch_count;
+  int rc = launch_iteration(h);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  h->kernels_per_cycle = h->launch_count - before;
+  h->graph = g;
+  CK(cudaGraphInstantiate(&h->gexec, g, 0));
+  return BSAM_OK;
+}
+
+void drop_graph(bsam_hier h) {
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  h->gexec = nullptr;
+  h->graph = nullptr;
+}
+
+int read_residual(bsam_hier h, double out[5]) {
+  CK(cudaMemcpyAsync(h->acc_host, h->acc.p, sizeof(ResAcc), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int i = 0; i < 5; ++i) out[i] = h->acc_host->out[i];
+  return BSAM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// plan construction
+struct Builder {
+  bsam_hier h;
+  const bsam_hier_desc *d;
+  std::vector<int> ints;
+  std::vector<int8_t> gt;
+  std::vector<int> gdst, ga, gb, gc, gd, ge;
+
+  const int32_t *P(int p) const { return d->patches + (size_t)p * PDN; }
+
+  DecompH make_decomp(int p0, int p1, int kind) {
+    // kind 0 colour cells, 1 cells, 2 coarse cells
+    DecompH D;
+    D.beg_off = (int)ints.size();
+    int acc = 0;
+    std::vector<int> beg;
+    for (int p = p0; p < p1; ++p) {
+      beg.push_back(acc);
+      const int mx = P(p)[PD_MX], my = P(p)[PD_MY];
+      acc += kind == 0 ? mx * my / 2 : kind == 1 ? mx * my : (mx / 2) * (my / 2);
+    }
+    beg.push_back(acc);
+    ints.insert(ints.end(), beg.begin(), beg.end());
+    D.n = acc;
+    D.nblocks = nblk(acc);
+    D.blk_off = (int)ints.size();
+    int p = 0;
+    for (int b = 0; b < D.nblocks; ++b) {
+      const int g = b * kBlock;
+      while (g >= beg[p + 1]) ++p;
+      ints.push_back(p);
+    }
+    return D;
+  }
+
+  // ghost program of one level: final rule per ghost cell (stages 1-3 of
+  // ebFillGhosts.m in order, later stages overriding), ring refresh items,
+  // physical corners last
+  int ghosts(int k, LevelPlan &L) {
+    std::map<int, size_t> rule;   // dst -> index into tmp
+    struct G { int8_t t; int dst, a, b, c, dd, e; };
+    std::vector<G> tmp, ringi, corners;
+    auto put = [&](G g) {
+      auto it = rule.find(g.dst);
+      if (it == rule.end()) {
+        rule[g.dst] = tmp.size();
+        tmp.push_back(g);
+      } else {
+        tmp[it->second] = g;
+      }
+    };
+    const bool qif = h->opts.ghost_interp == 0;
+    for (int p = L.p0; p < L.p1; ++p) {
+      const int32_t *r = P(p);
+      const int mx = r[PD_MX], my = r[PD_MY], cmx = mx / 2, cmy = my / 2;
+      const int qo = r[PD_QOFF];
+      auto Q = [&](int i, int j) { return qo + (i - 1) + (j - 1) * (mx + 2); };
+      // 1. coarse-fine: ring refresh + ebInterpCf
+      bool any = false;
+      for (int s = 0; s < 4; ++s) any |= (r[PD_FIW + s] != 0) || (r[PD_CCSW + s] == 3);
+      if (k > 1 && any) {
+        std::vector<int> qcsrc((size_t)(cmx + 2) * (cmy + 2), -1);
+        for (int t = r[PD_RING0]; t < r[PD_RING1]; ++t) {
+          const int src = d->ring[2 * t], dst = d->ring[2 * t + 1];
+          const int loc = dst - r[PD_QCOFF];
+          if (loc < 0 || loc >= (int)qcsrc.size()) return fail(BSAM_ERR_ARG, "ring destination outside QC");
+          qcsrc[loc] = src;
+          ringi.push_back({G_RING, dst, src, 0, 0, 0, 0});
+        }
+        bool bad = false;
+        auto QC = [&](int i, int j) {
+          const int v = qcsrc[(i - 1) + (j - 1) * (cmx + 2)];
+          if (v < 0) bad = true;
+          return v;
+        };
+        const int *fint = r + PD_FIW;
+        if (fint[0]) {
+          if (qif) {
+            for (int rho = 3; rho <= my - 1; rho += 2) put({G_QIF, Q(1, rho), Q(3, rho + 2), Q(2, rho + 1), QC(1, (rho + 1) / 2), 0, 0});
+            for (int rho = 4; rho <= my; rho += 2) put({G_QIF, Q(1, rho), Q(3, rho - 2), Q(2, rho - 1), QC(1, (rho + 2) / 2), 0, 0});
+            put({G_QIF_END, Q(1, my + 1), Q(3, my + 1), Q(2, my + 1), QC(1, cmy + 2), QC(1, cmy + 1), QC(1, cmy)});
+            put({G_QIF_END, Q(1, 2), Q(3, 2), Q(2, 2), QC(1, 1), QC(1, 2), QC(1, 3)});
+          } else {
+            for (int rho = 3; rho <= my + 1; rho += 2) put({G_LIF, Q(1, rho), Q(2, rho), Q(2, rho - 1), QC(1, (rho + 1) / 2), 0, 0});
+            for (int rho = 2; rho <= my; rho += 2) put({G_LIF, Q(1, rho), Q(2, rho), Q(2, rho + 1), QC(1, (rho + 2) / 2), 0, 0});
+          }
+        }
+        if (fint[1]) {
+          if (qif) {
+            for (int rho = 3; rho <= my - 1; rho += 2) put({G_QIF, Q(mx + 2, rho), Q(mx, rho + 2), Q(mx + 1, rho + 1), QC(cmx + 2, (rho + 1) / 2), 0, 0});
+            for (int rho = 4; rho <= my; rho += 2) put({G_QIF, Q(mx + 2, rho), Q(mx, rho - 2), Q(mx + 1, rho - 1), QC(cmx + 2, (rho + 2) / 2), 0, 0});
+            put({G_QIF_END, Q(mx + 2, my + 1), Q(mx, my + 1), Q(mx + 1, my + 1), QC(cmx + 2, cmy + 2), QC(cmx + 2, cmy + 1), QC(cmx + 2, cmy)});
+            put({G_QIF_END, Q(mx + 2, 2), Q(mx, 2), Q(mx + 1, 2), QC(cmx + 2, 1), QC(cmx + 2, 2), QC(cmx + 2, 3)});
+          } else {
+            for (int rho = 3; rho <= my + 1; rho += 2) put({G_LIF, Q(mx + 2, rho), Q(mx + 1, rho), Q(mx + 1, rho - 1), QC(cmx + 2, (rho + 1) / 2), 0, 0});
+            for (int rho = 2; rho <= my; rho += 2) put({G_LIF, Q(mx + 2, rho), Q(mx + 1, rho), Q(mx + 1, rho + 1), QC(cmx + 2, (rho + 2) / 2), 0, 0});
+          }
+        }
+        if (fint[2]) {
+          if (qif) {
+            for (int kap = 3; kap <= mx - 1; kap += 2) put({G_QIF, Q(kap, 1), Q(kap + 2, 3), Q(kap + 1, 2), QC((kap + 1) / 2, 1), 0, 0});
+            for (int kap = 4; kap <= mx; kap += 2) put({G_QIF, Q(kap, 1), Q(kap - 2, 3), Q(kap - 1, 2), QC((kap + 2) / 2, 1), 0, 0});
+            put({G_QIF_END, Q(mx + 1, 1), Q(mx + 1, 3), Q(mx + 1, 2), QC(cmx + 2, 1), QC(cmx + 1, 1), QC(cmx, 1)});
+            put({G_QIF_END, Q(2, 1), Q(2, 3), Q(2, 2), QC(1, 1), QC(2, 1), QC(3, 1)});
+          } else {
+            for (int kap = 3; kap <= mx + 1; kap += 2) put({G_LIF, Q(kap, 1), Q(kap, 2), Q(kap - 1, 2), QC((kap + 1) / 2, 1), 0, 0});
+            for (int kap = 2; kap <= mx; kap += 2) put({G_LIF, Q(kap, 1), Q(kap, 2), Q(kap + 1, 2), QC((kap + 2) / 2, 1), 0, 0});
+          }
+        }
+        if (fint[3]) {
+          if (qif) {
+            for (int kap = 3; kap <= mx - 1; kap += 2) put({G_QIF, Q(kap, my + 2), Q(kap + 2, my), Q(kap + 1, my + 1), QC((kap + 1) / 2, cmy + 2), 0, 0});
+            for (int kap = 4; kap <= mx; kap += 2) put({G_QIF, Q(kap, my + 2), Q(kap - 2, my), Q(kap - 1, my + 1), QC((kap + 2) / 2, cmy + 2), 0, 0});
+            put({G_QIF_END, Q(mx + 1, my + 2), Q(mx + 1, my), Q(mx + 1, my + 1), QC(cmx + 2, cmy + 2), QC(cmx + 1, cmy + 2), QC(cmx, cmy + 2)});
+            put({G_QIF_END, Q(2, my + 2), Q(2, my), Q(2, my + 1), QC(1, cmy + 2), QC(2, cmy + 2), QC(3, cmy + 2)});
+          } else {
+            for (int kap = 3; kap <= mx + 1; kap += 2) put({G_LIF, Q(kap, my + 2), Q(kap, my + 1), Q(kap - 1, my + 1), QC((kap + 1) / 2, cmy + 2), 0, 0});
+            for (int kap = 2; kap <= mx; kap += 2) put({G_LIF, Q(kap, my + 2), Q(kap, my + 1), Q(kap + 1, my + 1), QC((kap + 2) / 2, cmy + 2), 0, 0});
+          }
+        }
+        const int8_t ct = qif ? G_QIF : G_LIF_CORNER;
+        if (r[PD_CCSW] == 3) put(qif ? G{ct, Q(1, 1), Q(3, 3), Q(2, 2), QC(1, 1), 0, 0} : G{ct, Q(1, 1), Q(2, 2), 0, QC(1, 1), 0, 0});
+        if (r[PD_CCSE] == 3) put(qif ? G{ct, Q(mx + 2, 1), Q(mx, 3), Q(mx + 1, 2), QC(cmx + 2, 1), 0, 0} : G{ct, Q(mx + 2, 1), Q(mx + 1, 2), 0, QC(cmx + 2, 1), 0, 0});
+        if (r[PD_CCNW] == 3) put(qif ? G{ct, Q(1, my + 2), Q(3, my), Q(2, my + 1), QC(1, cmy + 2), 0, 0} : G{ct, Q(1, my + 2), Q(2, my + 1), 0, QC(1, cmy + 2), 0, 0});
+        if (r[PD_CCNE] == 3) put(qif ? G{ct, Q(mx + 2, my + 2), Q(mx, my), Q(mx + 1, my + 1), QC(cmx + 2, cmy + 2), 0, 0} : G{ct, Q(mx + 2, my + 2), Q(mx + 1, my + 1), 0, QC(cmx + 2, cmy + 2), 0, 0});
+        if (bad) return fail(BSAM_ERR_ARG, "coarse-fine stencil reads a QC cell outside the gathered ring");
+      }
+      // 2. same-level copies
+      for (int t = r[PD_SAME0]; t < r[PD_SAME1]; ++t) put({G_COPY, d->same[2 * t + 1], d->same[2 * t], 0, 0, 0, 0});
+      // 3. physical faces and corners
+      const int go = r[PD_BCGOFF];
+      const int gW = go, gE = go + my, gS = go + 2 * my, gN = go + 2 * my + mx;
+      for (int j = 2; j <= my + 1; ++j) {
+        if (r[PD_BCW] == 1) put({G_DIRICHLET, Q(1, j), Q(2, j), Q(3, j), 0, 0, gW + j - 2});
+        else if (r[PD_BCW] == 2) put({G_NEUMANN, Q(1, j), Q(2, j), 0, 0, 0, gW + j - 2});
+        if (r[PD_BCE] == 1) put({G_DIRICHLET, Q(mx + 2, j), Q(mx + 1, j), Q(mx, j), 0, 0, gE + j - 2});
+        else if (r[PD_BCE] == 2) put({G_NEUMANN, Q(mx + 2, j), Q(mx + 1, j), 0, 0, 0, gE + j - 2});
+      }
+      for (int i = 2; i <= mx + 1; ++i) {
+        if (r[PD_BCS] == 1) put({G_DIRICHLET, Q(i, 1), Q(i, 2), Q(i, 3), 0, 0, gS + i - 2});
+        else if (r[PD_BCS] == 2) put({G_NEUMANN, Q(i, 1), Q(i, 2), 1, 0, 0, gS + i - 2});
+        if (r[PD_BCN] == 1) put({G_DIRICHLET, Q(i, my + 2), Q(i, my + 1), Q(i, my), 0, 0, gN + i - 2});
+        else if (r[PD_BCN] == 2) put({G_NEUMANN, Q(i, my + 2), Q(i, my + 1), 1, 0, 0, gN + i - 2});
+      }
+      if (r[PD_CCSW] == 1) corners.push_back({G_PHYS_CORNER, Q(1, 1), Q(2, 1), Q(1, 2), Q(2, 2), 0, 0});
+      if (r[PD_CCSE] == 1) corners.push_back({G_PHYS_CORNER, Q(mx + 2, 1), Q(mx + 1, 1), Q(mx + 2, 2), Q(mx + 1, 2), 0, 0});
+      if (r[PD_CCNW] == 1) corners.push_back({G_PHYS_CORNER, Q(1, my + 2), Q(2, my + 2), Q(1, my + 1), Q(2, my + 1), 0, 0});
+      if (r[PD_CCNE] == 1) corners.push_back({G_PHYS_CORNER, Q(mx + 2, my + 2), Q(mx + 1, my + 2), Q(mx + 2, my + 1), Q(mx + 1, my + 1), 0, 0});
+    }
+    for (const G &g : corners)
+      if (rule.count(g.dst)) return fail(BSAM_ERR_ARG, "physical corner also written by another ghost stage");
+    auto emit = [&](const std::vector<G> &v) {
+      for (const G &g : v) {
+        gt.push_back(g.t); gdst.push_back(g.dst); ga.push_back(g.a); gb.push_back(g.b);
+        gc.push_back(g.c); gd.push_back(g.dd); ge.push_back(g.e);
+      }
+    };
+    L.g1_off = (int)gt.size();
+    emit(tmp);
+    emit(ringi);
+    L.g1_n = (int)gt.size() - L.g1_off;
+    L.g2_off = (int)gt.size();
+    emit(corners);
+    L.g2_n = (int)gt.size() - L.g2_off;
+    // every index must stay inside Q / QC / bcg
+    for (int i = L.g1_off; i < L.g2_off + L.g2_n; ++i) {
+      const int8_t t = gt[i];
+      auto okq = [&](int v) { return v >= 0 && v < d->n_q; };
+      bool ok = t == G_RING ? (gdst[i] >= 0 && gdst[i] < d->n_qc) : okq(gdst[i]);
+      ok = ok && okq(ga[i]);
+      if (t == G_QIF || t == G_QIF_END || t == G_LIF || t == G_PHYS_CORNER || t == G_DIRICHLET) ok = ok && okq(gb[i]);
+      if (t == G_QIF || t == G_QIF_END || t == G_LIF || t == G_LIF_CORNER || t == G_PHYS_CORNER) ok = ok && okq(gc[i]);
+      if (t == G_QIF_END) ok = ok && okq(gd[i]) && okq(ge[i]);
+      if (t == G_DIRICHLET || t == G_NEUMANN) ok = ok && ge[i] >= 0 && ge[i] < d->n_bcg;
+      if (!ok) return fail(BSAM_ERR_ARG, "ghost rule index out of range at level " + std::to_string(k));
+    }
+    return BSAM_OK;
+  }
+};
+
+int validate(const bsam_hier_desc *d) {
+  if (!d || d->nlev < 1 || d->root_idx < 1 || d->root_idx > d->nlev || d->npatch < 1)
+    return fail(BSAM_ERR_ARG, "bad hierarchy header");
+  if (!d->levels || !d->hs || !d->patches || !d->Q || !d->F || !d->FTrue || !d->CC || !d->InvDiagS || !d->DeW ||
+      !d->DnS || !d->covered || !d->Ainv || !d->bcRhs)
+    return fail(BSAM_ERR_ARG, "missing array");
+  int expect_p = 0;
+  for (int k = 1; k <= d->nlev; ++k) {
+    const int32_t *L = d->levels + (size_t)(k - 1) * LDN;
+    if (L[LD_P0] != expect_p || L[LD_P1] <= L[LD_P0] || L[LD_P1] > d->npatch)
+      return fail(BSAM_ERR_ARG, "level patch ranges must tile the patch table");
+    expect_p = L[LD_P1];
+    if (!(d->hs[2 * (k - 1)] > 0) || !(d->hs[2 * (k - 1) + 1] > 0)) return fail(BSAM_ERR_ARG, "bad cell size");
+  }
+  if (expect_p != d->npatch) return fail(BSAM_ERR_ARG, "patch count mismatch");
+  if (d->levels[LD_P1] - d->levels[LD_P0] != 1) return fail(BSAM_ERR_ARG, "level 1 must be one patch");
+  for (int p = 0; p < d->npatch; ++p) {
+    const int32_t *r = d->patches + (size_t)p * PDN;
+    const int64_t mx = r[PD_MX], my = r[PD_MY];
+    const int k = r[PD_LEVEL];
+    if (k < 1 || k > d->nlev || mx < 2 || my < 2 || (k > 1 && (mx % 2 || my % 2)))
+      return fail(BSAM_ERR_ARG, "bad patch size at patch " + std::to_string(p));
+    auto in = [](int64_t off, int64_t len, int64_t n) { return off >= 0 && off + len <= n; };
+    bool ok = in(r[PD_QOFF], (mx + 2) * (my + 2), d->n_q) && in(r[PD_COFF], mx * my, d->n_cells) &&
+              in(r[PD_DEWOFF], (mx + 1) * my, d->n_dew) && in(r[PD_DNSOFF], mx * (my + 1), d->n_dns) &&
+              in(r[PD_BCGOFF], 2 * (mx + my), d->n_bcg) && in(r[PD_SAME0], r[PD_SAME1] - r[PD_SAME0], d->n_same);
+    if (k > 1) {
+      const int64_t cmx = mx / 2, cmy = my / 2;
+      ok = ok && in(r[PD_QCOFF], (cmx + 2) * (cmy + 2), d->n_qc) && in(r[PD_CFDOFF], 2 * (cmx + cmy), d->n_cfd) &&
+           in(r[PD_PCOFF], (cmx + 1) * cmy + cmx * (cmy + 1) + cmx * cmy, d->n_pcoef) &&
+           in(r[PD_RING0], r[PD_RING1] - r[PD_RING0], d->n_ring) && in(r[PD_WIN0], (cmx + 2) * (cmy + 2), d->n_win) &&
+           in(r[PD_FP0], cmx * cmy, d->n_fp) && in(r[PD_CORR0], 2 * (cmx + cmy), d->n_corr);
+    }
+    for (int s = 0; s < 4; ++s) ok = ok && r[PD_BCW + s] >= 0 && r[PD_BCW + s] <= 2;
+    if (!ok) return fail(BSAM_ERR_ARG, "patch " + std::to_string(p) + ": offsets outside the flat arrays");
+  }
+  for (int64_t t = 0; t < d->n_same; ++t)
+    if (d->same[2 * t] < 0 || d->same[2 * t] >= d->n_q || d->same[2 * t + 1] < 0 || d->same[2 * t + 1] >= d->n_q)
+      return fail(BSAM_ERR_ARG, "same-level table index out of range");
+  for (int64_t t = 0; t < d->n_ring; ++t)
+    if (d->ring[2 * t] < 0 || d->ring[2 * t] >= d->n_q || d->ring[2 * t + 1] < 0 || d->ring[2 * t + 1] >= d->n_qc)
+      return fail(BSAM_ERR_ARG, "ring table index out of range");
+  for (int64_t t = 0; t < d->n_win; ++t)
+    if (d->win[t] < 0 || d->win[t] >= d->n_q) return fail(BSAM_ERR_ARG, "window table index out of range");
+  for (int64_t t = 0; t < d->n_fp; ++t)
+    if (d->fp[2 * t] < 0 || d->fp[2 * t] >= d->n_q || d->fp[2 * t + 1] < 0 || d->fp[2 * t + 1] >= d->n_cells)
+      return fail(BSAM_ERR_ARG, "footprint table index out of range");
+  for (int64_t t = 0; t < d->n_corr; ++t)
+    if (d->corr[t] < -1 || d->corr[t] >= d->n_cells) return fail(BSAM_ERR_ARG, "correction target out of range");
+  const int32_t *r1 = d->patches;
+  if ((int64_t)r1[PD_MX] * r1[PD_MY] != d->ncoarse) return fail(BSAM_ERR_ARG, "coarsest size mismatch");
+  return BSAM_OK;
+}
+
+int do_upload(bsam_hier h, const bsam_hier_desc *d) {
+  int rc = validate(d);
+  if (rc) return rc;
+  cudaStream_t s = h->stream;
+  h->nlev = d->nlev;
+  h->root = d->root_idx;
+  h->npatch = d->npatch;
+  h->hpatches.assign(d->patches, d->patches + (size_t)d->npatch * PDN);
+  h->hlevels.assign(d->levels, d->levels + (size_t)d->nlev * LDN);
+  h->hs.assign(d->hs, d->hs + 2 * d->nlev);
+  h->n_q = d->n_q;
+  h->n_cells = d->n_cells;
+  h->n_qc = d->n_qc;
+  if ((rc = h->Q.upload(d->Q, d->n_q, s)) || (rc = h->F.upload(d->F, d->n_cells, s)) ||
+      (rc = h->FTrue.upload(d->FTrue, d->n_cells, s)) || (rc = h->CC.upload(d->CC, d->n_cells, s)) ||
+      (rc = h->ID.upload(d->InvDiagS, d->n_cells, s)) || (rc = h->DeW.upload(d->DeW, d->n_dew, s)) ||
+      (rc = h->DnS.upload(d->DnS, d->n_dns, s)) || (rc = h->QC.upload(d->QC, d->n_qc, s)) ||
+      (rc = h->bcg.upload(d->bcg, d->n_bcg, s)) || (rc = h->cfd.upload(d->cfd, d->n_cfd, s)) ||
+      (rc = h->pcoef.upload(d->pcoef, d->n_pcoef, s)) || (rc = h->win.upload(d->win, d->n_win, s)) ||
+      (rc = h->fp.upload(d->fp, 2 * d->n_fp, s)) || (rc = h->ring.upload(d->ring, 2 * d->n_ring, s)) ||
+      (rc = h->Ainv.upload(d->Ainv, (size_t)d->ncoarse * d->ncoarse, s)) ||
+      (rc = h->bcRhs.upload(d->bcRhs, d->ncoarse, s)))
+    return rc;
+  // patches
+  std::vector<PatchD> pd(d->npatch);
+  for (int p = 0; p < d->npatch; ++p) {
+    const int32_t *r = d->patches + (size_t)p * PDN;
+    PatchD &q = pd[p];
+    q.mx = r[PD_MX]; q.my = r[PD_MY]; q.par0 = r[PD_PAR0]; q.level = r[PD_LEVEL];
+    q.q_off = r[PD_QOFF]; q.c_off = r[PD_COFF]; q.dew_off = r[PD_DEWOFF]; q.dns_off = r[PD_DNSOFF];
+    q.qc_off = r[PD_QCOFF]; q.bcg_off = r[PD_BCGOFF]; q.cfd_off = r[PD_CFDOFF]; q.pc_off = r[PD_PCOFF];
+    q.win_off = r[PD_WIN0]; q.fp_off = r[PD_FP0]; q.corr_off = r[PD_CORR0]; q.pad = 0;
+    for (int sd = 0; sd < 4; ++sd) q.bc[sd] = r[PD_BCW + sd];
+  }
+  if ((rc = h->patches.upload(pd.data(), pd.size(), s))) return rc;
+  // plan
+  Builder B{h, d};
+  h->lev.assign(d->nlev + 1, LevelPlan());
+  std::vector<uint8_t> flags(d->covered, d->covered + d->n_cells);
+  std::vector<int> ct_cell, ct_patch, ct_beg, ct_item, ct_j;
+  for (int k = 1; k <= d->nlev; ++k) {
+    LevelPlan &L = h->lev[k];
+    const int32_t *lv = d->levels + (size_t)(k - 1) * LDN;
+    L.k = k;
+    L.p0 = lv[LD_P0];
+    L.p1 = lv[LD_P1];
+    L.hx = d->hs[2 * (k - 1)];
+    L.hy = d->hs[2 * (k - 1) + 1];
+    L.pow2 = is_pow2(L.hx * L.hx) && is_pow2(L.hy * L.hy);
+    L.ncells = lv[LD_CELL1] - lv[LD_CELL0];
+    L.col = B.make_decomp(L.p0, L.p1, 0);
+    L.cell = B.make_decomp(L.p0, L.p1, 1);
+    if (k > 1) L.coarse = B.make_decomp(L.p0, L.p1, 2);
+    if (k > 1) {
+      L.ring_off = B.P(L.p0)[PD_RING0];
+      L.ring_n = B.P(L.p1 - 1)[PD_RING1] - L.ring_off;
+    }
+    if ((rc = B.ghosts(k, L))) return rc;
+    // flux corrections of this level's patches, gathered per target cell
+    if (k > 1) {
+      struct It { int cell, item, j; };
+      std::vector<It> items;
+      for (int p = L.p0; p < L.p1; ++p) {
+        const int32_t *r = B.P(p);
+        const int cmx = r[PD_MX] / 2, cmy = r[PD_MY] / 2;
+        int o = r[PD_CORR0];
+        for (int f = 0; f < 4; ++f) {
+          const int nn = f < 2 ? cmy : cmx;
+          for (int j = 0; j < nn; ++j) {
+            const int t = d->corr[o + j];
+            if (t >= 0) items.push_back({t, ((p - L.p0) << 2) | f, j});
+          }
+          o += nn;
+        }
+      }
+      std::stable_sort(items.begin(), items.end(), [](const It &a, const It &b) { return a.cell < b.cell; });
+      const LevelPlan &Lc = h->lev[k - 1];
+      L.ct_off = (int)ct_cell.size();
+      for (size_t i = 0; i < items.size();) {
+        size_t e = i;
+        while (e < items.size() && items[e].cell == items[i].cell) ++e;
+        const int cell = items[i].cell;
+        // owning patch of the target in level k-1
+        int q = -1;
+        for (int pp = Lc.p0; pp < Lc.p1; ++pp) {
+          const int32_t *rq = B.P(pp);
+          if (cell >= rq[PD_COFF] && cell < rq[PD_COFF] + rq[PD_MX] * rq[PD_MY]) { q = pp - Lc.p0; break; }
+        }
+        if (q < 0) return fail(BSAM_ERR_ARG, "correction target is not a cell of the parent level");
+        ct_cell.push_back(cell);
+        ct_patch.push_back(q);
+        ct_beg.push_back((int)ct_item.size());
+        for (size_t t = i; t < e; ++t) {
+          ct_item.push_back(items[t].item);
+          ct_j.push_back(items[t].j);
+        }
+        flags[cell] |= 2;
+        i = e;
+      }
+      L.ct_n = (int)ct_cell.size() - L.ct_off;
+      // sentinel row so that tbeg[t + 1] exists for the level's last target
+      ct_cell.push_back(0);
+      ct_patch.push_back(0);
+      ct_beg.push_back((int)ct_item.size());
+    }
+  }
+  // covered cells of levels >= root are excluded from the norms
+  int64_t nvis = 0;
+  for (int k = d->root_idx; k <= d->nlev; ++k) {
+    const int32_t *lv = d->levels + (size_t)(k - 1) * LDN;
+    for (int c = lv[LD_CELL0]; c < lv[LD_CELL1]; ++c) nvis += (d->covered[c] == 0);
+  }
+  h->ncell_visible = nvis;
+  // residual slots
+  std::vector<int> slot0;
+  std::vector<double> area;
+  int ns = 0;
+  for (int k = d->root_idx; k <= d->nlev; ++k) {
+    LevelPlan &L = h->lev[k];
+    L.res_slot = ns;
+    L.res_main_blocks = L.cell.nblocks;
+    L.res_tgt_blocks = (k < d->nlev) ? nblk(h->lev[k + 1].ct_n) : 0;
+    slot0.push_back(ns);
+    area.push_back(L.hx * L.hy);
+    ns += L.res_main_blocks + L.res_tgt_blocks;
+  }
+  slot0.push_back(ns);
+  h->nslots = ns;
+  h->nres_levels = (int)area.size();
+  if ((rc = h->flags.upload(flags.data(), flags.size(), s)) || (rc = h->ints.upload(B.ints.data(), B.ints.size(), s)) ||
+      (rc = h->g_type.upload(B.gt.data(), B.gt.size(), s)) || (rc = h->g_dst.upload(B.gdst.data(), B.gdst.size(), s)) ||
+      (rc = h->g_a.upload(B.ga.data(), B.ga.size(), s)) || (rc = h->g_b.upload(B.gb.data(), B.gb.size(), s)) ||
+      (rc = h->g_c.upload(B.gc.data(), B.gc.size(), s)) || (rc = h->g_d.upload(B.gd.data(), B.gd.size(), s)) ||
+      (rc = h->g_e.upload(B.ge.data(), B.ge.size(), s)) || (rc = h->ct_cell.upload(ct_cell.data(), ct_cell.size(), s)) ||
+      (rc = h->ct_patch.upload(ct_patch.data(), ct_patch.size(), s)) ||
+      (rc = h->ct_beg.upload(ct_beg.data(), ct_beg.size(), s)) ||
+      (rc = h->ct_item.upload(ct_item.data(), ct_item.size(), s)) || (rc = h->ct_j.upload(ct_j.data(), ct_j.size(), s)) ||
+      (rc = h->level_slot0.upload(slot0.data(), slot0.size(), s)) || (rc = h->area.upload(area.data(), area.size(), s)) ||
+      (rc = h->slots.alloc(std::max(ns, 1))) || (rc = h->acc.alloc(1)))
+    return rc;
+  CK(cudaMemsetAsync(h->acc.p, 0, sizeof(ResAcc), s));
+  // coarsest
+  const int32_t *r1 = d->patches;
+  h->ncoarse = d->ncoarse;
+  h->n1 = r1[PD_MX];
+  h->coarse_c_off = r1[PD_COFF];
+  h->coarse_q_off = r1[PD_QOFF];
+  // partial sums for composite sums
+  int np = 0;
+  for (int k = d->root_idx; k <= d->nlev; ++k) np += h->lev[k].cell.nblocks;
+  h->npartials = np;
+  if ((rc = h->partials.alloc((size_t)4 * std::max(np, 1)))) return rc;
+  if (!h->acc_host) CK(cudaMallocHost(&h->acc_host, sizeof(ResAcc)));
+  CK(cudaStreamSynchronize(s));
+  return BSAM_OK;
+}
+
+void release(bsam_hier h) {
+  drop_graph(h);
+  h->Q.release(); h->F.release(); h->FTrue.release(); h->QC.release(); h->CC.release(); h->ID.release();
+  h->DeW.release(); h->DnS.release(); h->bcg.release(); h->cfd.release(); h->pcoef.release(); h->Ainv.release();
+  h->bcRhs.release(); h->slots.release(); h->area.release(); h->partials.release(); h->flags.release();
+  h->win.release(); h->fp.release(); h->ring.release(); h->ints.release(); h->ct_cell.release();
+  h->ct_patch.release(); h->ct_beg.release(); h->ct_item.release(); h->ct_j.release(); h->level_slot0.release();
+  h->g_type.release(); h->g_dst.release(); h->g_a.release(); h->g_b.release(); h->g_c.release(); h->g_d.release();
+  h->g_e.release(); h->patches.release(); h->acc.release();
+  h->saveQ.release(); h->saveQC.release(); h->saveF.release();
+  if (h->acc_host) cudaFreeHost(h->acc_host);
+  h->acc_host = nullptr;
+}
+
+int check_opts(const bsam_solve_opts *o) {
+  if (!o || o->npre < 0 || o->npost < 0 || o->max_vcycles < 0 || !(o->rel_tol >= 0) || !(o->omega > 0) ||
+      (o->ghost_interp != 0 && o->ghost_interp != 1) || (o->precision != 0 && o->precision != 1))
+    return fail(BSAM_ERR_ARG, "invalid solve options");
+  return BSAM_OK;
+}
+
+int set_device(bsam_hier h) {
+  CK(cudaSetDevice(h->ctx->device));
+  return BSAM_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char *bsam_last_error(void) { return g_err.c_str(); }
+
+int bsam_ctx_create(int device, bsam_ctx *out) {
+  if (!out) return fail(BSAM_ERR_ARG, "null output");
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return fail(BSAM_ERR_NODEV, "no CUDA device available");
+  if (device < 0 || device >= n) return fail(BSAM_ERR_ARG, "device ordinal out of range");
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, device));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(BSAM_ERR_NODEV, std::string("libbsam_dev is built for sm_103a; device is ") + prop.name);
+  CK(cudaSetDevice(device));
+  bsam_ctx c = new bsam_ctx_s;
+  c->device = device;
+  cudaError_t se = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (se != cudaSuccess) {
+    delete c;
+    return cuda_fail(se, "cudaStreamCreate");
+  }
+  *out = c;
+  return BSAM_OK;
+}
+
+int bsam_ctx_destroy(bsam_ctx ctx) {
+  if (!ctx) return BSAM_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return BSAM_OK;
+}
+
+int bsam_hier_upload(bsam_ctx ctx, const bsam_hier_desc *desc, const bsam_solve_opts *opts, bsam_hier *out) {
+  if (!ctx || !out) return fail(BSAM_ERR_ARG, "null argument");
+  int rc = check_opts(opts);
+  if (rc) return rc;
+  bsam_hier h = new bsam_hier_s;
+  h->ctx = ctx;
+  h->stream = ctx->stream;
+  h->opts = *opts;
+  if ((rc = set_device(h)) || (rc = do_upload(h, desc))) {
+    release(h);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return BSAM_OK;
+}
+
+int bsam_hier_free(bsam_hier h) {
+  if (!h) return BSAM_OK;
+  set_device(h);
+  cudaStreamSynchronize(h->stream);
+  release(h);
+  delete h;
+  return BSAM_OK;
+}
+
+int bsam_set_opts(bsam_hier h, const bsam_solve_opts *opts) {
+  if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
+  int rc = check_opts(opts);
+  if (rc) return rc;
+  const bool replan = opts->ghost_interp != h->opts.ghost_interp;
+  if (replan) return fail(BSAM_ERR_STATE, "GhostInterp is fixed at upload; upload the hierarchy again");
+  h->opts = *opts;
+  drop_graph(h);
+  return BSAM_OK;
+}
+
+static DBuf<double> *field_buf(bsam_hier h, int which) {
+  switch (which) {
+    case BSAM_FIELD_Q: return &h->Q;
+    case BSAM_FIELD_F: return &h->F;
+    case BSAM_FIELD_FTRUE: return &h->FTrue;
+    case BSAM_FIELD_QC: return &h->QC;
+    case BSAM_FIELD_CC: return &h->CC;
+    case BSAM_FIELD_INVDIAG: return &h->ID;
+    default: return nullptr;
+  }
+}
+
+int bsam_set_field(bsam_hier h, int which, const double *host, int64_t n) {
+  if (!h || !host) return fail(BSAM_ERR_ARG, "null argument");
+  DBuf<double> *b = field_buf(h, which);
+  if (!b) return fail(BSAM_ERR_ARG, "unknown field");
+  if ((size_t)n != b->n) return fail(BSAM_ERR_ARG, "field length mismatch");
+  int rc = set_device(h);
+  if (rc) return rc;
+  if (n) CK(cudaMemcpyAsync(b->p, host, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
+int bsam_get_field(bsam_hier h, int which, double *host, int64_t n) {
+  if (!h || !host) return fail(BSAM_ERR_ARG, "null argument");
+  DBuf<double> *b = field_buf(h, which);
+  if (!b) return fail(BSAM_ERR_ARG, "unknown field");
+  if ((size_t)n != b->n) return fail(BSAM_ERR_ARG, "field length mismatch");
+  int rc = set_device(h);
+  if (rc) return rc;
+  if (n) CK(cudaMemcpyAsync(host, b->p, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
+int bsam_fill_ghosts(bsam_hier h, int level) {
+  if (!h || level < 1 || level > h->nlev) return fail(BSAM_ERR_ARG, "level out of range");
+  int rc = set_device(h);
+  if (rc) return rc;
+  launch_fill(h, level);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
+int bsam_prolong_level(bsam_hier h, int level) {
+  if (!h || level < 2 || level > h->nlev) return fail(BSAM_ERR_ARG, "level out of range");
+  int rc = set_device(h);
+  if (rc) return rc;
+  launch_prolong(h, level, 0);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
+int bsam_comp_residual(bsam_hier h, double out[5]) {
+  if (!h || !out) return fail(BSAM_ERR_ARG, "null argument");
+  int rc = set_device(h);
+  if (rc) return rc;
+  launch_residual(h);
+  CK(cudaGetLastError());
+  return read_residual(h, out);
+}
+
+int bsam_vcycle(bsam_hier h) {
+  if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
+  int rc = set_device(h);
+  if (rc || (rc = launch_iteration(h))) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
+int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles, double *final_rel,
+                      int64_t *visible_cells) {
+  if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
+  int rc = set_device(h);
+  if (rc) return rc;
+  for (int k = 1; k <= h->nlev; ++k) launch_fill(h, k);
+  launch_residual(h);
+  CK(cudaGetLastError());
+  double res[5];
+  if ((rc = read_residual(h, res))) return rc;
+  int nh = 0;
+  if (res_hist && nh < hist_cap) res_hist[nh] = res[0];
+  ++nh;
+  double rel = res[3];
+  int it = 0;
+  if ((rc = build_graph(h))) return rc;
+  while (it < h->opts.max_vcycles && rel > h->opts.rel_tol) {
+    ++it;
+    CK(cudaGraphLaunch(h->gexec, h->stream));
+    h->graph_launches++;
+    if ((rc = read_residual(h, res))) return rc;
+    if (res_hist && nh < hist_cap) res_hist[nh] = res[0];
+    ++nh;
+    rel = res[3];
+  }
+  if (vcycles) *vcycles = it;
+  if (final_rel) *final_rel = rel;
+  if (visible_cells) *visible_cells = (int64_t)res[4];
+  return BSAM_OK;
+}
+
+int bsam_composite_mean(bsam_hier h, double *mean, double *area) {
+  double out[4];
+  (void)out;
+  if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
+  int rc = set_device(h);
+  if (rc) return rc;
+  Fields f = fields(h);
+  int o = 0;
+  std::vector<int> starts;
+  for (int k = h->root; k <= h->nlev; ++k) {
+    const LevelPlan &L = h->lev[k];
+    Decomp D = decomp(h, L.cell);
+    starts.push_back(o);
+    k_sums<<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), D, f, h->partials.p + 4 * o);
+    o += D.nblocks;
+  }
+  CK(cudaGetLastError());
+  std::vector<double> part((size_t)4 * o);
+  CK(cudaMemcpyAsync(part.data(), h->partials.p, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  double tot = 0, ar = 0;
+  int li = 0;
+  for (int k = h->root; k <= h->nlev; ++k, ++li) {
+    const LevelPlan &L = h->lev[k];
+    const double da = L.hx * L.hy;
+    double su = 0, nv = 0;
+    for (int b = starts[li]; b < starts[li] + L.cell.nblocks; ++b) {
+      su = su + part[4 * b];
+      nv = nv + part[4 * b + 3];
+    }
+    tot = tot + su * da;
+    ar = ar + nv * da;
+  }
+  if (mean) *mean = tot / std::max(ar, 2.2250738585072014e-308);
+  if (area) *area = ar;
+  return BSAM_OK;
+}
+
+int bsam_mass_check(bsam_hier h, double out[4]) {
+  if (!h || !out) return fail(BSAM_ERR_ARG, "null argument");
+  int rc = set_device(h);
+  if (rc) return rc;
+  Fields f = fields(h);
+  int o = 0;
+  std::vector<int> starts;
+  for (int k = h->root; k <= h->nlev; ++k) {
+    const LevelPlan &L = h->lev[k];
+    Decomp D = decomp(h, L.cell);
+    starts.push_back(o);
+    k_sums<<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), D, f, h->partials.p + 4 * o);
+    o += D.nblocks;
+  }
+  CK(cudaGetLastError());
+  std::vector<double> part((size_t)4 * o);
+  CK(cudaMemcpyAsync(part.data(), h->partials.p, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->stream));
+  // boundary flux (perimeter-sized): computed on the host from downloaded
+  // boundary rows of Q, in the reference's loop order
+  std::vector<double> Qh(h->n_q);
+  CK(cudaMemcpyAsync(Qh.data(), h->Q.p, sizeof(double) * h->n_q, cudaMemcpyDeviceToHost, h->stream));
+  std::vector<double> DeWh(h->DeW.n), DnSh(h->DnS.n);
+  std::vector<uint8_t> flh(h->flags.n);
+  CK(cudaMemcpyAsync(DeWh.data(), h->DeW.p, sizeof(double) * DeWh.size(), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(DnSh.data(), h->DnS.p, sizeof(double) * DnSh.size(), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(flh.data(), h->flags.p, flh.size(), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  double lhs = 0, scale = 0, rhs = 0;
+  int li = 0;
+  for (int k = h->root; k <= h->nlev; ++k, ++li) {
+    const LevelPlan &L = h->lev[k];
+    const double da = L.hx * L.hy, hx = L.hx, hy = L.hy;
+    double sm = 0, sa = 0;
+    for (int b = starts[li]; b < starts[li] + L.cell.nblocks; ++b) {
+      sm = sm + part[4 * b + 1];
+      sa = sa + part[4 * b + 2];
+    }
+    lhs = lhs + sm * da;
+    scale = scale + sa * da;
+    for (int p = L.p0; p < L.p1; ++p) {
+      const int32_t *r = h->hpatches.data() + (size_t)p * PDN;
+      const int mx = r[PD_MX], my = r[PD_MY];
+      auto Q = [&](int i, int j) { return Qh[r[PD_QOFF] + (i - 1) + (size_t)(j - 1) * (mx + 2)]; };
+      auto cov = [&](int i, int j) { return flh[r[PD_COFF] + (i - 1) + (size_t)(j - 1) * mx] & 1; };
+      const double *DeW = DeWh.data() + r[PD_DEWOFF], *DnS = DnSh.data() + r[PD_DNSOFF];
+      if (r[PD_BCW] > 0) { double fl = 0; for (int j = 1; j <= my; ++j) if (!cov(1, j)) fl = fl + DeW[(size_t)(j - 1) * (mx + 1)] * (Q(1, j + 1) - Q(2, j + 1)) / hx; rhs = rhs + fl * hy; }
+      if (r[PD_BCE] > 0) { double fl = 0; for (int j = 1; j <= my; ++j) if (!cov(mx, j)) fl = fl + DeW[mx + (size_t)(j - 1) * (mx + 1)] * (Q(mx + 2, j + 1) - Q(mx + 1, j + 1)) / hx; rhs = rhs + fl * hy; }
+      if (r[PD_BCS] > 0) { double fl = 0; for (int i = 1; i <= mx; ++i) if (!cov(i, 1)) fl = fl + DnS[i - 1] * (Q(i + 1, 1) - Q(i + 1, 2)) / hy; rhs = rhs + fl * hx; }
+      if (r[PD_BCN] > 0) { double fl = 0; for (int i = 1; i <= mx; ++i) if (!cov(i, my)) fl = fl + DnS[(i - 1) + (size_t)my * mx] * (Q(i + 1, my + 2) - Q(i + 1, my + 1)) / hy; rhs = rhs + fl * hx; }
+    }
+  }
+  out[0] = lhs;
+  out[1] = rhs;
+  out[2] = lhs - rhs;
+  double m = std::max(std::max(scale, std::fabs(lhs)), std::max(std::fabs(rhs), 2.2250738585072014e-308));
+  out[3] = std::fabs(lhs - rhs) / m;
+  return BSAM_OK;
+}
+
+int bsam_save_state(bsam_hier h) {
+  if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
+  int rc = set_device(h);
+  if (rc) return rc;
+  if (!h->saveQ.p && ((rc = h->saveQ.alloc(h->Q.n)) || (rc = h->saveQC.alloc(h->QC.n)) || (rc = h->saveF.alloc(h->F.n))))
+    return rc;
+  CK(cudaMemcpyAsync(h->saveQ.p, h->Q.p, sizeof(double) * h->Q.n, cudaMemcpyDeviceToDevice, h->stream));
+  if (h->QC.n) CK(cudaMemcpyAsync(h->saveQC.p, h->QC.p, sizeof(double) * h->QC.n, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->saveF.p, h->F.p, sizeof(double) * h->F.n, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
+int bsam_restore_state(bsam_hier h) {
+  if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
+  if (!h->saveQ.p) return fail(BSAM_ERR_STATE, "no saved state");
+  int rc = set_device(h);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(h->Q.p, h->saveQ.p, sizeof(double) * h->Q.n, cudaMemcpyDeviceToDevice, h->stream));
+  if (h->QC.n) CK(cudaMemcpyAsync(h->QC.p, h->saveQC.p, sizeof(double) * h->QC.n, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->F.p, h->saveF.p, sizeof(double) * h->F.n, cudaMemcpyDeviceToDevice, h->stream));
+  return BSAM_OK;
+}
+
+int bsam_launch_count(bsam_hier h, int64_t *count) {
+  if (!h || !count) return fail(BSAM_ERR_ARG, "null argument");
+  *count = h->launch_count + h->graph_launches * h->kernels_per_cycle;
+  return BSAM_OK;
+}
+
+int bsam_stream(bsam_hier h, void **stream) {
+  if (!h || !stream) return fail(BSAM_ERR_ARG, "null argument");
+  *stream = (void *)h->stream;
+  return BSAM_OK;
+}
+
+int bsam_kernels_per_vcycle(bsam_hier h, int64_t *count) {
+  if (!h || !count) return fail(BSAM_ERR_ARG, "null argument");
+  int rc = set_device(h);
+  if (rc || (rc = build_graph(h))) return rc;
+  *count = h->kernels_per_cycle;
+  return BSAM_OK;
+}
+
+int bsam_profile_vcycles(bsam_hier h, int ncycles, double ms[BSAM_NKINDS], int64_t launches[BSAM_NKINDS],
+                         double bytes[BSAM_NKINDS]) {
+  if (!h || !ms || !launches || !bytes || ncycles < 1) return fail(BSAM_ERR_ARG, "bad argument");
+  int rc = set_device(h);
+  if (rc) return rc;
+  for (int i = 0; i < BSAM_NKINDS; ++i) { ms[i] = 0; launches[i] = 0; bytes[i] = 0; }
+  h->profiling = true;
+  h->recs.clear();
+  for (int c = 0; c < ncycles && !rc; ++c) rc = launch_iteration(h);
+  h->profiling = false;
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  for (auto &r : h->recs) {
+    float t = 0;
+    if (e == cudaSuccess && !rc) {
+      cudaEventElapsedTime(&t, r.a, r.b);
+      ms[r.kind] += t;
+      launches[r.kind] += 1;
+      bytes[r.kind] += r.bytes;
+    }
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  h->recs.clear();
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "profile sync");
+  return BSAM_OK;
+}
+
+}  // extern "C"

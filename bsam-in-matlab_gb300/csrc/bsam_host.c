@@ -1,0 +1,171 @@
+/*
+ * bsam_host.c -- host-side helpers for hierarchy set-up (not the solve path).
+ *
+ *  - Vectorised C-library math (exp, tanh, cosh, sin, cos, atan2, hypot,
+ *    sqrt) so coefficient sampling gives the same bits on every host,
+ *    independent of a vector-math library's approximations.
+ *  - The starfish polygon geometry of DiffuseDomainBSAM/src/ddStarfishGeometry.m:
+ *    the radially sampled closed polygon, its bounding-box tree (leaves of
+ *    at most eight segments, midpoint splits), and the exact point-to-
+ *    segment signed distance with the tree pruning of the reference's
+ *    vectorised traversal (right child first; prune when the box distance
+ *    exceeds the current best plus 64 eps).  The sign comes from the
+ *    radial-ray intersection with the enclosing segment.
+ *
+ * Compiled with -ffp-contract=off so the arithmetic is the same on x86-64
+ * and aarch64 hosts.
+ */
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+
+#define VEC1(name, fn) \
+  void bsam_v##name(const double *x, double *y, int64_t n) { for (int64_t i = 0; i < n; ++i) y[i] = fn(x[i]); }
+VEC1(exp, exp)
+VEC1(tanh, tanh)
+VEC1(cosh, cosh)
+VEC1(sin, sin)
+VEC1(cos, cos)
+VEC1(sqrt, sqrt)
+void bsam_vatan2(const double *y, const double *x, double *out, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) out[i] = atan2(y[i], x[i]);
+}
+void bsam_vhypot(const double *x, const double *y, double *out, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) out[i] = hypot(x[i], y[i]);
+}
+
+/* ---------------------------------------------------------------------- */
+typedef struct {
+  double box[4];     /* minx miny maxx maxy */
+  int left, right;   /* 0 = leaf (node ids are 1-based like the reference) */
+  int first, last;   /* segment range, 1-based inclusive */
+} Node;
+
+typedef struct {
+  int ns;            /* number of segments = npoints - 1 */
+  double *a, *e, *len2;  /* a(j,:), e(j,:) interleaved [2*ns]; len2[ns] */
+  double *v;         /* vertices [2*npoints] */
+  Node *nodes;
+  int nnodes, cap;
+} Starfish;
+
+static int build_node(Starfish *g, int first, int last) {
+  if (g->nnodes == g->cap) {
+    g->cap = g->cap ? 2 * g->cap : 256;
+    g->nodes = (Node *)realloc(g->nodes, sizeof(Node) * g->cap);
+  }
+  const int id = ++g->nnodes;  /* 1-based */
+  Node *nd = &g->nodes[id - 1];
+  double mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+  /* box over a(first:last,:) and b(first:last,:) = v(2:end): the vertices */
+  for (int j = first; j <= last; ++j) {
+    const double ax = g->v[2 * (j - 1)], ay = g->v[2 * (j - 1) + 1];
+    const double bx = g->v[2 * j], by = g->v[2 * j + 1];
+    if (ax < mnx) mnx = ax; if (bx < mnx) mnx = bx;
+    if (ay < mny) mny = ay; if (by < mny) mny = by;
+    if (ax > mxx) mxx = ax; if (bx > mxx) mxx = bx;
+    if (ay > mxy) mxy = ay; if (by > mxy) mxy = by;
+  }
+  nd->box[0] = mnx; nd->box[1] = mny; nd->box[2] = mxx; nd->box[3] = mxy;
+  nd->left = nd->right = 0;
+  nd->first = first; nd->last = last;
+  if (last - first > 7) {
+    const int mid = (first + last) / 2;
+    const int l = build_node(g, first, mid);
+    const int r = build_node(g, mid + 1, last);
+    g->nodes[id - 1].left = l;
+    g->nodes[id - 1].right = r;
+  }
+  return id;
+}
+
+/* Polygon of n points with r(theta) = s0*(s1 + s2*sin(k*theta + th0)),
+   theta = linspace(0, 2*pi, n), last vertex = first.  The reference's
+   starfish is s0 = 0.9, s1 = 1.2, s2 = 0.7, k = 5, th0 = 0. */
+void *bsam_starfish_new(int n, double s0, double s1, double s2, double k, double th0) {
+  Starfish *g = (Starfish *)calloc(1, sizeof(Starfish));
+  g->ns = n - 1;
+  g->v = (double *)malloc(sizeof(double) * 2 * n);
+  const double twopi = 2 * M_PI;
+  for (int i = 0; i < n; ++i) {
+    /* linspace(0, 2*pi, n): d1 + (i*(d2-d1))/(n-1), last = d2 */
+    double th = (i == n - 1) ? twopi : ((double)i * twopi) / (double)(n - 1);
+    double arg = (th0 == 0.0) ? k * th : k * th + th0;
+    double r = s0 * (s1 + s2 * sin(arg));
+    g->v[2 * i] = r * cos(th);
+    g->v[2 * i + 1] = r * sin(th);
+  }
+  g->v[2 * (n - 1)] = g->v[0];
+  g->v[2 * (n - 1) + 1] = g->v[1];
+  g->a = (double *)malloc(sizeof(double) * 2 * g->ns);
+  g->e = (double *)malloc(sizeof(double) * 2 * g->ns);
+  g->len2 = (double *)malloc(sizeof(double) * g->ns);
+  for (int j = 0; j < g->ns; ++j) {
+    g->a[2 * j] = g->v[2 * j];
+    g->a[2 * j + 1] = g->v[2 * j + 1];
+    g->e[2 * j] = g->v[2 * (j + 1)] - g->v[2 * j];
+    g->e[2 * j + 1] = g->v[2 * (j + 1) + 1] - g->v[2 * j + 1];
+    g->len2[j] = g->e[2 * j] * g->e[2 * j] + g->e[2 * j + 1] * g->e[2 * j + 1];
+  }
+  build_node(g, 1, g->ns);
+  return g;
+}
+
+void bsam_starfish_free(void *p) {
+  Starfish *g = (Starfish *)p;
+  if (!g) return;
+  free(g->v); free(g->a); free(g->e); free(g->len2); free(g->nodes); free(g);
+}
+
+int bsam_starfish_nvert(void *p) { return ((Starfish *)p)->ns + 1; }
+void bsam_starfish_vertices(void *p, double *out) {
+  Starfish *g = (Starfish *)p;
+  for (int i = 0; i < 2 * (g->ns + 1); ++i) out[i] = g->v[i];
+}
+
+static void visit(const Starfish *g, int id, double x, double y, double *best) {
+  const Node *nd = &g->nodes[id - 1];
+  const double *bb = nd->box;
+  const double dx = fmax(fmax(bb[0] - x, 0.0), x - bb[2]);
+  const double dy = fmax(fmax(bb[1] - y, 0.0), y - bb[3]);
+  if (!(dx * dx + dy * dy <= *best + 64 * DBL_EPSILON)) return;
+  if (nd->left != 0) {
+    visit(g, nd->right, x, y, best);
+    visit(g, nd->left, x, y, best);
+    return;
+  }
+  double local = *best;
+  for (int j = nd->first; j <= nd->last; ++j) {
+    const double ax = g->a[2 * (j - 1)], ay = g->a[2 * (j - 1) + 1];
+    const double ex = g->e[2 * (j - 1)], ey = g->e[2 * (j - 1) + 1];
+    double t = ((x - ax) * ex + (y - ay) * ey) / g->len2[j - 1];
+    t = fmax(0.0, fmin(1.0, t));
+    const double px = (x - ax) - t * ex, py = (y - ay) - t * ey;
+    const double dd = px * px + py * py;
+    local = fmin(local, dd);
+  }
+  *best = local;
+}
+
+/* Signed distance, positive inside (ddStarfishGeometry.m:140-177). */
+void bsam_starfish_distance(void *p, const double *X, const double *Y, double *d, int64_t n) {
+  const Starfish *g = (const Starfish *)p;
+  const double twopi = 2 * M_PI;
+  const int ns = g->ns;
+  for (int64_t i = 0; i < n; ++i) {
+    const double x = X[i], y = Y[i];
+    double ang = atan2(y, x);
+    ang = ang - floor(ang / twopi) * twopi;      /* mod(atan2(y,x), 2*pi) */
+    int seg = (int)floor(ang * ns / twopi) + 1;
+    if (seg > ns) seg = ns;
+    const double ax = g->a[2 * (seg - 1)], ay = g->a[2 * (seg - 1) + 1];
+    double best = (x - ax) * (x - ax) + (y - ay) * (y - ay);
+    visit(g, 1, x, y, &best);
+    const double ux = cos(ang), uy = sin(ang);
+    const double ex = g->e[2 * (seg - 1)], ey = g->e[2 * (seg - 1) + 1];
+    const double radius = (ax * ey - ay * ex) / (ux * ey - uy * ex);
+    const double s = (hypot(x, y) > radius) ? -1.0 : 1.0;
+    d[i] = s * sqrt(best);
+  }
+}

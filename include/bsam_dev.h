@@ -1,0 +1,164 @@
+/*
+ * bsam_dev.h -- C-ABI of libbsam_dev.so, the GB300 (sm_103a) solve path of
+ * the BSAM adaptive FAS V-cycle.
+ *
+ * The reference (BSAM-in-MATLAB) has one hot path, the pure function
+ *     H = ebSolveCycles(H)          EllipticBSAM/src/ebSolveCycles.m:1-80
+ *                                   EllipticBSAMTree/src/ebtSolveCycles.m
+ * called from ebSolve.m:38,41,52, ebtSolve.m:40,43,54 and, once per time
+ * step, ParabolicBSAM/src/ebpSolve.m:50.  A host (the MATLAB MEX gateway,
+ * or the Python mirror in bsam-in-matlab_gb300/bsam) flattens H into the
+ * tables below once per hierarchy change, uploads them, and replaces each
+ * ebSolveCycles call with bsam_solve_cycles.  The arithmetic is IEEE FP64 in
+ * the reference's operation order: results match the reference up to the
+ * coarsest direct solve, whose sparse LU is replaced by a dense inverse.
+ *
+ * Conventions: every call returns BSAM_OK (0) or an error code; the message
+ * of the most recent failure on the calling thread is bsam_last_error().
+ * Arrays are host pointers; field arrays are concatenations of per-patch
+ * column-major arrays (x fastest), exactly the reference's layout.  Levels
+ * are 1-based like the reference's H.lev{k}.  No call allocates on behalf of
+ * the caller beyond what bsam_hier_upload documents.
+ */
+#ifndef BSAM_DEV_H
+#define BSAM_DEV_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes; the MEX gateway maps them to error ids bsam:device:<name> */
+#define BSAM_OK 0
+#define BSAM_ERR_ARG 1      /* invalid argument or malformed table          */
+#define BSAM_ERR_CUDA 2     /* CUDA runtime failure                         */
+#define BSAM_ERR_NOMEM 3    /* device memory exhausted                      */
+#define BSAM_ERR_STATE 4    /* call not valid in the current state          */
+#define BSAM_ERR_NODEV 5    /* no usable sm_103 device                      */
+
+/* fields for bsam_set_field / bsam_get_field */
+#define BSAM_FIELD_Q 0      /* padded solution, all levels                  */
+#define BSAM_FIELD_F 1      /* working force (cells)                        */
+#define BSAM_FIELD_FTRUE 2  /* true source (cells)                          */
+#define BSAM_FIELD_QC 3     /* padded coarse shadows (levels >= 2)          */
+#define BSAM_FIELD_CC 4     /* reaction coefficient (cells)                 */
+#define BSAM_FIELD_INVDIAG 5 /* relaxation diagonal InvDiagS (cells)        */
+
+typedef struct bsam_ctx_s *bsam_ctx;
+typedef struct bsam_hier_s *bsam_hier;
+
+/* Flat hierarchy: the reference's H (ebMakeLevel.m, ebBuildOps.m,
+ * ebtBuildOps.m, ebGatherParentCoeffs.m, ebCoarsest.m) with patch-local
+ * indices made global.  Column layouts of `levels` and `patches` are the
+ * LD_* and PD_* enumerations of bsam-in-matlab_gb300/bsam/flat.py.        */
+typedef struct {
+  int32_t nlev, root_idx, npatch;
+  const int32_t *levels;    /* [nlev][8]  n0 n1 p0 p1 cell0 cell1 q0 q1     */
+  const double *hs;         /* [nlev][2]  hx hy                             */
+  const int32_t *patches;   /* [npatch][36]                                 */
+  const double *Q, *F, *FTrue, *QC, *CC, *InvDiagS, *DeW, *DnS;
+  const double *bcg;        /* boundary data per patch: W(my) E(my) S(mx) N(mx) */
+  const double *cfd;        /* interface D per patch: W(cmy) E(cmy) S(cmx) N(cmx) */
+  const double *pcoef;      /* parent coefficients: PDeW, PDnS, PCC per patch */
+  const uint8_t *covered;   /* 1 = covered by a finer level (cells)         */
+  const int32_t *same;      /* [n_same][2] (src Q, dst Q)                   */
+  const int32_t *ring;      /* [n_ring][2] (src Q, dst QC)                  */
+  const int32_t *win;       /* [n_win] src Q per parent-window cell         */
+  const int32_t *fp;        /* [n_fp][2] (parent Q, parent cell)            */
+  const int32_t *corr;      /* [n_corr] target cell per coarse face or -1   */
+  const double *Ainv;       /* [ncoarse][ncoarse] row-major coarsest inverse */
+  const double *bcRhs;      /* [ncoarse]                                    */
+  int64_t n_q, n_cells, n_dew, n_dns, n_qc, n_bcg, n_cfd, n_pcoef;
+  int64_t n_same, n_ring, n_win, n_fp, n_corr;
+  int32_t ncoarse, singular;
+} bsam_hier_desc;
+
+/* Solver options: ebOptions.m:44-73 names (NPre, NPost, Omega, GhostInterp,
+ * MassCorrection, MaxVCycles, RelTol) plus the precision form.           */
+typedef struct {
+  int32_t npre, npost;
+  double omega;
+  int32_t ghost_interp;     /* 0 = 'qif', 1 = 'lif'                         */
+  int32_t mass_correction;  /* MassCorrection                               */
+  int32_t max_vcycles;
+  double rel_tol;
+  int32_t precision;        /* 0 = fp64 (drop-in), 1 = mixed                */
+} bsam_solve_opts;
+
+/* Context: one device, one stream.  Replaces nothing in the reference (the
+ * MATLAB session); created once by the gateway.                          */
+int bsam_ctx_create(int device, bsam_ctx *out);
+int bsam_ctx_destroy(bsam_ctx ctx);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *bsam_last_error(void);
+
+/* Upload a hierarchy (allocates its device arrays and execution plan).
+ * Replaces the per-call struct copy of ebSolveCycles(H): called after
+ * ebSetup.m:10-69, ebAddLevel.m:6-32 (ebtAddLevel.m), ebpRegrid.m:16-58,
+ * ebpSetTime.m:11-55.  Validates every table index before any copy.     */
+int bsam_hier_upload(bsam_ctx ctx, const bsam_hier_desc *desc, const bsam_solve_opts *opts,
+                     bsam_hier *out);
+int bsam_hier_free(bsam_hier h);
+int bsam_set_opts(bsam_hier h, const bsam_solve_opts *opts);
+
+/* Whole-field copies host <-> device (n = element count, checked). */
+int bsam_set_field(bsam_hier h, int which, const double *host, int64_t n);
+int bsam_get_field(bsam_hier h, int which, double *host, int64_t n);
+
+/* ebFillGhosts(H,k) (EllipticBSAM/src/ebFillGhosts.m:17-94). */
+int bsam_fill_ghosts(bsam_hier h, int level);
+
+/* Initial guess of a new level by bilinear prolongation of the parent
+ * window (ebAddLevel.m:26-31): Q_k interior = prolongBilin(W). */
+int bsam_prolong_level(bsam_hier h, int level);
+
+/* H = ebSolveCycles(H) (ebSolveCycles.m:8-70): ghost fill, residual r_0,
+ * then V-cycles until rel <= RelTol or MaxVCycles.  res_hist receives
+ * vcycles+1 max-norm residuals (up to hist_cap).  The solution stays on the
+ * device; read it with bsam_get_field(BSAM_FIELD_Q). */
+int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles, double *final_rel,
+                      int64_t *visible_cells);
+
+/* One ebVcycle(H, nlev) + ebTransfer(H,0,'filldown') (ebVcycle.m:16-35,
+ * ebTransfer.m:73-79), force reset included (ebSolveCycles.m:30-34). */
+int bsam_vcycle(bsam_hier h);
+
+/* ebCompResidual (ebCompResidual.m:15-85): out = {linf, l2, fnorm, rel, ncell}. */
+int bsam_comp_residual(bsam_hier h, double out[5]);
+
+/* ebCompositeMean (ebCompositeMean.m:4-23) of the solution. */
+int bsam_composite_mean(bsam_hier h, double *mean, double *area);
+
+/* ebMassCheck (ebMassCheck.m:15-66): out = {lhs, flux, defect, rel}. */
+int bsam_mass_check(bsam_hier h, double out[4]);
+
+/* Measurement support (no reference counterpart): the CUDA stream the
+ * hierarchy's kernels run on (a cudaStream_t), and per-kernel device times
+ * of `ncycles` eagerly launched V-cycles, each kernel bracketed by CUDA
+ * events on that stream.  kinds: 0 relax, 1 ghost fill, 2 restrict, 3 ring,
+ * 4 coarse load, 5 flux corrections, 6 prolong-correct, 7 coarsest,
+ * 8 residual; ms[k] = total ms, launches[k], bytes[k] = algorithmic bytes. */
+int bsam_stream(bsam_hier h, void **stream);
+#define BSAM_NKINDS 9
+int bsam_profile_vcycles(bsam_hier h, int ncycles, double ms[BSAM_NKINDS], int64_t launches[BSAM_NKINDS],
+                         double bytes[BSAM_NKINDS]);
+
+/* Device-side snapshot of the solution state (Q, QC, F) and its restore,
+ * so repeated solves of one resident hierarchy start from the same state
+ * without host traffic (no reference counterpart).  restore is stream-
+ * ordered (asynchronous); the first save allocates the snapshot buffers. */
+int bsam_save_state(bsam_hier h);
+int bsam_restore_state(bsam_hier h);
+
+/* Kernels launched on this hierarchy so far (eager and graph-replayed). */
+int bsam_launch_count(bsam_hier h, int64_t *count);
+
+/* Number of kernels one V-cycle (+ fill-down + residual) launches. */
+int bsam_kernels_per_vcycle(bsam_hier h, int64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BSAM_DEV_H */

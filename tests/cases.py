@@ -1,0 +1,65 @@
+"""Problem definitions shared by the tests (the reference's own cases)."""
+import numpy as np
+
+from bsam import ebProblem
+
+
+def config1_problem(tree=False):
+    """README elliptic example (README.md: -Laplace(u) + u = f, Dirichlet 0)."""
+    u = lambda x, y: np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y)
+    f = lambda x, y: (1 + 8 * np.pi ** 2) * u(x, y)
+    return ebProblem([0, 1, 0, 1], 1, 1, f, ('dirichlet', 0), u)
+
+
+def vardc_problem():
+    """mmsCases('vardc') (EllipticBSAM/tests/mmsCases.m:4-16)."""
+    uex = lambda x, y: np.sin(np.pi * x) * np.cos(np.pi * y)
+    D = lambda x, y: 1 + 0.5 * np.sin(2 * np.pi * x) * np.cos(np.pi * y)
+    C = lambda x, y: 1 + x * y
+    Dx = lambda x, y: np.pi * np.cos(2 * np.pi * x) * np.cos(np.pi * y)
+    Dy = lambda x, y: -0.5 * np.pi * np.sin(2 * np.pi * x) * np.sin(np.pi * y)
+    ux = lambda x, y: np.pi * np.cos(np.pi * x) * np.cos(np.pi * y)
+    uy = lambda x, y: -np.pi * np.sin(np.pi * x) * np.sin(np.pi * y)
+    lap = lambda x, y: -2 * np.pi ** 2 * uex(x, y)
+    f = lambda x, y: -(Dx(x, y) * ux(x, y) + Dy(x, y) * uy(x, y) + D(x, y) * lap(x, y)) + C(x, y) * uex(x, y)
+    return ebProblem([0, 1, 0, 1], D, C, f, ('dirichlet', uex), uex)
+
+
+def pureneumann_problem():
+    """mmsCases('pureneumann') (EllipticBSAM/tests/mmsCases.m:18-22)."""
+    uex = lambda x, y: np.cos(2 * np.pi * x) * np.cos(2 * np.pi * y)
+    f = lambda x, y: 8 * np.pi ** 2 * uex(x, y)
+    return ebProblem([0, 1, 0, 1], 1, 0, f, ('neumann', 0), uex)
+
+
+def gauss51_problem():
+    """mmsCases('gauss51') (EllipticBSAM/tests/mmsCases.m:24-32): u - lap u = f,
+    homogeneous Neumann on (-0.25, 0.25)^2."""
+    from bsam import hostlib
+    sg = 0.25
+    gp = lambda t: -np.pi * np.sin(4 * np.pi * t) / sg ** 2
+    gpp = lambda t: -4 * np.pi ** 2 * np.cos(4 * np.pi * t) / sg ** 2
+    uex = lambda x, y: hostlib.exp(-(np.sin(2 * np.pi * x) ** 2 + np.sin(2 * np.pi * y) ** 2) / (2 * sg ** 2))
+    f = lambda x, y: uex(x, y) * (1 - (gpp(x) + gp(x) ** 2 + gpp(y) + gp(y) ** 2))
+    return ebProblem([-0.25, 0.25, -0.25, 0.25], 1, 1, f, ('neumann', 0), uex)
+
+
+def box_in_box_tag(X, Y, L):
+    """T3 tag function (EllipticBSAM/tests/runAllTests.m:53-56)."""
+    return ((L == 1) * (np.maximum(np.abs(X), np.abs(Y)) < 0.1875)
+            + (L == 2) * (np.maximum(np.abs(X), np.abs(Y)) < 0.125)
+            + (L == 3) * (np.maximum(np.abs(X), np.abs(Y)) < 0.0625))
+
+
+def printed_close(value, printed):
+    """True when `value` rounds to the printed decimal string `printed`
+    (half a unit in its last digit, plus a little slack)."""
+    s = printed.strip()
+    if 'e' in s.lower():
+        mant, ex = s.lower().split('e')
+        dec = len(mant.split('.')[1]) if '.' in mant else 0
+        ulp = 10.0 ** (int(ex) - dec)
+    else:
+        dec = len(s.split('.')[1]) if '.' in s else 0
+        ulp = 10.0 ** (-dec)
+    return abs(value - float(s)) <= 0.5 * ulp * (1 + 1e-9) + 1e-300

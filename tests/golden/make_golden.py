@@ -1,0 +1,84 @@
+"""Extract the reference's recorded outputs into tests/golden/reference_outputs.json.
+
+Run in a container where the reference repository is mounted (default
+/root/reference, or pass a path).  The reference is MATLAB and cannot run
+here; its own verification run (MATLAB R2026a) recorded these numbers in
+verification/, and they are the golden values the oracle is pinned to.
+"""
+import csv
+import json
+import os
+import re
+import sys
+
+REF = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+VER = os.path.join(REF, 'verification')
+out = {}
+
+# G1: starfish residual history (verification/starfish-full-residual.csv)
+with open(os.path.join(VER, 'starfish-full-residual.csv')) as f:
+    rows = list(csv.DictReader(f))
+out['starfish_residual_history'] = [float(r['absoluteResidual']) for r in rows]
+
+# G2: starfish summary (verification/starfish-full.json)
+with open(os.path.join(VER, 'starfish-full.json')) as f:
+    sj = json.load(f)
+out['starfish'] = {k: sj[k] for k in ('baseCells', 'levels', 'epsilon', 'boundaryPoints', 'visibleCells',
+                                      'storedAmrCells', 'vcycles', 'relativeResidual', 'balanceDefect',
+                                      'patchesPerLevel', 'cellsPerLevel', 'interfaceBandCells',
+                                      'uncoveredBandCells', 'setupAndSolveSeconds', 'uniformSetupAndSolveSeconds',
+                                      'uniformRelativeResiduals')}
+
+# G3/G4: README examples (verification/readme-examples.txt)
+stage_re = re.compile(r'\[ebsam\] stage (\d+): (\d+) AMR level\(s\), (\d+) V-cycle\(s\), \|r\|/\|f\| = ([0-9.e+-]+), '
+                      r'avg factor ([0-9.]+), (\d+) visible cells')
+added_re = re.compile(r'\[(ebsam|ebtsam)\] added level (\d+) \((\d+) patch\(es\), (\d+) cells, h = ([0-9.e+-]+)\)')
+heat_re = re.compile(r'\[ebsam-p\] step\s+(\d+)/(\d+)\s+t=([0-9.]+)\s+V=(\d+)\s+rel=([0-9.e+-]+)\s+levels=(\d+)\s+'
+                     r'cells=(\d+)\s+mass=([0-9.e+-]+)')
+stages, added, heat = [], [], []
+with open(os.path.join(VER, 'readme-examples.txt')) as f:
+    for line in f:
+        m = stage_re.search(line)
+        if m:
+            stages.append({'stage': int(m[1]), 'amrLevels': int(m[2]), 'vcycles': int(m[3]), 'rel': m[4],
+                           'avgFactor': m[5], 'visibleCells': int(m[6])})
+        m = added_re.search(line)
+        if m:
+            added.append({'tree': m[1] == 'ebtsam', 'level': int(m[2]), 'np': int(m[3]), 'cells': int(m[4]),
+                          'h': m[5]})
+        m = heat_re.search(line)
+        if m:
+            heat.append({'step': int(m[1]), 'nsteps': int(m[2]), 't': float(m[3]), 'V': int(m[4]), 'rel': m[5],
+                         'levels': int(m[6]), 'cells': int(m[7]), 'mass': m[8]})
+out['readme_ring_stages'] = stages[:3]
+out['readme_tree_stages'] = stages[3:6]
+out['readme_ring_added'] = [a for a in added if not a['tree']]
+out['readme_tree_added'] = [a for a in added if a['tree']]
+out['readme_heat_steps'] = heat
+
+# G5: suite output lines used by the tests (verification/suite-output.txt)
+suite = open(os.path.join(VER, 'suite-output.txt')).read().splitlines()
+t1 = []
+for line in suite:
+    m = re.match(r'\s+m=\s*(\d+)\s+err_inf=([0-9.e+-]+)\s+err_l2=([0-9.e+-]+)\s+factor=([0-9.]+)\s+V=(\d+)\s+t=', line)
+    if m:
+        t1.append({'m': int(m[1]), 'err_inf': m[2], 'err_l2': m[3], 'factor': m[4], 'V': int(m[5])})
+out['suite_T1_uniform_mms'] = t1[:4]
+t3 = []
+for line in suite:
+    m = re.match(r'\s+\[(qif|lif)\] m0=\s*(\d+) L=(\d): err=([0-9.e+-]+) factor=([0-9.]+) mass=([0-9.e+-]+) V=(\d+)',
+                 line)
+    if m:
+        t3.append({'interp': m[1], 'm0': int(m[2]), 'L': int(m[3]), 'err': m[4], 'factor': m[5], 'mass': m[6],
+                   'V': int(m[7])})
+out['suite_T3_box_in_box'] = t3[:24]        # EllipticBSAM/tests/runAllTests.m
+out['suite_T3_box_in_box_tree'] = t3[24:48]  # EllipticBSAMTree/tests/runAllTreeTests.m
+out['source'] = {'repository': 'BSAM-in-MATLAB', 'files': ['verification/starfish-full-residual.csv',
+                                                          'verification/starfish-full.json',
+                                                          'verification/readme-examples.txt',
+                                                          'verification/suite-output.txt'],
+                 'matlab': sj.get('matlab')}
+dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'reference_outputs.json')
+with open(dst, 'w') as f:
+    json.dump(out, f, indent=1)
+print('wrote', dst)

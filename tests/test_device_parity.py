@@ -1,0 +1,84 @@
+"""GPU parity: the CUDA solve path against the C oracle on the same hierarchy.
+
+Both receive the identical flat tables; the device must reproduce the
+oracle's residual history and final field bit for bit (FP64 path).
+"""
+import numpy as np
+import pytest
+
+from bsam import ebOptions, hierarchy as hier
+from bsam.solve import build_hierarchy, ebSolve, ebtSolve
+from bsam.flat import flatten
+from bsam_oracle import OracleBackend, OracleHier
+from cases import config1_problem, vardc_problem, pureneumann_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def dev():
+    from bsam.device import DeviceBackend
+    return DeviceBackend.get(0)
+
+
+def _both(prob, opts, tree=False):
+    """Build one hierarchy (oracle set-up), then solve it on both paths."""
+    H = build_hierarchy(prob, opts, OracleBackend(), tree=tree)
+    fl = flatten(H)
+    oh = OracleHier(fl, opts)
+    it_o, hist_o, rel_o, vis_o = oh.solve_cycles(opts.MaxVCycles + 2)
+    from bsam.device import DevHier
+    dh = DevHier(dev().ctx, fl, opts)
+    it_d, hist_d, rel_d, vis_d = dh.solve_cycles(opts.MaxVCycles + 2)
+    Qd = dh.get(0, fl.Q.size)
+    return (it_o, hist_o, rel_o, vis_o, oh.Q), (it_d, hist_d, rel_d, vis_d, Qd)
+
+
+def _assert_bitwise(o, d):
+    assert o[0] == d[0]
+    assert o[3] == d[3]
+    np.testing.assert_array_equal(o[1], d[1])
+    assert o[2] == d[2]
+    np.testing.assert_array_equal(o[4], d[4])
+
+
+@pytest.mark.parametrize('tree', [False, True])
+def test_config1_fixed_hierarchy_bitwise(tree):
+    opts = ebOptions('BaseCells', 32, 'MaxLevels', 3, 'TagThreshold', 1e-2, 'Indicator', 'fun',
+                     'TagFunction', lambda x, y: (x - 0.4) ** 2 + (y - 0.55) ** 2 < 0.04, 'Verbose', 0,
+                     'RelTol', 1e-10)
+    o, d = _both(config1_problem(), opts, tree)
+    _assert_bitwise(o, d)
+
+
+@pytest.mark.parametrize('interp', ['qif', 'lif'])
+@pytest.mark.parametrize('mass', [True, False])
+def test_options_bitwise(interp, mass):
+    opts = ebOptions('BaseCells', 32, 'MaxLevels', 3, 'Indicator', 'fun',
+                     'TagFunction', lambda x, y: np.abs(x - y) < 0.15, 'Verbose', 0, 'RelTol', 1e-10,
+                     'GhostInterp', interp, 'MassCorrection', mass)
+    o, d = _both(vardc_problem(), opts)
+    _assert_bitwise(o, d)
+
+
+def test_singular_neumann_bitwise():
+    opts = ebOptions('BaseCells', 32, 'MaxLevels', 2, 'Indicator', 'fun',
+                     'TagFunction', lambda x, y: (x - 0.5) ** 2 + (y - 0.5) ** 2 < 0.05, 'Verbose', 0,
+                     'RelTol', 1e-10)
+    o, d = _both(pureneumann_problem(), opts)
+    _assert_bitwise(o, d)
+
+
+def test_config1_solution_driven_matches_oracle_pipeline():
+    """Full ebSolve (solve, tag, add level, solve) on the device vs the
+    oracle pipeline: same hierarchies, bitwise equal stage histories."""
+    p = config1_problem()
+    a = ebSolve(p, 'BaseCells', 32, 'MaxLevels', 3, 'TagThreshold', 1e-2, 'Verbose', 0, backend=OracleBackend())
+    b = ebSolve(p, 'BaseCells', 32, 'MaxLevels', 3, 'TagThreshold', 1e-2, 'Verbose', 0, backend=dev())
+    for sa, sb in zip(a['stats']['stages'], b['stats']['stages']):
+        assert sa['vcycles'] == sb['vcycles']
+        np.testing.assert_array_equal(sa['resHist'], sb['resHist'])
+    for la, lb in zip(a['levels'], b['levels']):
+        np.testing.assert_array_equal(la['box'], lb['box'])
+    for k in range(1, a['H'].nlev + 1):
+        for qa, qb in zip(a['H'].lev[k].Q, b['H'].lev[k].Q):
+            np.testing.assert_array_equal(qa, qb)
