@@ -104,6 +104,9 @@ struct LevelPlan {
 
 }  // namespace
 
+// error reporting shared with the other translation units of the library
+int bsam_internal_set_error(int code, const std::string &msg) { return fail(code, msg); }
+
 struct bsam_ctx_s {
   int device = 0;
   cudaStream_t stream = nullptr;
