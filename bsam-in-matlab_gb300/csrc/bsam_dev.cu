@@ -93,7 +93,8 @@ struct LevelPlan {
   double hx = 0, hy = 0;
   bool pow2 = false;
   DecompH col, cell, coarse;
-  int g1_off = 0, g1_n = 0, g2_off = 0, g2_n = 0;
+  int g1_off = 0, g1_n = 0;
+  int rc_off = 0, rc_n = 0;        // relax chunk records
   int ring_off = 0, ring_n = 0;
   // corrections contributed by this (fine) level, targets in level k-1
   int ct_off = 0, ct_n = 0;
@@ -132,6 +133,12 @@ struct bsam_hier_s {
   DBuf<int> g_dst, g_a, g_b, g_c, g_d, g_e;
   DBuf<PatchD> patches;
   DBuf<ResAcc> acc;
+  DBuf<Rule> perim;                // per-patch perimeter ghost rules (inline)
+  DBuf<RelaxChunk> rchunks;        // relax chunk records, all levels
+  DBuf<unsigned char> blk_seg;     // residual block -> segment
+  DBuf<LevelX> levelx;             // per-level descriptors for multi-level kernels
+  DBuf<ResSeg> segs;               // residual launch segments
+  int nseg = 0, nres_blocks = 0;
   ResAcc *acc_host = nullptr;  // pinned
   int nslots = 0, nres_levels = 0, npartials = 0;
   // graph of one V-cycle + fill-down + residual
@@ -165,6 +172,7 @@ LevelD leveld(bsam_hier h, int k) {
   d.hx = L.hx; d.hy = L.hy;
   d.hx2 = L.hx * L.hx; d.hy2 = L.hy * L.hy;
   d.ihx2 = 1.0 / d.hx2; d.ihy2 = 1.0 / d.hy2;
+  d.pow2 = L.pow2 ? 1 : 0;
   return d;
 }
 
@@ -178,6 +186,25 @@ Decomp decomp(bsam_hier h, const DecompH &D) {
 }
 
 inline int nblk(int n) { return (n + kBlock - 1) / kBlock; }
+
+// Every kernel goes out with programmatic stream serialization: the next
+// kernel is scheduled while the previous one drains and waits for it at its
+// griddepcontrol.wait (kernels.cuh chain_in).
+template <typename... KArgs, typename... Args>
+void launch_k(bsam_hier h, void (*kern)(KArgs...), int grid, int block, Args... args) {
+  if (grid <= 0) return;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, args...);
+}
 
 // launch bookkeeping: optional per-kernel CUDA events for profiling
 struct Launch {
@@ -204,88 +231,77 @@ struct Launch {
 enum { K_RELAX, K_GHOST, K_RESTRICT, K_RING, K_LOAD, K_CORR, K_PROLONG, K_COARSEST, K_RESID };
 
 // ---------------------------------------------------------------------------
-void launch_fill(bsam_hier h, int k) {
-  const LevelPlan &L = h->lev[k];
-  GhostItems G{h->g_type.p, h->g_dst.p, h->g_a.p, h->g_b.p, h->g_c.p, h->g_d.p, h->g_e.p};
-  if (L.g1_n) {
-    Launch l(h, K_GHOST, 0);
-    k_ghost<<<nblk(L.g1_n), kBlock, 0, h->stream>>>(G, L.g1_off, L.g1_n, h->Q.p, h->QC.p, h->bcg.p, L.hx, L.hy);
-  }
-  if (L.g2_n) {
-    Launch l(h, K_GHOST, 0);
-    k_ghost<<<nblk(L.g2_n), kBlock, 0, h->stream>>>(G, L.g2_off, L.g2_n, h->Q.p, h->QC.p, h->bcg.p, L.hx, L.hy);
-  }
+GhostItems ghost_items(bsam_hier h) {
+  return GhostItems{h->g_type.p, h->g_dst.p, h->g_a.p, h->g_b.p, h->g_c.p, h->g_d.p, h->g_e.p};
 }
 
+void launch_fill(bsam_hier h, int k) {
+  const LevelPlan &L = h->lev[k];
+  if (!L.g1_n) return;
+  Launch l(h, K_GHOST, 0);
+  launch_k(h, k_ghost, nblk(L.g1_n), kBlock, ghost_items(h), L.g1_off, L.g1_n, h->Q.p, h->QC.p,
+           (const double *)h->bcg.p, L.hx, L.hy);
+}
+
+// ebRelaxLevel (ebRelaxLevel.m:28-38): 2*nsweeps colour passes; the ghost
+// refill after every colour is folded into the next pass (k_relax `fresh`),
+// and one fill after the last pass leaves the ghost frame as the reference's.
 void launch_relax(bsam_hier h, int k, int nsweeps) {
+  if (nsweeps <= 0) return;
   const LevelPlan &L = h->lev[k];
   Fields f = fields(h);
   LevelD ld = leveld(h, k);
-  Decomp D = decomp(h, L.col);
+  const RelaxChunk *ch = h->rchunks.p + L.rc_off;
+  const int grid = (L.rc_n + kBlock / kChunk - 1) / (kBlock / kChunk);
+  const int unit = h->opts.omega == 1.0 ? 1 : 0;
   for (int s = 0; s < nsweeps; ++s)
     for (int m = 0; m < 2; ++m) {
-      {
-        Launch l(h, K_RELAX, 24.0 * (double)L.ncells);
-        if (L.pow2)
-          k_relax<true><<<D.nblocks, kBlock, 0, h->stream>>>(ld, D, f, m, h->opts.omega);
-        else
-          k_relax<false><<<D.nblocks, kBlock, 0, h->stream>>>(ld, D, f, m, h->opts.omega);
-      }
-      launch_fill(h, k);
+      const int fresh = (s > 0 || m > 0) ? 1 : 0;
+      Launch l(h, K_RELAX, 24.0 * (double)L.ncells);
+      if (L.pow2)
+        launch_k(h, k_relax<true>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m, h->opts.omega, unit,
+                 fresh);
+      else
+        launch_k(h, k_relax<false>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m, h->opts.omega, unit,
+                 fresh);
     }
+  launch_fill(h, k);
 }
 
 void launch_restrict(bsam_hier h, int k, int to_parent) {
   const LevelPlan &L = h->lev[k];
   Decomp D = decomp(h, L.coarse);
   Launch l(h, K_RESTRICT, 12.0 * (double)L.ncells);
-  k_restrict<<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), D, fields(h), to_parent);
+  launch_k(h, k_restrict, D.nblocks, kBlock, leveld(h, k), D, fields(h), to_parent);
 }
 
-void launch_ring(bsam_hier h, int k) {
-  const LevelPlan &L = h->lev[k];
-  if (!L.ring_n) return;
-  Launch l(h, K_RING, 0);
-  k_ring<<<nblk(L.ring_n), kBlock, 0, h->stream>>>(h->ring.p, L.ring_off, L.ring_n, h->Q.p, h->QC.p);
+CorrCSR corr_csr(bsam_hier h, const LevelPlan &L) {
+  return CorrCSR{h->ct_cell.p + L.ct_off, h->ct_patch.p + L.ct_off, h->ct_beg.p + L.ct_off, h->ct_item.p, h->ct_j.p};
 }
 
+// ebTransfer 'ring' + ebCoarseLoad (ebVcycle.m:28-29) in one launch
 void launch_coarse_load(bsam_hier h, int k) {
   const LevelPlan &L = h->lev[k];
   Decomp D = decomp(h, L.coarse);
-  Fields f = fields(h);
-  const bool pow2 = L.pow2 && h->lev[k - 1].pow2;
-  {
-    Launch l(h, K_LOAD, 50.0 * (double)L.ncells);
-    if (pow2)
-      k_coarse_load<true><<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), leveld(h, k - 1), D, f);
-    else
-      k_coarse_load<false><<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), leveld(h, k - 1), D, f);
-  }
-  if (h->opts.mass_correction && L.ct_n) {
-    Launch l(h, K_CORR, 0);
-    const int *tc = h->ct_cell.p + L.ct_off, *tb = h->ct_beg.p + L.ct_off;
-    if (h->lev[k - 1].pow2)
-      k_corr<true><<<nblk(L.ct_n), kBlock, 0, h->stream>>>(leveld(h, k), leveld(h, k - 1), f, tc, tb, h->ct_item.p,
-                                                          h->ct_j.p, L.ct_n);
-    else
-      k_corr<false><<<nblk(L.ct_n), kBlock, 0, h->stream>>>(leveld(h, k), leveld(h, k - 1), f, tc, tb, h->ct_item.p,
-                                                           h->ct_j.p, L.ct_n);
-  }
+  const int ntgt = h->opts.mass_correction ? L.ct_n : 0;
+  const int grid = nblk(L.ring_n) + D.nblocks + nblk(ntgt);
+  Launch l(h, K_LOAD, 50.0 * (double)L.ncells);
+  launch_k(h, k_load, grid, kBlock, leveld(h, k), leveld(h, k - 1), D, fields(h), (const int *)h->ring.p, L.ring_off,
+           L.ring_n, corr_csr(h, L), ntgt);
 }
 
 void launch_prolong(bsam_hier h, int k, int correct) {
   const LevelPlan &L = h->lev[k];
   Decomp D = decomp(h, L.coarse);
   Launch l(h, K_PROLONG, 20.0 * (double)L.ncells);
-  k_prolong<<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), D, fields(h), correct);
+  launch_k(h, k_prolong, D.nblocks, kBlock, leveld(h, k), D, fields(h), correct);
 }
 
 void launch_coarsest(bsam_hier h) {
   {
     Launch l(h, K_COARSEST, 8.0 * (double)h->ncoarse * h->ncoarse);
-    const int threads = h->ncoarse * 32;
-    k_coarsest<<<nblk(threads), kBlock, 0, h->stream>>>(h->Ainv.p, h->bcRhs.p, fields(h), h->coarse_c_off,
-                                                        h->coarse_q_off, h->n1, h->ncoarse);
+    launch_k(h, k_coarsest, nblk(h->ncoarse * 32), kBlock, (const double *)h->Ainv.p, (const double *)h->bcRhs.p,
+             fields(h), h->coarse_c_off, h->coarse_q_off, h->n1, h->ncoarse);
   }
   launch_fill(h, 1);
 }
@@ -298,7 +314,6 @@ void launch_vcycle(bsam_hier h, int k) {
   launch_relax(h, k, h->opts.npre);
   launch_restrict(h, k, 1);
   launch_fill(h, k - 1);
-  launch_ring(h, k);
   launch_coarse_load(h, k);
   launch_vcycle(h, k - 1);
   launch_prolong(h, k, 1);
@@ -313,47 +328,20 @@ void launch_filldown(bsam_hier h) {
   }
 }
 
+// ebCompResidual (ebCompResidual.m:15-85): one launch over every level, then
+// the final reduction
 void launch_residual(bsam_hier h) {
-  Fields f = fields(h);
-  if (h->opts.mass_correction) {
-    for (int k = std::max(2, h->root + 1); k <= h->nlev; ++k) {
-      launch_ring(h, k);
-      launch_restrict(h, k, 0);
-    }
-  }
-  for (int k = h->root; k <= h->nlev; ++k) {
-    const LevelPlan &L = h->lev[k];
-    Decomp D = decomp(h, L.cell);
-    {
-      Launch l(h, K_RESID, 41.0 * (double)L.ncells);
-      if (L.pow2)
-        k_residual<true><<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), D, f, h->acc.p, h->slots.p + L.res_slot,
-                                                              h->opts.mass_correction);
-      else
-        k_residual<false><<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, k), D, f, h->acc.p, h->slots.p + L.res_slot,
-                                                               h->opts.mass_correction);
-    }
-    // targets in level k receive the corrections of level k+1
-    if (k < h->nlev && h->opts.mass_correction && h->lev[k + 1].ct_n) {
-      const LevelPlan &Lf = h->lev[k + 1];
-      Launch l(h, K_RESID, 0);
-      double *slot = h->slots.p + L.res_slot + L.res_main_blocks;
-      const int *tc = h->ct_cell.p + Lf.ct_off, *tp = h->ct_patch.p + Lf.ct_off, *tb = h->ct_beg.p + Lf.ct_off;
-      if (L.pow2)
-        k_residual_targets<true><<<nblk(Lf.ct_n), kBlock, 0, h->stream>>>(
-            leveld(h, k + 1), leveld(h, k), h->patches.p + L.p0, f, tc, tp, tb, h->ct_item.p, h->ct_j.p, Lf.ct_n,
-            h->acc.p, slot);
-      else
-        k_residual_targets<false><<<nblk(Lf.ct_n), kBlock, 0, h->stream>>>(
-            leveld(h, k + 1), leveld(h, k), h->patches.p + L.p0, f, tc, tp, tb, h->ct_item.p, h->ct_j.p, Lf.ct_n,
-            h->acc.p, slot);
-    }
-  }
+  double bytes = 0;
+  for (int k = h->root; k <= h->nlev; ++k) bytes += 41.0 * (double)h->lev[k].ncells;
   {
-    Launch l(h, K_RESID, 0);
-    k_residual_final<<<1, 32, 0, h->stream>>>(h->acc.p, h->slots.p, h->level_slot0.p, h->area.p, h->nres_levels,
-                                               (double)h->ncell_visible);
+    Launch l(h, K_RESID, bytes);
+    launch_k(h, k_residual, h->nres_blocks, kBlock, (const LevelX *)h->levelx.p, (const ResSeg *)h->segs.p,
+             (const unsigned char *)h->blk_seg.p, fields(h), (const int *)h->ring.p, h->slots.p, h->nslots,
+             h->opts.mass_correction);
   }
+  Launch l(h, K_RESID, 0);
+  launch_k(h, k_residual_final, 1, kFinal, h->acc.p, (const double *)h->slots.p, h->nslots,
+           (const int *)h->level_slot0.p, (const double *)h->area.p, h->nres_levels, (double)h->ncell_visible);
 }
 
 // one ebSolveCycles iteration body: F = FTrue, V-cycle, fill-down, residual
@@ -403,6 +391,9 @@ struct Builder {
   std::vector<int> ints;
   std::vector<int8_t> gt;
   std::vector<int> gdst, ga, gb, gc, gd, ge;
+  std::vector<Rule> perim;         // per patch: W(my) E(my) S(mx) N(mx) inline rule (type -1: physical)
+  std::vector<RelaxChunk> chunks;  // relax chunk records
+  std::vector<int> pe_off;         // per patch offset into perim
 
   const int32_t *P(int p) const { return d->patches + (size_t)p * PDN; }
 
@@ -540,34 +531,85 @@ struct Builder {
         if (r[PD_BCN] == 1) put({G_DIRICHLET, Q(i, my + 2), Q(i, my + 1), Q(i, my), 0, 0, gN + i - 2});
         else if (r[PD_BCN] == 2) put({G_NEUMANN, Q(i, my + 2), Q(i, my + 1), 1, 0, 0, gN + i - 2});
       }
+      // physical corners: (face ghost + face ghost) - interior; the face
+      // ghosts are referenced by their destination here and resolved to
+      // rule indices once the level's rules are final
       if (r[PD_CCSW] == 1) corners.push_back({G_PHYS_CORNER, Q(1, 1), Q(2, 1), Q(1, 2), Q(2, 2), 0, 0});
       if (r[PD_CCSE] == 1) corners.push_back({G_PHYS_CORNER, Q(mx + 2, 1), Q(mx + 1, 1), Q(mx + 2, 2), Q(mx + 1, 2), 0, 0});
       if (r[PD_CCNW] == 1) corners.push_back({G_PHYS_CORNER, Q(1, my + 2), Q(2, my + 2), Q(1, my + 1), Q(2, my + 1), 0, 0});
       if (r[PD_CCNE] == 1) corners.push_back({G_PHYS_CORNER, Q(mx + 2, my + 2), Q(mx + 1, my + 2), Q(mx + 2, my + 1), Q(mx + 1, my + 1), 0, 0});
     }
-    for (const G &g : corners)
+    L.g1_off = (int)gt.size();
+    for (G &g : corners) {
       if (rule.count(g.dst)) return fail(BSAM_ERR_ARG, "physical corner also written by another ghost stage");
+      auto i1 = rule.find(g.a), i2 = rule.find(g.b);
+      if (i1 == rule.end() || i2 == rule.end()) return fail(BSAM_ERR_ARG, "physical corner next to a ghost without a rule");
+      g.a = L.g1_off + (int)i1->second;
+      g.b = L.g1_off + (int)i2->second;
+    }
     auto emit = [&](const std::vector<G> &v) {
       for (const G &g : v) {
         gt.push_back(g.t); gdst.push_back(g.dst); ga.push_back(g.a); gb.push_back(g.b);
         gc.push_back(g.c); gd.push_back(g.dd); ge.push_back(g.e);
       }
     };
-    L.g1_off = (int)gt.size();
     emit(tmp);
     emit(ringi);
-    L.g1_n = (int)gt.size() - L.g1_off;
-    L.g2_off = (int)gt.size();
     emit(corners);
-    L.g2_n = (int)gt.size() - L.g2_off;
+    L.g1_n = (int)gt.size() - L.g1_off;
+    // perimeter rule table for the relaxation's ghost evaluation: every cell
+    // of an internal face has a value rule (COPY/QIF/QIF_END/LIF)
+    for (int p = L.p0; p < L.p1; ++p) {
+      const int32_t *r = P(p);
+      const int mx = r[PD_MX], my = r[PD_MY], qo = r[PD_QOFF];
+      auto Q = [&](int i, int j) { return qo + (i - 1) + (j - 1) * (mx + 2); };
+      pe_off[p] = (int)perim.size();
+      auto add = [&](int side, int dst) -> bool {
+        if (r[PD_BCW + side] != 0) { perim.push_back(Rule{-1, 0, 0, 0, 0, 0}); return true; }
+        auto it = rule.find(dst);
+        if (it == rule.end()) return false;
+        const G &g = tmp[it->second];
+        if (g.t != G_COPY && g.t != G_QIF && g.t != G_QIF_END && g.t != G_LIF) return false;
+        perim.push_back(Rule{g.t, g.a, g.b, g.c, g.dd, g.e});
+        return true;
+      };
+      bool ok = true;
+      for (int j = 2; j <= my + 1; ++j) ok = ok && add(0, Q(1, j));
+      for (int j = 2; j <= my + 1; ++j) ok = ok && add(1, Q(mx + 2, j));
+      for (int i = 2; i <= mx + 1; ++i) ok = ok && add(2, Q(i, 1));
+      for (int i = 2; i <= mx + 1; ++i) ok = ok && add(3, Q(i, my + 2));
+      if (!ok) return fail(BSAM_ERR_ARG, "internal face ghost without an interpolation or copy rule at level " +
+                                             std::to_string(k));
+    }
+    // relax chunks: the colour cells of each patch in pieces of kChunk
+    L.rc_off = (int)chunks.size();
+    for (int p = L.p0; p < L.p1; ++p) {
+      const int32_t *r = P(p);
+      const int ncol = r[PD_MX] * r[PD_MY] / 2;
+      for (int s0 = 0; s0 < ncol; s0 += kChunk) {
+        RelaxChunk c{};
+        c.q_off = r[PD_QOFF]; c.c_off = r[PD_COFF]; c.dew_off = r[PD_DEWOFF]; c.dns_off = r[PD_DNSOFF];
+        c.bcg_off = r[PD_BCGOFF]; c.pe_off = pe_off[p]; c.mx = r[PD_MX]; c.my = r[PD_MY];
+        c.par0 = r[PD_PAR0]; c.s0 = s0; c.n = std::min(kChunk, ncol - s0); c.pad = 0;
+        for (int sd = 0; sd < 4; ++sd) c.bc[sd] = r[PD_BCW + sd];
+        chunks.push_back(c);
+      }
+    }
+    L.rc_n = (int)chunks.size() - L.rc_off;
     // every index must stay inside Q / QC / bcg
-    for (int i = L.g1_off; i < L.g2_off + L.g2_n; ++i) {
+    for (int i = L.g1_off; i < L.g1_off + L.g1_n; ++i) {
       const int8_t t = gt[i];
       auto okq = [&](int v) { return v >= 0 && v < d->n_q; };
       bool ok = t == G_RING ? (gdst[i] >= 0 && gdst[i] < d->n_qc) : okq(gdst[i]);
       ok = ok && okq(ga[i]);
-      if (t == G_QIF || t == G_QIF_END || t == G_LIF || t == G_PHYS_CORNER || t == G_DIRICHLET) ok = ok && okq(gb[i]);
-      if (t == G_QIF || t == G_QIF_END || t == G_LIF || t == G_LIF_CORNER || t == G_PHYS_CORNER) ok = ok && okq(gc[i]);
+      if (t == G_PHYS_CORNER) {
+        ok = gdst[i] >= 0 && gdst[i] < d->n_q && ga[i] >= L.g1_off && ga[i] < i && gb[i] >= L.g1_off && gb[i] < i &&
+             okq(gc[i]);
+        if (!ok) return fail(BSAM_ERR_ARG, "physical corner rule out of range at level " + std::to_string(k));
+        continue;
+      }
+      if (t == G_QIF || t == G_QIF_END || t == G_LIF || t == G_DIRICHLET) ok = ok && okq(gb[i]);
+      if (t == G_QIF || t == G_QIF_END || t == G_LIF || t == G_LIF_CORNER) ok = ok && okq(gc[i]);
       if (t == G_QIF_END) ok = ok && okq(gd[i]) && okq(ge[i]);
       if (t == G_DIRICHLET || t == G_NEUMANN) ok = ok && ge[i] >= 0 && ge[i] < d->n_bcg;
       if (!ok) return fail(BSAM_ERR_ARG, "ghost rule index out of range at level " + std::to_string(k));
@@ -661,12 +703,12 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
     q.mx = r[PD_MX]; q.my = r[PD_MY]; q.par0 = r[PD_PAR0]; q.level = r[PD_LEVEL];
     q.q_off = r[PD_QOFF]; q.c_off = r[PD_COFF]; q.dew_off = r[PD_DEWOFF]; q.dns_off = r[PD_DNSOFF];
     q.qc_off = r[PD_QCOFF]; q.bcg_off = r[PD_BCGOFF]; q.cfd_off = r[PD_CFDOFF]; q.pc_off = r[PD_PCOFF];
-    q.win_off = r[PD_WIN0]; q.fp_off = r[PD_FP0]; q.corr_off = r[PD_CORR0]; q.pad = 0;
+    q.win_off = r[PD_WIN0]; q.fp_off = r[PD_FP0]; q.corr_off = r[PD_CORR0]; q.pe_off = 0;
     for (int sd = 0; sd < 4; ++sd) q.bc[sd] = r[PD_BCW + sd];
   }
-  if ((rc = h->patches.upload(pd.data(), pd.size(), s))) return rc;
   // plan
   Builder B{h, d};
+  B.pe_off.assign(d->npatch, 0);
   h->lev.assign(d->nlev + 1, LevelPlan());
   std::vector<uint8_t> flags(d->covered, d->covered + d->n_cells);
   std::vector<int> ct_cell, ct_patch, ct_beg, ct_item, ct_j;
@@ -736,6 +778,12 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
       ct_beg.push_back((int)ct_item.size());
     }
   }
+  for (int p = 0; p < d->npatch; ++p) pd[p].pe_off = B.pe_off[p];
+  if ((rc = h->patches.upload(pd.data(), pd.size(), s))) return rc;
+  if (B.perim.empty()) B.perim.push_back(Rule{-1, 0, 0, 0, 0, 0});
+  if ((rc = h->perim.upload(B.perim.data(), B.perim.size(), s)) ||
+      (rc = h->rchunks.upload(B.chunks.data(), B.chunks.size(), s)))
+    return rc;
   // covered cells of levels >= root are excluded from the norms
   int64_t nvis = 0;
   for (int k = d->root_idx; k <= d->nlev; ++k) {
@@ -743,10 +791,13 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
     for (int c = lv[LD_CELL0]; c < lv[LD_CELL1]; ++c) nvis += (d->covered[c] == 0);
   }
   h->ncell_visible = nvis;
-  // residual slots
+  // residual launch: segments per level >= root (main cells, then targets,
+  // each with its own slots), then the QC refresh segments of the levels
+  // above the root
   std::vector<int> slot0;
   std::vector<double> area;
-  int ns = 0;
+  std::vector<ResSeg> segs;
+  int ns = 0, nbk = 0;
   for (int k = d->root_idx; k <= d->nlev; ++k) {
     LevelPlan &L = h->lev[k];
     L.res_slot = ns;
@@ -754,11 +805,35 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
     L.res_tgt_blocks = (k < d->nlev) ? nblk(h->lev[k + 1].ct_n) : 0;
     slot0.push_back(ns);
     area.push_back(L.hx * L.hy);
-    ns += L.res_main_blocks + L.res_tgt_blocks;
+    segs.push_back(ResSeg{0, k, nbk, ns});
+    nbk += L.res_main_blocks;
+    ns += L.res_main_blocks;
+    if (L.res_tgt_blocks) {
+      segs.push_back(ResSeg{1, k, nbk, ns});
+      nbk += L.res_tgt_blocks;
+      ns += L.res_tgt_blocks;
+    }
   }
   slot0.push_back(ns);
+  for (int k = std::max(2, d->root_idx + 1); k <= d->nlev; ++k) {
+    LevelPlan &L = h->lev[k];
+    if (L.ring_n) {
+      segs.push_back(ResSeg{2, k, nbk, 0});
+      nbk += nblk(L.ring_n);
+    }
+    segs.push_back(ResSeg{3, k, nbk, 0});
+    nbk += L.coarse.nblocks;
+  }
   h->nslots = ns;
   h->nres_levels = (int)area.size();
+  h->nseg = (int)segs.size();
+  h->nres_blocks = nbk;
+  if (segs.size() > 255) return fail(BSAM_ERR_ARG, "too many residual segments");
+  std::vector<unsigned char> blk_seg(std::max(nbk, 1), 0);
+  for (size_t i = 0; i < segs.size(); ++i) {
+    const int end = (i + 1 < segs.size()) ? segs[i + 1].block0 : nbk;
+    for (int b2 = segs[i].block0; b2 < end; ++b2) blk_seg[b2] = (unsigned char)i;
+  }
   if ((rc = h->flags.upload(flags.data(), flags.size(), s)) || (rc = h->ints.upload(B.ints.data(), B.ints.size(), s)) ||
       (rc = h->g_type.upload(B.gt.data(), B.gt.size(), s)) || (rc = h->g_dst.upload(B.gdst.data(), B.gdst.size(), s)) ||
       (rc = h->g_a.upload(B.ga.data(), B.ga.size(), s)) || (rc = h->g_b.upload(B.gb.data(), B.gb.size(), s)) ||
@@ -768,8 +843,26 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
       (rc = h->ct_beg.upload(ct_beg.data(), ct_beg.size(), s)) ||
       (rc = h->ct_item.upload(ct_item.data(), ct_item.size(), s)) || (rc = h->ct_j.upload(ct_j.data(), ct_j.size(), s)) ||
       (rc = h->level_slot0.upload(slot0.data(), slot0.size(), s)) || (rc = h->area.upload(area.data(), area.size(), s)) ||
-      (rc = h->slots.alloc(std::max(ns, 1))) || (rc = h->acc.alloc(1)))
+      (rc = h->slots.alloc(3 * (size_t)std::max(ns, 1))) || (rc = h->acc.alloc(1)) ||
+      (rc = h->blk_seg.upload(blk_seg.data(), blk_seg.size(), s)) ||
+      (rc = h->segs.upload(segs.data(), segs.size(), s)))
     return rc;
+  // per-level descriptors for the multi-level residual kernel
+  {
+    std::vector<LevelX> X(d->nlev + 1);
+    for (int k = 1; k <= d->nlev; ++k) {
+      LevelPlan &L = h->lev[k];
+      X[k].L = leveld(h, k);
+      X[k].cell = decomp(h, L.cell);
+      X[k].coarse = decomp(h, L.coarse);
+      X[k].C = corr_csr(h, L);
+      X[k].ct_n = L.ct_n;
+      X[k].ring_off = L.ring_off;
+      X[k].ring_n = L.ring_n;
+      X[k].pad = 0;
+    }
+    if ((rc = h->levelx.upload(X.data(), X.size(), s))) return rc;
+  }
   CK(cudaMemsetAsync(h->acc.p, 0, sizeof(ResAcc), s));
   // coarsest
   const int32_t *r1 = d->patches;
@@ -795,7 +888,8 @@ void release(bsam_hier h) {
   h->win.release(); h->fp.release(); h->ring.release(); h->ints.release(); h->ct_cell.release();
   h->ct_patch.release(); h->ct_beg.release(); h->ct_item.release(); h->ct_j.release(); h->level_slot0.release();
   h->g_type.release(); h->g_dst.release(); h->g_a.release(); h->g_b.release(); h->g_c.release(); h->g_d.release();
-  h->g_e.release(); h->patches.release(); h->acc.release();
+  h->g_e.release(); h->patches.release(); h->acc.release(); h->perim.release(); h->levelx.release();
+  h->segs.release(); h->rchunks.release(); h->blk_seg.release();
   h->saveQ.release(); h->saveQC.release(); h->saveF.release();
   if (h->acc_host) cudaFreeHost(h->acc_host);
   h->acc_host = nullptr;

@@ -4,13 +4,21 @@
 // reference's floating-point operation order (the library is compiled with
 // --fmad=false, so no multiply-add is contracted).  Work is flattened per
 // level over all patches: a level's items (colour cells, cells, coarse
-// cells, ghost items, ...) are numbered consecutively patch after patch and
-// cut into 256-item blocks; `blk_p0[b]` names the patch that holds block b's
-// first item, `beg[p]..beg[p+1]` the items of patch p.
+// cells, ...) are numbered consecutively patch after patch and cut into
+// 256-item blocks; `blk_p0[b]` names the patch that holds block b's first
+// item, `beg[p]..beg[p+1]` the items of patch p.
 //
 // Memory layout in HBM: one array per field with every patch of every level
 // concatenated, each patch column-major (x fastest) like the reference; the
 // solution Q and the coarse shadows QC carry their one-cell ghost frame.
+//
+// Launch chaining (programmatic dependent launch): every kernel opens with
+// griddepcontrol.launch_dependents, so the next kernel of the V-cycle is
+// scheduled while this one drains, then loads what no kernel of the solve
+// writes (patch records, coefficients, ghost rules, index tables) and only
+// then executes griddepcontrol.wait, after which it reads and writes the
+// solution state.  Every thread executes the wait before it exits, so no
+// kernel completes before its predecessor.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -19,12 +27,19 @@
 
 namespace bsam {
 
+__device__ __forceinline__ void chain_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void chain_in() {
+  chain_trigger();
+  chain_wait();
+}
+
 // per-patch metadata on the device
 struct PatchD {
   int mx, my, par0, level;
   int q_off, c_off, dew_off, dns_off;
   int qc_off, bcg_off, cfd_off, pc_off;
-  int win_off, fp_off, corr_off, pad;
+  int win_off, fp_off, corr_off, pe_off;   // pe_off: perimeter ghost-rule table
   int bc[4];
 };
 
@@ -45,61 +60,35 @@ struct Decomp {
 struct LevelD {
   const PatchD *patches;       // this level's patches
   double hx, hy, hx2, hy2, ihx2, ihy2;   // ihx2 = 1/hx2 (used only when exact)
+  int pow2;                    // hx2 and hy2 are powers of two
 };
 
-__device__ __forceinline__ int find_patch(const Decomp &D, int g) {
-  int p = __ldg(D.blk_p0 + blockIdx.x);
+// `b` is the block index within the decomposition
+__device__ __forceinline__ int find_patch(const Decomp &D, int b, int g) {
+  int p = __ldg(D.blk_p0 + b);
   while (g >= __ldg(D.beg + p + 1)) ++p;
   return p;
 }
 
-// ---------------------------------------------------------------------------
-// relax2d (EllipticBSAM/src/ebKernels.m:37-95): one colour of the red-black
-// Gauss-Seidel sweep over all patches of a level.  One thread per cell of the
-// colour; the partial physical ghosts ((8/3)g + (1/3)u_2 Dirichlet, h g
-// Neumann) are formed in registers, the u_1 coupling being folded into
-// InvDiagS.  Neighbours of the other colour are not written in this pass,
-// so in-place updates equal the reference's candidate-then-write.
-template <bool kPow2>
-__global__ void __launch_bounds__(kBlock) k_relax(LevelD L, Decomp D, Fields f, int m, double omega) {
-  const int g = blockIdx.x * kBlock + threadIdx.x;
-  if (g >= D.n) return;
-  const int p = find_patch(D, g);
-  const PatchD &P = L.patches[p];
-  const int mx = P.mx, my = P.my, half = mx >> 1;
-  const int s = g - __ldg(D.beg + p);
-  const int lj = s / half;
-  const int li = 2 * (s - lj * half) + ((m + lj + P.par0) & 1);
-  const int ldq = mx + 2;
-  double *__restrict__ Q = f.Q + P.q_off;
-  const int c = (li + 1) + (lj + 1) * ldq;
-  const double *__restrict__ g4 = f.bcg + P.bcg_off;
-  double qe = Q[c + 1], qw = Q[c - 1], qn = Q[c + ldq], qs = Q[c - ldq];
-  if (li == 0 && P.bc[0]) qw = (P.bc[0] == 1) ? (8.0 / 3.0) * g4[lj] + (1.0 / 3.0) * Q[c + 1] : L.hx * g4[lj];
-  if (li == mx - 1 && P.bc[1]) qe = (P.bc[1] == 1) ? (8.0 / 3.0) * g4[my + lj] + (1.0 / 3.0) * Q[c - 1] : L.hx * g4[my + lj];
-  if (lj == 0 && P.bc[2]) qs = (P.bc[2] == 1) ? (8.0 / 3.0) * g4[2 * my + li] + (1.0 / 3.0) * Q[c + ldq] : L.hy * g4[2 * my + li];
-  if (lj == my - 1 && P.bc[3]) qn = (P.bc[3] == 1) ? (8.0 / 3.0) * g4[2 * my + mx + li] + (1.0 / 3.0) * Q[c - ldq] : L.hy * g4[2 * my + mx + li];
-  const double *__restrict__ DeW = f.DeW + P.dew_off;
-  const double *__restrict__ DnS = f.DnS + P.dns_off;
-  const int cc = P.c_off + li + lj * mx;
-  double t = __ldg(f.F + cc);
-  t = t + divh<kPow2>(qe * __ldg(DeW + (li + 1) + lj * (mx + 1)), L.hx2, L.ihx2);
-  t = t + divh<kPow2>(qw * __ldg(DeW + li + lj * (mx + 1)), L.hx2, L.ihx2);
-  t = t + divh<kPow2>(qn * __ldg(DnS + li + (lj + 1) * mx), L.hy2, L.ihy2);
-  t = t + divh<kPow2>(qs * __ldg(DnS + li + lj * mx), L.hy2, L.ihy2);
-  t = t * __ldg(f.ID + cc);
-  Q[c] = (omega == 1.0) ? t : omega * t + (1 - omega) * Q[c];
+__device__ __forceinline__ double divr(double x, double h2, double ih2, int pow2) {
+  return pow2 ? x * ih2 : x / h2;
+}
+
+__device__ __forceinline__ double op_cell_r(const double *__restrict__ Qa, int ldq, const double *__restrict__ DeW,
+                                            const double *__restrict__ DnS, double cc, int mx, int li, int lj,
+                                            const LevelD &L) {
+  return L.pow2 ? op_cell<true>(Qa, ldq, DeW, DnS, cc, mx, li, lj, L.hx2, L.hy2, L.ihx2, L.ihy2)
+                : op_cell<false>(Qa, ldq, DeW, DnS, cc, mx, li, lj, L.hx2, L.hy2, L.ihx2, L.ihy2);
 }
 
 // ---------------------------------------------------------------------------
-// Ghost fill (EllipticBSAM/src/ebFillGhosts.m:17-94, ebInterpCf.m:36-154).
+// Ghost rules (EllipticBSAM/src/ebFillGhosts.m:17-94, ebInterpCf.m:36-154).
 // The three ordered stages (coarse-fine interpolation, same-level copy,
 // physical closure) are resolved on the host into one final rule per ghost
-// cell; every rule reads only interior cells, parent cells or boundary
-// data, so a level's ghost cells are filled in one pass.  Physical corners
-// read face ghosts and run as a second pass.  Coarse-window values are read
-// from the parent's Q directly (the QC ring is refreshed from the same
-// cells in the same pass).
+// cell.  Value rules read only interior cells, parent cells (the coarse
+// window is read from the parent's Q, which is what the QC ring holds) or
+// boundary data; a physical corner evaluates its two face-ghost rules
+// itself, so a level's ghost frame is filled in one pass.
 enum GhostType : int8_t {
   G_COPY = 0, G_QIF = 1, G_QIF_END = 2, G_LIF = 3, G_LIF_CORNER = 4,
   G_DIRICHLET = 5, G_NEUMANN = 6, G_RING = 7, G_PHYS_CORNER = 8
@@ -110,158 +99,359 @@ struct GhostItems {
   const int *dst, *a, *b, *c, *d, *e;
 };
 
+__device__ __forceinline__ double eval_rule(const GhostItems &G, int i, const double *Q, const double *bcg, double hx,
+                                            double hy) {
+  constexpr double A1 = -1.0 / 5.0, A2 = 2.0 / 3.0, A3 = 8.0 / 15.0;
+  constexpr double B1 = 5.0 / 32.0, B2 = 15.0 / 16.0, B3 = -3.0 / 32.0;
+  const int a = G.a[i];
+  switch (G.type[i]) {
+    case G_COPY: return Q[a];
+    case G_QIF: return (A1 * Q[a] + A2 * Q[G.b[i]]) + A3 * Q[G.c[i]];
+    case G_QIF_END:
+      return (A1 * Q[a] + A2 * Q[G.b[i]]) + A3 * ((B1 * Q[G.c[i]] + B2 * Q[G.d[i]]) + B3 * Q[G.e[i]]);
+    case G_LIF: return ((2.0 / 3.0) * Q[G.c[i]] + (2.0 / 3.0) * Q[a]) - (1.0 / 3.0) * Q[G.b[i]];
+    case G_LIF_CORNER: return (2.0 / 3.0) * Q[G.c[i]] + (1.0 / 3.0) * Q[a];
+    case G_DIRICHLET: return ((8.0 / 3.0) * bcg[G.e[i]] - 2 * Q[a]) + (1.0 / 3.0) * Q[G.b[i]];
+    default: return Q[a] + (G.b[i] ? hy : hx) * bcg[G.e[i]];   // G_NEUMANN
+  }
+}
+
 __global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, double *__restrict__ Q,
                                                   double *__restrict__ QC, const double *__restrict__ bcg,
                                                   double hx, double hy) {
+  chain_trigger();
   const int t = blockIdx.x * kBlock + threadIdx.x;
-  if (t >= n) return;
   const int i = off + t;
-  const int8_t ty = G.type[i];
-  const int dst = G.dst[i], a = G.a[i];
+  const int8_t ty = (t < n) ? G.type[i] : (int8_t)-1;
+  const int dst = (t < n) ? G.dst[i] : 0;
+  chain_wait();
+  if (t >= n) return;
+  if (ty == G_RING) {
+    QC[dst] = Q[G.a[i]];
+  } else if (ty == G_PHYS_CORNER) {
+    // (face ghost 1 + face ghost 2) - interior, the face ghosts evaluated by
+    // their own final rules (ebFillGhosts.m:84-89 reads them after stage 3)
+    const double v1 = eval_rule(G, G.a[i], Q, bcg, hx, hy);
+    const double v2 = eval_rule(G, G.b[i], Q, bcg, hx, hy);
+    Q[dst] = (v1 + v2) - Q[G.c[i]];
+  } else {
+    Q[dst] = eval_rule(G, i, Q, bcg, hx, hy);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// relax2d (EllipticBSAM/src/ebKernels.m:37-95): one colour of the red-black
+// Gauss-Seidel sweep over all patches of a level, one thread per cell of
+// the colour.  The colour cells of each patch are cut into chunks of
+// kChunk that never straddle two patches; a chunk record carries everything
+// a thread needs about its patch, so one load precedes the data loads.
+// Partial physical ghosts ((8/3)g + (1/3)u_2 Dirichlet, h g Neumann) are
+// formed in registers, the u_1 coupling being folded into InvDiagS.  The
+// reference refills every ghost after each colour (ebRelaxLevel.m:36); with
+// `fresh` set, a boundary thread instead evaluates its neighbour ghost's
+// rule (stored inline per perimeter cell): every rule of an internal face
+// reads only cells of the other colour (final after the previous pass),
+// parent cells, or the reading cell itself (pre-update), so the value equals
+// the refilled ghost bit for bit.  The first pass of a relaxation reads the
+// ghosts as the last fill left them, as the reference does.
+constexpr int kChunk = 64;
+
+struct RelaxChunk {
+  int q_off, c_off, dew_off, dns_off;
+  int bcg_off, pe_off, mx, my;
+  int par0, s0, n, pad;      // first colour-cell index in the patch, cells in the chunk
+  int bc[4];
+};
+
+struct Rule {                // one ghost rule, inline (perimeter table)
+  int type, a, b, c, d, e;
+};
+
+__device__ __forceinline__ double eval_inline(const Rule &R, const double *Q) {
   constexpr double A1 = -1.0 / 5.0, A2 = 2.0 / 3.0, A3 = 8.0 / 15.0;
   constexpr double B1 = 5.0 / 32.0, B2 = 15.0 / 16.0, B3 = -3.0 / 32.0;
-  double v;
-  switch (ty) {
-    case G_COPY: v = Q[a]; break;
-    case G_QIF: v = (A1 * Q[a] + A2 * Q[G.b[i]]) + A3 * Q[G.c[i]]; break;
-    case G_QIF_END:
-      v = (A1 * Q[a] + A2 * Q[G.b[i]]) + A3 * ((B1 * Q[G.c[i]] + B2 * Q[G.d[i]]) + B3 * Q[G.e[i]]);
-      break;
-    case G_LIF: v = ((2.0 / 3.0) * Q[G.c[i]] + (2.0 / 3.0) * Q[a]) - (1.0 / 3.0) * Q[G.b[i]]; break;
-    case G_LIF_CORNER: v = (2.0 / 3.0) * Q[G.c[i]] + (1.0 / 3.0) * Q[a]; break;
-    case G_DIRICHLET: v = ((8.0 / 3.0) * bcg[G.e[i]] - 2 * Q[a]) + (1.0 / 3.0) * Q[G.b[i]]; break;
-    case G_NEUMANN: v = Q[a] + (G.b[i] ? hy : hx) * bcg[G.e[i]]; break;
-    case G_RING: QC[dst] = Q[a]; return;
-    default: v = (Q[a] + Q[G.b[i]]) - Q[G.c[i]]; break;  // G_PHYS_CORNER
+  switch (R.type) {
+    case G_COPY: return Q[R.a];
+    case G_QIF: return (A1 * Q[R.a] + A2 * Q[R.b]) + A3 * Q[R.c];
+    case G_QIF_END: return (A1 * Q[R.a] + A2 * Q[R.b]) + A3 * ((B1 * Q[R.c] + B2 * Q[R.d]) + B3 * Q[R.e]);
+    default: return ((2.0 / 3.0) * Q[R.c] + (2.0 / 3.0) * Q[R.a]) - (1.0 / 3.0) * Q[R.b];   // G_LIF
   }
-  Q[dst] = v;
+}
+
+template <bool kPow2>
+__global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__restrict__ chunks, int nchunks, Fields f,
+                                                  const Rule *__restrict__ perim, int m, double omega, int unit_omega,
+                                                  int fresh) {
+  chain_trigger();
+  const int ch = blockIdx.x * (kBlock / kChunk) + threadIdx.x / kChunk;
+  bool ok = ch < nchunks;
+  RelaxChunk R;
+  if (ok) R = chunks[ch];
+  const int s = ok ? R.s0 + (threadIdx.x & (kChunk - 1)) : 0;
+  ok = ok && s < R.s0 + R.n;
+  if (!ok) {
+    chain_wait();
+    return;
+  }
+  const int mx = R.mx, my = R.my, half = mx >> 1;
+  const int lj = s / half;
+  const int li = 2 * (s - lj * half) + ((m + lj + R.par0) & 1);
+  const int ldq = mx + 2;
+  const int c = (li + 1) + (lj + 1) * ldq;
+  const int cc = R.c_off + li + lj * mx;
+  // static operands: coefficients, diagonal, boundary data, ghost rules
+  const double *__restrict__ DeW = f.DeW + R.dew_off;
+  const double *__restrict__ DnS = f.DnS + R.dns_off;
+  const double dE = __ldg(DeW + (li + 1) + lj * (mx + 1)), dW = __ldg(DeW + li + lj * (mx + 1));
+  const double dN = __ldg(DnS + li + (lj + 1) * mx), dS = __ldg(DnS + li + lj * mx);
+  const double idg = __ldg(f.ID + cc);
+  const double *__restrict__ g4 = f.bcg + R.bcg_off;
+  // a cell touches at most one x side (W or E) and one y side (S or N):
+  // kind 0 interior neighbour, 1 Dirichlet, 2 Neumann, 3 ghost rule
+  int kx = 0, ky = 0, sx = 0, sy = 0;       // sx: 0 west 1 east; sy: 0 south 1 north
+  double gx = 0, gy = 0;
+  Rule rx, ry;
+  if (li == 0 || li == mx - 1) {
+    sx = (li == 0) ? 0 : 1;
+    const int bc = R.bc[sx];
+    if (bc) { kx = bc; gx = __ldg(g4 + sx * my + lj); }
+    else if (fresh) { kx = 3; rx = perim[R.pe_off + sx * my + lj]; }
+  }
+  if (lj == 0 || lj == my - 1) {
+    sy = (lj == 0) ? 0 : 1;
+    const int bc = R.bc[2 + sy];
+    if (bc) { ky = bc; gy = __ldg(g4 + 2 * my + sy * mx + li); }
+    else if (fresh) { ky = 3; ry = perim[R.pe_off + 2 * my + sy * mx + li]; }
+  }
+  chain_wait();
+  double *__restrict__ Q = f.Q + R.q_off;
+  double qe = Q[c + 1], qw = Q[c - 1], qn = Q[c + ldq], qs = Q[c - ldq];
+  if (kx > 0) {
+    double v;
+    if (kx == 1) v = (8.0 / 3.0) * gx + (1.0 / 3.0) * Q[sx ? c - 1 : c + 1];
+    else if (kx == 2) v = L.hx * gx;
+    else v = eval_inline(rx, f.Q);
+    if (sx) qe = v; else qw = v;
+  }
+  if (ky > 0) {
+    double v;
+    if (ky == 1) v = (8.0 / 3.0) * gy + (1.0 / 3.0) * Q[sy ? c - ldq : c + ldq];
+    else if (ky == 2) v = L.hy * gy;
+    else v = eval_inline(ry, f.Q);
+    if (sy) qn = v; else qs = v;
+  }
+  double t = f.F[cc];
+  t = t + divh<kPow2>(qe * dE, L.hx2, L.ihx2);
+  t = t + divh<kPow2>(qw * dW, L.hx2, L.ihx2);
+  t = t + divh<kPow2>(qn * dN, L.hy2, L.ihy2);
+  t = t + divh<kPow2>(qs * dS, L.hy2, L.ihy2);
+  t = t * idg;
+  if (unit_omega) Q[c] = t;
+  else Q[c] = omega * t + (1 - omega) * Q[c];
 }
 
 // ---------------------------------------------------------------------------
 // restrict2 (ebKernels.m:98-102) of each patch interior into its QC interior
 // and, for 'restrict' (ebTransfer.m:10-33), into the parent's Q over the
 // footprint.  One thread per coarse cell.
-__global__ void __launch_bounds__(kBlock) k_restrict(LevelD L, Decomp D, Fields f, int to_parent) {
-  const int g = blockIdx.x * kBlock + threadIdx.x;
-  if (g >= D.n) return;
-  const int p = find_patch(D, g);
-  const PatchD &P = L.patches[p];
-  const int cmx = P.mx >> 1;
-  const int s = g - __ldg(D.beg + p);
-  const int cj = s / cmx, ci = s - cj * cmx;
-  const int ldq = P.mx + 2;
-  const double *__restrict__ Q = f.Q + P.q_off;
+__device__ __forceinline__ double restrict_cell(const double *Q, int ldq, int ci, int cj) {
   const int c = (2 * ci + 1) + (2 * cj + 1) * ldq;
-  const double R = 0.25 * (((Q[c] + Q[c + 1]) + Q[c + ldq]) + Q[c + ldq + 1]);
-  f.QC[P.qc_off + (ci + 1) + (cj + 1) * (cmx + 2)] = R;
-  if (to_parent) f.Q[__ldg(f.fp + 2 * (P.fp_off + s))] = R;
+  return 0.25 * (((Q[c] + Q[c + 1]) + Q[c + ldq]) + Q[c + ldq + 1]);
 }
 
-// QC ring <- parent Q (ebTransfer.m:35-55 'ring'), one thread per ring cell
-__global__ void __launch_bounds__(kBlock) k_ring(const int *__restrict__ ring, int off, int n, const double *Q,
-                                                 double *__restrict__ QC) {
-  const int t = blockIdx.x * kBlock + threadIdx.x;
-  if (t >= n) return;
-  const int i = off + t;
-  QC[__ldg(ring + 2 * i + 1)] = Q[__ldg(ring + 2 * i)];
-}
-
-// ---------------------------------------------------------------------------
-// FAS coarse load over the footprint (ebCoarseLoad.m:17-32 with
-// ebParentCoeffs.m): F_parent = restrict2(F - op(Q)) + op_c(QC, parent coeffs).
-// One thread per coarse cell; the four fine residuals are summed in the
-// restrict2 order (1,1), (2,1), (1,2), (2,2).
-template <bool kPow2>
-__global__ void __launch_bounds__(kBlock) k_coarse_load(LevelD L, LevelD Lc, Decomp D, Fields f) {
+__global__ void __launch_bounds__(kBlock) k_restrict(LevelD L, Decomp D, Fields f, int to_parent) {
+  chain_trigger();
   const int g = blockIdx.x * kBlock + threadIdx.x;
-  if (g >= D.n) return;
-  const int p = find_patch(D, g);
+  if (g >= D.n) {
+    chain_wait();
+    return;
+  }
+  const int p = find_patch(D, blockIdx.x, g);
   const PatchD &P = L.patches[p];
-  const int mx = P.mx, cmx = mx >> 1, cmy = P.my >> 1;
+  const int cmx = P.mx >> 1, q_off = P.q_off, ldq = P.mx + 2, qc_off = P.qc_off;
   const int s = g - __ldg(D.beg + p);
   const int cj = s / cmx, ci = s - cj * cmx;
-  const double *Qp = f.Q + P.q_off;
-  const double *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off;
-  const double *Fp = f.F + P.c_off, *CC = f.CC + P.c_off;
-  double rf[4];
-#pragma unroll
-  for (int t = 0; t < 4; ++t) {
-    const int li = 2 * ci + (t & 1), lj = 2 * cj + (t >> 1);
-    const int cc = li + lj * mx;
-    rf[t] = Fp[cc] - op_cell<kPow2>(Qp, mx + 2, DeW, DnS, CC[cc], mx, li, lj, L.hx2, L.hy2, L.ihx2, L.ihy2);
-  }
-  const double rr = 0.25 * (((rf[0] + rf[1]) + rf[2]) + rf[3]);
-  const double *PDeW = f.pcoef + P.pc_off;
-  const double *PDnS = PDeW + (cmx + 1) * cmy;
-  const double *PCC = PDnS + cmx * (cmy + 1);
-  const double lc = op_cell<kPow2>(f.QC + P.qc_off, cmx + 2, PDeW, PDnS, PCC[s], cmx, ci, cj, Lc.hx2, Lc.hy2,
-                                   Lc.ihx2, Lc.ihy2);
-  f.F[__ldg(f.fp + 2 * (P.fp_off + s) + 1)] = rr + lc;
+  const int dst = to_parent ? __ldg(f.fp + 2 * (P.fp_off + s)) : 0;
+  chain_wait();
+  const double R = restrict_cell(f.Q + q_off, ldq, ci, cj);
+  f.QC[qc_off + (ci + 1) + (cj + 1) * (cmx + 2)] = R;
+  if (to_parent) f.Q[dst] = R;
 }
-
+// ---------------------------------------------------------------------------
 // ebFaceCorrections (ebFaceCorrections.m:18-61): correction of coarse face j
-// on face fc (0 W, 1 E, 2 S, 3 N) of patch P; hc2 is the parent h^2 in the
-// face-normal direction
-template <bool kPow2>
-__device__ __forceinline__ double face_corr(const PatchD &P, const Fields &f, int fc, int j, double hc2,
-                                            double ihc2) {
+// on face fc (0 W, 1 E, 2 S, 3 N) of patch P.  The coarse values are read
+// where the reference's QC holds them: the outer (ring) cell from the
+// parent's Q through the window table, the inner cell from QC's interior
+// (`qc_inner` false) or recomputed as the restriction of its four fine cells
+// (`qc_inner` true: the residual's refresh, ebCompResidual.m:32-38).
+__device__ __forceinline__ double face_corr(const PatchD &P, const Fields &f, int fc, int j, double hc2, double ihc2,
+                                            int pow2, bool qc_inner) {
   const int mx = P.mx, my = P.my, cmx = mx >> 1, cmy = my >> 1;
   const int ldq = mx + 2, ldc = cmx + 2;
   const double *Q = f.Q + P.q_off, *QC = f.QC + P.qc_off;
+  const int *win = f.win + P.win_off;
   const double *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off, *cfd = f.cfd + P.cfd_off;
-  // 0-based padded indices; fine rows 2j+1, 2j+2 of the padded array
   double v;
   switch (fc) {
     case 0: {
       const int r1 = 2 * j + 1, r2 = 2 * j + 2;
+      const double out = f.Q[win[(j + 1) * ldc]];
+      const double in = qc_inner ? restrict_cell(Q, ldq, 0, j) : QC[1 + (j + 1) * ldc];
       v = (DeW[(2 * j) * (mx + 1)] * (Q[1 + r1 * ldq] - Q[r1 * ldq]) +
            DeW[(2 * j + 1) * (mx + 1)] * (Q[1 + r2 * ldq] - Q[r2 * ldq])) +
-          cfd[j] * (QC[(j + 1) * ldc] - QC[1 + (j + 1) * ldc]);
+          cfd[j] * (out - in);
       break;
     }
     case 1: {
       const int r1 = 2 * j + 1, r2 = 2 * j + 2;
+      const double out = f.Q[win[cmx + 1 + (j + 1) * ldc]];
+      const double in = qc_inner ? restrict_cell(Q, ldq, cmx - 1, j) : QC[cmx + (j + 1) * ldc];
       v = (DeW[mx + (2 * j) * (mx + 1)] * (Q[mx + r1 * ldq] - Q[mx + 1 + r1 * ldq]) +
            DeW[mx + (2 * j + 1) * (mx + 1)] * (Q[mx + r2 * ldq] - Q[mx + 1 + r2 * ldq])) +
-          cfd[cmy + j] * (QC[cmx + 1 + (j + 1) * ldc] - QC[cmx + (j + 1) * ldc]);
+          cfd[cmy + j] * (out - in);
       break;
     }
     case 2: {
       const int c1 = 2 * j + 1, c2 = 2 * j + 2;
-      v = (DnS[2 * j] * (Q[c1 + ldq] - Q[c1]) + DnS[2 * j + 1] * (Q[c2 + ldq] - Q[c2])) +
-          cfd[2 * cmy + j] * (QC[j + 1] - QC[j + 1 + ldc]);
+      const double out = f.Q[win[j + 1]];
+      const double in = qc_inner ? restrict_cell(Q, ldq, j, 0) : QC[j + 1 + ldc];
+      v = (DnS[2 * j] * (Q[c1 + ldq] - Q[c1]) + DnS[2 * j + 1] * (Q[c2 + ldq] - Q[c2])) + cfd[2 * cmy + j] * (out - in);
       break;
     }
     default: {
       const int c1 = 2 * j + 1, c2 = 2 * j + 2;
+      const double out = f.Q[win[j + 1 + (cmy + 1) * ldc]];
+      const double in = qc_inner ? restrict_cell(Q, ldq, j, cmy - 1) : QC[j + 1 + cmy * ldc];
       v = (DnS[2 * j + my * mx] * (Q[c1 + my * ldq] - Q[c1 + (my + 1) * ldq]) +
            DnS[2 * j + 1 + my * mx] * (Q[c2 + my * ldq] - Q[c2 + (my + 1) * ldq])) +
-          cfd[2 * cmy + cmx + j] * (QC[j + 1 + (cmy + 1) * ldc] - QC[j + 1 + cmy * ldc]);
+          cfd[2 * cmy + cmx + j] * (out - in);
       break;
     }
   }
-  return divh<kPow2>(v, hc2, ihc2);
+  return divr(v, hc2, ihc2, pow2);
 }
 
-// Flux-balance corrections (ebCoarseLoad.m:37-45) in gather form: one thread
-// per target coarse cell adds its corrections in the reference's order
-// (fine patch ascending, faces W, E, S, N).  `items` encode
-// (level-local patch << 2 | face) and `jj` the coarse face index.
-template <bool kPow2>
-__global__ void __launch_bounds__(kBlock) k_corr(LevelD L, LevelD Lc, Fields f, const int *__restrict__ tcell,
-                                                 const int *__restrict__ tbeg, const int *__restrict__ items,
-                                                 const int *__restrict__ jj, int n) {
-  const int t = blockIdx.x * kBlock + threadIdx.x;
-  if (t >= n) return;
-  const int cell = tcell[t];
-  double v = f.F[cell];
-  for (int i = tbeg[t]; i < tbeg[t + 1]; ++i) {
-    const int it = items[i];
+// gather-form corrections of one target coarse cell: contributions in the
+// reference's order (fine patch ascending, faces W, E, S, N)
+struct CorrCSR {
+  const int *cell, *patch, *beg, *item, *jj;   // item = (level-local fine patch << 2) | face
+};
+
+__device__ __forceinline__ double add_corrections(double v, const CorrCSR &C, int t, const LevelD &Lf, const LevelD &Lc,
+                                                  const Fields &f, bool qc_inner) {
+  for (int i = C.beg[t]; i < C.beg[t + 1]; ++i) {
+    const int it = C.item[i];
     const int fc = it & 3;
-    const PatchD &P = L.patches[it >> 2];
-    v = v + face_corr<kPow2>(P, f, fc, jj[i], fc < 2 ? Lc.hx2 : Lc.hy2, fc < 2 ? Lc.ihx2 : Lc.ihy2);
+    v = v + face_corr(Lf.patches[it >> 2], f, fc, C.jj[i], fc < 2 ? Lc.hx2 : Lc.hy2, fc < 2 ? Lc.ihx2 : Lc.ihy2,
+                      Lc.pow2, qc_inner);
   }
-  f.F[cell] = v;
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// FAS coarse load of level k (ebVcycle.m:28-29): one launch with three block
+// ranges --
+//   [0, nb_ring)            QC ring <- parent Q      (ebTransfer.m:35-55)
+//   [nb_ring, +D.nblocks)   F_parent = restrict2(F - op(Q)) + op_c(QC, parent
+//                           coefficients) over the footprint (ebCoarseLoad.m:17-32,
+//                           ebParentCoeffs.m), the four fine residuals summed in
+//                           restrict2 order (1,1), (2,1), (1,2), (2,2)
+//   [.., +nb_tgt)           F_target = F_target + corrections (ebCoarseLoad.m:37-45)
+// QC ring values are read from the parent's Q through the window table, so
+// the three ranges are independent.
+// op2d at one cell from preloaded face coefficients (same operation order
+// as op_cell)
+__device__ __forceinline__ double op_pre(double q, double qe, double qw, double qn, double qs, double dE, double dW,
+                                         double dN, double dS, double cc, const LevelD &L) {
+  const double feE = dE * (qe - q), feW = dW * (q - qw), fnN = dN * (qn - q), fnS = dS * (q - qs);
+  return (divr(-(feE - feW), L.hx2, L.ihx2, L.pow2) - divr(fnN - fnS, L.hy2, L.ihy2, L.pow2)) + cc * q;
+}
+
+__global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, Fields f, const int *__restrict__ ring,
+                                                 int ring_off, int n_ring, CorrCSR C, int n_tgt) {
+  chain_trigger();
+  const int nb_ring = (n_ring + kBlock - 1) / kBlock;
+  int b = blockIdx.x;
+  if (b < nb_ring) {
+    const int t = b * kBlock + threadIdx.x;
+    int src = 0, dst = 0;
+    if (t < n_ring) {
+      src = __ldg(ring + 2 * (ring_off + t));
+      dst = __ldg(ring + 2 * (ring_off + t) + 1);
+    }
+    chain_wait();
+    if (t < n_ring) f.QC[dst] = f.Q[src];
+    return;
+  }
+  b -= nb_ring;
+  if (b < D.nblocks) {
+    const int g = b * kBlock + threadIdx.x;
+    if (g >= D.n) {
+      chain_wait();
+      return;
+    }
+    const int p = find_patch(D, b, g);
+    const PatchD &P = L.patches[p];
+    const int mx = P.mx, cmx = mx >> 1, cmy = P.my >> 1, ldq = mx + 2;
+    const int s = g - __ldg(D.beg + p);
+    const int cj = s / cmx, ci = s - cj * cmx;
+    const int q_off = P.q_off, c_off = P.c_off, qc_off = P.qc_off;
+    // static operands of the four fine cells (restrict2 order) and of the
+    // coarse operator
+    const double *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off, *CC = f.CC + c_off;
+    double dE[4], dW[4], dN[4], dS[4], cf[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int li = 2 * ci + (t & 1), lj = 2 * cj + (t >> 1);
+      dE[t] = __ldg(DeW + (li + 1) + lj * (mx + 1));
+      dW[t] = __ldg(DeW + li + lj * (mx + 1));
+      dN[t] = __ldg(DnS + li + (lj + 1) * mx);
+      dS[t] = __ldg(DnS + li + lj * mx);
+      cf[t] = __ldg(CC + li + lj * mx);
+    }
+    const int ldc = cmx + 2;
+    const int *win = f.win + P.win_off;
+    const int w = (ci + 1) + (cj + 1) * ldc;
+    // ring neighbours of the coarse operator come from the parent's Q
+    const int se = (ci == cmx - 1) ? __ldg(win + w + 1) : -1;
+    const int sw = (ci == 0) ? __ldg(win + w - 1) : -1;
+    const int sn = (cj == cmy - 1) ? __ldg(win + w + ldc) : -1;
+    const int ss = (cj == 0) ? __ldg(win + w - ldc) : -1;
+    const double *PDeW = f.pcoef + P.pc_off;
+    const double *PDnS = PDeW + (cmx + 1) * cmy;
+    const double *PCC = PDnS + cmx * (cmy + 1);
+    const double pE = __ldg(PDeW + (ci + 1) + cj * (cmx + 1)), pW = __ldg(PDeW + ci + cj * (cmx + 1));
+    const double pN = __ldg(PDnS + ci + (cj + 1) * cmx), pS = __ldg(PDnS + ci + cj * cmx);
+    const double pC = __ldg(PCC + s);
+    const int dst = __ldg(f.fp + 2 * (P.fp_off + s) + 1);
+    chain_wait();
+    const double *Qp = f.Q + q_off;
+    const double *Fp = f.F + c_off;
+    double rf[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int li = 2 * ci + (t & 1), lj = 2 * cj + (t >> 1);
+      const int c = (li + 1) + (lj + 1) * ldq;
+      rf[t] = Fp[li + lj * mx] - op_pre(Qp[c], Qp[c + 1], Qp[c - 1], Qp[c + ldq], Qp[c - ldq], dE[t], dW[t], dN[t],
+                                        dS[t], cf[t], L);
+    }
+    const double rr = 0.25 * (((rf[0] + rf[1]) + rf[2]) + rf[3]);
+    const double *QC = f.QC + qc_off;
+    const double q = QC[w];
+    const double qe = se >= 0 ? f.Q[se] : QC[w + 1];
+    const double qw = sw >= 0 ? f.Q[sw] : QC[w - 1];
+    const double qn = sn >= 0 ? f.Q[sn] : QC[w + ldc];
+    const double qs = ss >= 0 ? f.Q[ss] : QC[w - ldc];
+    const double lc = op_pre(q, qe, qw, qn, qs, pE, pW, pN, pS, pC, Lc);
+    f.F[dst] = rr + lc;
+    return;
+  }
+  b -= D.nblocks;
+  const int t = b * kBlock + threadIdx.x;
+  const int cell = t < n_tgt ? C.cell[t] : 0;
+  chain_wait();
+  if (t >= n_tgt) return;
+  f.F[cell] = add_corrections(f.F[cell], C, t, L, Lc, f, false);
 }
 
 // ---------------------------------------------------------------------------
@@ -270,23 +460,34 @@ __global__ void __launch_bounds__(kBlock) k_corr(LevelD L, LevelD Lc, Fields f, 
 // (new-level initial guess, ebAddLevel.m:26-31).  One thread per coarse cell
 // writes its four fine cells.
 __global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, Fields f, int correct) {
+  chain_trigger();
   const int g = blockIdx.x * kBlock + threadIdx.x;
-  if (g >= D.n) return;
-  const int p = find_patch(D, g);
+  if (g >= D.n) {
+    chain_wait();
+    return;
+  }
+  const int p = find_patch(D, blockIdx.x, g);
   const PatchD &P = L.patches[p];
   const int cm = P.mx >> 1;
   const int s = g - __ldg(D.beg + p);
   const int b = s / cm, a = s - b * cm;
   const int ldw = cm + 2;
   const int *win = f.win + P.win_off;
-  const double *QC = f.QC + P.qc_off;
+  int src[3][3];
+#pragma unroll
+  for (int dj = 0; dj < 3; ++dj)
+#pragma unroll
+    for (int di = 0; di < 3; ++di) src[dj][di] = __ldg(win + (a + di) + (b + dj) * ldw);
+  const int qc_off = P.qc_off, q_off = P.q_off, ldq = P.mx + 2;
+  chain_wait();
+  const double *QC = f.QC + qc_off;
   double E[3][3];
 #pragma unroll
   for (int dj = 0; dj < 3; ++dj)
 #pragma unroll
     for (int di = 0; di < 3; ++di) {
       const int w = (a + di) + (b + dj) * ldw;
-      const double wv = f.Q[__ldg(win + w)];
+      const double wv = f.Q[src[dj][di]];
       E[dj][di] = correct ? wv - QC[w] : wv;
     }
   const double C = E[1][1], Wm = E[1][0], Wp = E[1][2], Sm = E[0][1], Sp = E[2][1];
@@ -294,8 +495,7 @@ __global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, Fields f
   const double f21 = (((9 * C + 3 * Wp) + 3 * Sm) + E[0][2]) / 16;
   const double f12 = (((9 * C + 3 * Wm) + 3 * Sp) + E[2][0]) / 16;
   const double f22 = (((9 * C + 3 * Wp) + 3 * Sp) + E[2][2]) / 16;
-  const int ldq = P.mx + 2;
-  double *Q = f.Q + P.q_off;
+  double *Q = f.Q + q_off;
   const int c = (2 * a + 1) + (2 * b + 1) * ldq;
   if (correct) {
     Q[c] = Q[c] + f11;
@@ -315,13 +515,31 @@ __global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, Fields f
 // row; lane l sums columns l, l+32, ... in order, then a halving tree.
 __global__ void __launch_bounds__(kBlock) k_coarsest(const double *__restrict__ Ainv, const double *__restrict__ bcRhs,
                                                      Fields f, int c_off, int q_off, int n1, int N) {
+  chain_trigger();
   const int row = (blockIdx.x * kBlock + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (row >= N) return;
+  if (row >= N) {
+    chain_wait();
+    return;
+  }
   const double *a = Ainv + (size_t)row * N;
+  constexpr int kPre = 8;   // inverse entries held in registers (N <= 256)
+  double av[kPre], bv[kPre];
+#pragma unroll
+  for (int i = 0; i < kPre; ++i) {
+    const int c = lane + 32 * i;
+    av[i] = c < N ? __ldg(a + c) : 0.0;
+    bv[i] = c < N ? __ldg(bcRhs + c) : 0.0;
+  }
+  chain_wait();
   const double *F = f.F + c_off;
   double s = 0.0;
-  for (int c = lane; c < N; c += 32) s = s + a[c] * (F[c] + bcRhs[c]);
+#pragma unroll
+  for (int i = 0; i < kPre; ++i) {
+    const int c = lane + 32 * i;
+    if (c < N) s = s + av[i] * (F[c] + bv[i]);
+  }
+  for (int c = lane + 32 * kPre; c < N; c += 32) s = s + a[c] * (F[c] + bcRhs[c]);
 #pragma unroll
   for (int off = 16; off >= 1; off >>= 1) {
     const double o = __shfl_down_sync(0xffffffffu, s, off);
@@ -334,17 +552,36 @@ __global__ void __launch_bounds__(kBlock) k_coarsest(const double *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// Composite residual (ebCompResidual.m:54-83): r = FTrue - op(Q) on visible
-// cells; correction targets are skipped here and handled by
-// k_residual_targets.  Max-norms reduce through an order-free atomic max on
-// the bit pattern of non-negative doubles; the L2 sum keeps one partial per
-// block in a fixed slot.
+// Composite residual (ebCompResidual.m:15-85) of every level >= root in one
+// launch.  Segments (block ranges) of four kinds:
+//   0  r = FTrue - op(Q) on the visible cells of a level, correction targets
+//      excluded while the corrections are on
+//   1  r at the level's correction targets, corrections added in order, the
+//      coarse values taken as the refreshed QC holds them
+//   2  QC ring refresh of a level (ebCompResidual.m:25)
+//   3  QC interior refresh of a level (ebCompResidual.m:32-38)
+// Max-norms reduce through an order-free atomic max on the bit pattern of
+// non-negative doubles; the L2 sum keeps one partial per residual block in a
+// fixed slot.
 struct ResAcc {
-  unsigned long long linf_bits, fnorm_bits;
   double out[5];        // linf, l2, fnorm, rel, ncell
 };
 
-__device__ __forceinline__ void block_reduce_store(double li, double sq, double fn, ResAcc *acc, double *slot) {
+struct ResSeg {
+  int kind, level, block0, slot0;
+};
+
+struct LevelX {
+  LevelD L;
+  Decomp cell, coarse;
+  CorrCSR C;            // corrections contributed by this (fine) level
+  int ct_n, ring_off, ring_n, pad;
+};
+
+// per residual block: max |r|, sum r^2, max |FTrue| of its 256 cells, in a
+// fixed warp-tree order
+__device__ __forceinline__ void block_reduce_store(double li, double sq, double fn, double *slot_li, double *slot_sq,
+                                                   double *slot_fn) {
   __shared__ double s_li[kBlock / 32], s_sq[kBlock / 32], s_fn[kBlock / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -356,105 +593,160 @@ __device__ __forceinline__ void block_reduce_store(double li, double sq, double 
   if (lane == 0) { s_li[w] = li; s_sq[w] = sq; s_fn[w] = fn; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double L = s_li[0], S = s_sq[0], Fn = s_fn[0];
-    for (int i = 1; i < kBlock / 32; ++i) { L = fmax(L, s_li[i]); S = S + s_sq[i]; Fn = fmax(Fn, s_fn[i]); }
-    atomicMax(&acc->linf_bits, (unsigned long long)__double_as_longlong(L));
-    atomicMax(&acc->fnorm_bits, (unsigned long long)__double_as_longlong(Fn));
-    *slot = S;
+    double Lm = s_li[0], S = s_sq[0], Fn = s_fn[0];
+    for (int i = 1; i < kBlock / 32; ++i) { Lm = fmax(Lm, s_li[i]); S = S + s_sq[i]; Fn = fmax(Fn, s_fn[i]); }
+    *slot_li = Lm;
+    *slot_sq = S;
+    *slot_fn = Fn;
   }
 }
 
-template <bool kPow2>
-__global__ void __launch_bounds__(kBlock) k_residual(LevelD L, Decomp D, Fields f, ResAcc *acc, double *slots,
-                                                     int skip_targets) {
-  const int g = blockIdx.x * kBlock + threadIdx.x;
+__global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ X, const ResSeg *__restrict__ segs,
+                                                     const unsigned char *__restrict__ blk_seg, Fields f,
+                                                     const int *__restrict__ ring, double *slots, int nslots,
+                                                     int mass_corr) {
+  chain_trigger();
+  const ResSeg S = segs[blk_seg[blockIdx.x]];
+  const int b = blockIdx.x - S.block0;
+  const int g = b * kBlock + threadIdx.x;
+  const LevelX &Xk = X[S.level];
+  if (S.kind >= 2) {
+    chain_wait();
+    if (!mass_corr) return;
+    if (S.kind == 2) {
+      if (g < Xk.ring_n) {
+        const int i = Xk.ring_off + g;
+        f.QC[__ldg(ring + 2 * i + 1)] = f.Q[__ldg(ring + 2 * i)];
+      }
+      return;
+    }
+    if (g >= Xk.coarse.n) return;
+    const int p = find_patch(Xk.coarse, b, g);
+    const PatchD &P = Xk.L.patches[p];
+    const int cmx = P.mx >> 1;
+    const int s = g - __ldg(Xk.coarse.beg + p);
+    const int cj = s / cmx, ci = s - cj * cmx;
+    f.QC[P.qc_off + (ci + 1) + (cj + 1) * (cmx + 2)] = restrict_cell(f.Q + P.q_off, P.mx + 2, ci, cj);
+    return;
+  }
   double li = 0, sq = 0, fn = 0;
-  if (g < D.n) {
-    const int p = find_patch(D, g);
-    const PatchD &P = L.patches[p];
-    const int mx = P.mx;
-    const int s = g - __ldg(D.beg + p);
-    const int lj = s / mx, lx = s - lj * mx;
-    const int cc = P.c_off + s;
-    const uint8_t fl = f.flags[cc];
-    // covered cells are not part of the composite norm; correction targets
-    // are evaluated by k_residual_targets when the corrections are on
-    if (!(fl & 1) && !(skip_targets && (fl & 2))) {
-      const double ft = f.FTrue[cc];
-      const double r = ft - op_cell<kPow2>(f.Q + P.q_off, mx + 2, f.DeW + P.dew_off, f.DnS + P.dns_off, f.CC[cc],
-                                           mx, lx, lj, L.hx2, L.hy2, L.ihx2, L.ihy2);
+  if (S.kind == 0) {
+    bool on = false;
+    int c = 0, ldq = 0, q_off = 0;
+    double ft = 0, dE = 0, dW = 0, dN = 0, dS = 0, cf = 0;
+    if (g < Xk.cell.n) {
+      const int p = find_patch(Xk.cell, b, g);
+      const PatchD &P = Xk.L.patches[p];
+      const int mx = P.mx;
+      const int s = g - __ldg(Xk.cell.beg + p);
+      const int lj = s / mx, lx = s - lj * mx;
+      const int cc = P.c_off + s;
+      const uint8_t fl = __ldg(f.flags + cc);
+      if (!(fl & 1) && !(mass_corr && (fl & 2))) {
+        on = true;
+        ft = __ldg(f.FTrue + cc);
+        const double *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off;
+        dE = __ldg(DeW + (lx + 1) + lj * (mx + 1));
+        dW = __ldg(DeW + lx + lj * (mx + 1));
+        dN = __ldg(DnS + lx + (lj + 1) * mx);
+        dS = __ldg(DnS + lx + lj * mx);
+        cf = __ldg(f.CC + cc);
+        ldq = mx + 2;
+        q_off = P.q_off;
+        c = (lx + 1) + (lj + 1) * ldq;
+      }
+    }
+    chain_wait();
+    if (on) {
+      const double *Qp = f.Q + q_off;
+      const double r = ft - op_pre(Qp[c], Qp[c + 1], Qp[c - 1], Qp[c + ldq], Qp[c - ldq], dE, dW, dN, dS, cf, Xk.L);
       li = fabs(r);
       sq = r * r;
       fn = fabs(ft);
     }
-  }
-  block_reduce_store(li, sq, fn, acc, slots + blockIdx.x);
-}
-
-// residual at correction targets of level k-1 (they are visible cells):
-// r = FTrue - op(Q) + corrections in order
-template <bool kPow2>
-__global__ void __launch_bounds__(kBlock) k_residual_targets(LevelD Lf, LevelD Lc, const PatchD *patches_c, Fields f,
-                                                             const int *__restrict__ tcell, const int *__restrict__ tpatch,
-                                                             const int *__restrict__ tbeg, const int *__restrict__ items,
-                                                             const int *__restrict__ jj, int n, ResAcc *acc,
-                                                             double *slots) {
-  const int t = blockIdx.x * kBlock + threadIdx.x;
-  double li = 0, sq = 0, fn = 0;
-  if (t < n) {
-    const int cell = tcell[t];
-    const PatchD &Pc = patches_c[tpatch[t]];
-    const int s = cell - Pc.c_off;
-    const int lj = s / Pc.mx, lx = s - lj * Pc.mx;
-    const double ft = f.FTrue[cell];
-    double r = ft - op_cell<kPow2>(f.Q + Pc.q_off, Pc.mx + 2, f.DeW + Pc.dew_off, f.DnS + Pc.dns_off, f.CC[cell],
-                                   Pc.mx, lx, lj, Lc.hx2, Lc.hy2, Lc.ihx2, Lc.ihy2);
-    for (int i = tbeg[t]; i < tbeg[t + 1]; ++i) {
-      const int it = items[i];
-      const int fc = it & 3;
-      r = r + face_corr<kPow2>(Lf.patches[it >> 2], f, fc, jj[i], fc < 2 ? Lc.hx2 : Lc.hy2,
-                               fc < 2 ? Lc.ihx2 : Lc.ihy2);
-    }
-    if (!(f.flags[cell] & 1)) {
-      li = fabs(r);
-      sq = r * r;
-      fn = fabs(ft);
+  } else {
+    chain_wait();   // kind 1: targets of this level, corrections from the level above
+    const LevelX &Xf = X[S.level + 1];
+    if (mass_corr && g < Xf.ct_n) {
+      const int cell = Xf.C.cell[g];
+      const PatchD &Pc = Xk.L.patches[Xf.C.patch[g]];
+      const int s = cell - Pc.c_off;
+      const int lj = s / Pc.mx, lx = s - lj * Pc.mx;
+      const double ft = f.FTrue[cell];
+      double r = ft - op_cell_r(f.Q + Pc.q_off, Pc.mx + 2, f.DeW + Pc.dew_off, f.DnS + Pc.dns_off, f.CC[cell], Pc.mx,
+                                lx, lj, Xk.L);
+      r = add_corrections(r, Xf.C, g, Xf.L, Xk.L, f, true);
+      if (!(f.flags[cell] & 1)) {
+        li = fabs(r);
+        sq = r * r;
+        fn = fabs(ft);
+      }
     }
   }
-  block_reduce_store(li, sq, fn, acc, slots + blockIdx.x);
+  const int sl = S.slot0 + b;
+  block_reduce_store(li, sq, fn, slots + sl, slots + nslots + sl, slots + 2 * nslots + sl);
 }
 
-// finish the residual: L2 from the per-block partials in slot order, each
-// level's partials weighted by its cell area; rel = linf / max(fnorm, realmin)
-__global__ void k_residual_final(ResAcc *acc, const double *slots, const int *level_slot0, const double *area,
-                                 int nlevels_res, double ncell) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// finish the residual in one block: max-norms over every residual block,
+// L2 per level from that level's block partials in a fixed tree order,
+// weighted by the level's cell area; rel = linf / max(fnorm, realmin)
+constexpr int kFinal = 512;
+__global__ void __launch_bounds__(kFinal) k_residual_final(ResAcc *acc, const double *slots, int nslots,
+                                                          const int *level_slot0, const double *area, int nlevels_res,
+                                                          double ncell) {
+  chain_in();
+  __shared__ double s_a[kFinal], s_b[kFinal];
+  const int t = threadIdx.x;
+  double li = 0, fn = 0;
+  for (int i = t; i < nslots; i += kFinal) {
+    li = fmax(li, slots[i]);
+    fn = fmax(fn, slots[2 * nslots + i]);
+  }
+  s_a[t] = li;
+  s_b[t] = fn;
+  __syncthreads();
+  for (int off = kFinal / 2; off >= 1; off >>= 1) {
+    if (t < off) {
+      s_a[t] = fmax(s_a[t], s_a[t + off]);
+      s_b[t] = fmax(s_b[t], s_b[t + off]);
+    }
+    __syncthreads();
+  }
+  const double linf = s_a[0];
+  double fnorm = s_b[0];
+  __syncthreads();
   double l2sq = 0;
   for (int l = 0; l < nlevels_res; ++l) {
     double s = 0;
-    for (int i = level_slot0[l]; i < level_slot0[l + 1]; ++i) s = s + slots[i];
-    l2sq = l2sq + s * area[l];
+    for (int i = level_slot0[l] + t; i < level_slot0[l + 1]; i += kFinal) s = s + slots[nslots + i];
+    s_a[t] = s;
+    __syncthreads();
+    for (int off = kFinal / 2; off >= 1; off >>= 1) {
+      if (t < off) s_a[t] = s_a[t] + s_a[t + off];
+      __syncthreads();
+    }
+    l2sq = l2sq + s_a[0] * area[l];
+    __syncthreads();
   }
-  const double linf = __longlong_as_double((long long)acc->linf_bits);
-  double fnorm = __longlong_as_double((long long)acc->fnorm_bits);
-  fnorm = fnorm > 2.2250738585072014e-308 ? fnorm : 2.2250738585072014e-308;
-  acc->out[0] = linf;
-  acc->out[1] = sqrt(l2sq);
-  acc->out[2] = fnorm;
-  acc->out[3] = linf / fnorm;
-  acc->out[4] = ncell;
-  acc->linf_bits = 0;
-  acc->fnorm_bits = 0;
+  if (t == 0) {
+    fnorm = fnorm > 2.2250738585072014e-308 ? fnorm : 2.2250738585072014e-308;
+    acc->out[0] = linf;
+    acc->out[1] = sqrt(l2sq);
+    acc->out[2] = fnorm;
+    acc->out[3] = linf / fnorm;
+    acc->out[4] = ncell;
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Composite sums over visible cells (ebCompositeMean.m, ebMassCheck.m lhs):
 // per-block partials of sum(u), sum(C u - FTrue), sum(|FTrue|)
 __global__ void __launch_bounds__(kBlock) k_sums(LevelD L, Decomp D, Fields f, double *partials) {
+  chain_in();
   const int g = blockIdx.x * kBlock + threadIdx.x;
   double su = 0, sm = 0, sa = 0, nv = 0;
   if (g < D.n) {
-    const int p = find_patch(D, g);
+    const int p = find_patch(D, blockIdx.x, g);
     const PatchD &P = L.patches[p];
     const int s = g - __ldg(D.beg + p);
     const int lj = s / P.mx, lx = s - lj * P.mx;
