@@ -12,9 +12,12 @@ composite residual 1e-10 (10 cycles).
   e2e     the same solves through the C-ABI with host buffers: per solve the
           initial guess and source go host->device, the solution and the
           residual history come back (pinned host memory).
-  roofline  the red-black smoother, algorithmic bytes 48 B per cell per
-          red+black sweep (24 B per colour pass), per-launch CUDA-event times
-          of eagerly launched V-cycles, against the measured HBM copy peak.
+  roofline  the red-black smoother on the finest level (the dominant kernel),
+          algorithmic bytes 48 B per cell per red+black sweep (24 B per colour
+          pass), per-launch CUDA-event times of eagerly launched V-cycles, on
+          the library's stream, against the measured HBM copy peak; `traffic`
+          is the DRAM bytes per launch of the same launch from the committed
+          ncu summary (profiles/k_relax_starfish_finest.md).
   cpu_baseline  the C oracle (a restatement of the reference's MATLAB path)
           on the host cores, a bounded sample of whole solves.
 
@@ -55,6 +58,16 @@ def starfish_hierarchy(backend):
         warnings.simplefilter('ignore')
         H = build_hierarchy(prob, opts, backend)
     return H, opts
+
+
+def load_traffic():
+    """DRAM bytes per finest-level smoother launch from the committed ncu summary."""
+    import re
+    p = os.path.join(ROOT, 'profiles', 'k_relax_starfish_finest.md')
+    if not os.path.exists(p):
+        return None
+    m = re.search(r'dram_bytes_per_launch:\s*([0-9.eE+]+)', open(p).read())
+    return float(m.group(1)) if m else None
 
 
 def load_peaks():
@@ -259,9 +272,12 @@ def main():
 
     # ---- roofline of the smoother -------------------------------------------
     prof = dh.profile(3)
+    fine = dh.profile(3, level=H.nlev)
     peak, peak_kind = load_peaks()
-    rl = prof['relax']
+    rl = fine['relax']
     achieved = rl['bytes'] / (rl['ms'] / 1e3) / 1e9
+    ra = prof['relax']
+    achieved_all = ra['bytes'] / (ra['ms'] / 1e3) / 1e9
     per_kind = {k: {'ms_per_cycle': v['ms'] / 3, 'launches_per_cycle': v['launches'] / 3} for k, v in prof.items()}
 
     if rank == 0:
@@ -289,10 +305,13 @@ def main():
                     'd2h_bytes_per_step': int(8 * Qout.size + hist_bytes),
                     'p50_ms': float(np.percentile(e2e_ms, 50)), 'p99_ms': float(np.percentile(e2e_ms, 99))},
             'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
-                         'frac': achieved / peak, 'traffic': None, 'peak_kind': peak_kind,
-                         'kernel': 'k_relax (red-black GS colour pass, all levels)',
+                         'frac': achieved / peak, 'traffic': load_traffic(), 'peak_kind': peak_kind,
+                         'kernel': f'k_relax, finest level ({fl.levels[H.nlev - 1, 5] - fl.levels[H.nlev - 1, 4]} '
+                                   f'cells, one colour pass)',
                          'bytes_per_launch': rl['bytes'] / max(rl['launches'], 1),
-                         'avg_launch_us': 1e3 * rl['ms'] / max(rl['launches'], 1)},
+                         'avg_launch_us': 1e3 * rl['ms'] / max(rl['launches'], 1),
+                         'all_levels': {'achieved': achieved_all, 'frac': achieved_all / peak,
+                                        'avg_launch_us': 1e3 * ra['ms'] / max(ra['launches'], 1)}},
             'cpu_baseline': cpu,
             'gpu_launches': int(launches),
             'clocks': clk.summary(),

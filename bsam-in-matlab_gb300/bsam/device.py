@@ -79,7 +79,7 @@ def lib():
         L.bsam_composite_mean.argtypes = [P, C.POINTER(D), C.POINTER(D)]
         L.bsam_mass_check.argtypes = [P, P]
         L.bsam_stream.argtypes = [P, C.POINTER(P)]
-        L.bsam_profile_vcycles.argtypes = [P, C.c_int, P, P, P]
+        L.bsam_profile_vcycles.argtypes = [P, C.c_int, C.c_int, P, P, P]
         L.bsam_kernels_per_vcycle.argtypes = [P, C.POINTER(I64)]
         L.bsam_save_state.argtypes = [P]
         L.bsam_restore_state.argtypes = [P]
@@ -210,11 +210,11 @@ class DevHier:
         check(lib().bsam_stream(self.h, C.byref(s)))
         return s.value
 
-    def profile(self, ncycles):
+    def profile(self, ncycles, level=0):
         ms = np.zeros(NKINDS)
         nl = np.zeros(NKINDS, dtype=np.int64)
         by = np.zeros(NKINDS)
-        check(lib().bsam_profile_vcycles(self.h, int(ncycles), _ptr(ms), _ptr(nl), _ptr(by)))
+        check(lib().bsam_profile_vcycles(self.h, int(ncycles), int(level), _ptr(ms), _ptr(nl), _ptr(by)))
         return {KIND_NAMES[i]: {'ms': ms[i], 'launches': int(nl[i]), 'bytes': by[i]} for i in range(NKINDS)}
 
     def save_state(self):

@@ -147,6 +147,7 @@ struct bsam_hier_s {
   int64_t kernels_per_cycle = 0;
   // profiling
   bool profiling = false;
+  int profile_level = 0;           // 0: every level
   struct Rec { int kind; cudaEvent_t a, b; double bytes; };
   std::vector<Rec> recs;
   int64_t launch_count = 0;
@@ -212,16 +213,18 @@ struct Launch {
   int kind;
   double bytes;
   cudaEvent_t a = nullptr, b = nullptr;
-  Launch(bsam_hier h_, int kind_, double bytes_) : h(h_), kind(kind_), bytes(bytes_) {
+  bool rec = false;
+  Launch(bsam_hier h_, int kind_, double bytes_, int level = 0) : h(h_), kind(kind_), bytes(bytes_) {
     h->launch_count++;
-    if (h->profiling) {
+    rec = h->profiling && (h->profile_level == 0 || h->profile_level == level);
+    if (rec) {
       cudaEventCreate(&a);
       cudaEventCreate(&b);
       cudaEventRecord(a, h->stream);
     }
   }
   ~Launch() {
-    if (h->profiling) {
+    if (rec) {
       cudaEventRecord(b, h->stream);
       h->recs.push_back({kind, a, b, bytes});
     }
@@ -238,7 +241,7 @@ GhostItems ghost_items(bsam_hier h) {
 void launch_fill(bsam_hier h, int k) {
   const LevelPlan &L = h->lev[k];
   if (!L.g1_n) return;
-  Launch l(h, K_GHOST, 0);
+  Launch l(h, K_GHOST, 0, k);
   launch_k(h, k_ghost, nblk(L.g1_n), kBlock, ghost_items(h), L.g1_off, L.g1_n, h->Q.p, h->QC.p,
            (const double *)h->bcg.p, L.hx, L.hy);
 }
@@ -257,7 +260,7 @@ void launch_relax(bsam_hier h, int k, int nsweeps) {
   for (int s = 0; s < nsweeps; ++s)
     for (int m = 0; m < 2; ++m) {
       const int fresh = (s > 0 || m > 0) ? 1 : 0;
-      Launch l(h, K_RELAX, 24.0 * (double)L.ncells);
+      Launch l(h, K_RELAX, 24.0 * (double)L.ncells, k);
       if (L.pow2)
         launch_k(h, k_relax<true>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m, h->opts.omega, unit,
                  fresh);
@@ -271,7 +274,7 @@ void launch_relax(bsam_hier h, int k, int nsweeps) {
 void launch_restrict(bsam_hier h, int k, int to_parent) {
   const LevelPlan &L = h->lev[k];
   Decomp D = decomp(h, L.coarse);
-  Launch l(h, K_RESTRICT, 12.0 * (double)L.ncells);
+  Launch l(h, K_RESTRICT, 12.0 * (double)L.ncells, k);
   launch_k(h, k_restrict, D.nblocks, kBlock, leveld(h, k), D, fields(h), to_parent);
 }
 
@@ -285,7 +288,7 @@ void launch_coarse_load(bsam_hier h, int k) {
   Decomp D = decomp(h, L.coarse);
   const int ntgt = h->opts.mass_correction ? L.ct_n : 0;
   const int grid = nblk(L.ring_n) + D.nblocks + nblk(ntgt);
-  Launch l(h, K_LOAD, 50.0 * (double)L.ncells);
+  Launch l(h, K_LOAD, 50.0 * (double)L.ncells, k);
   launch_k(h, k_load, grid, kBlock, leveld(h, k), leveld(h, k - 1), D, fields(h), (const int *)h->ring.p, L.ring_off,
            L.ring_n, corr_csr(h, L), ntgt);
 }
@@ -293,13 +296,13 @@ void launch_coarse_load(bsam_hier h, int k) {
 void launch_prolong(bsam_hier h, int k, int correct) {
   const LevelPlan &L = h->lev[k];
   Decomp D = decomp(h, L.coarse);
-  Launch l(h, K_PROLONG, 20.0 * (double)L.ncells);
+  Launch l(h, K_PROLONG, 20.0 * (double)L.ncells, k);
   launch_k(h, k_prolong, D.nblocks, kBlock, leveld(h, k), D, fields(h), correct);
 }
 
 void launch_coarsest(bsam_hier h) {
   {
-    Launch l(h, K_COARSEST, 8.0 * (double)h->ncoarse * h->ncoarse);
+    Launch l(h, K_COARSEST, 8.0 * (double)h->ncoarse * h->ncoarse, 1);
     launch_k(h, k_coarsest, nblk(h->ncoarse * 32), kBlock, (const double *)h->Ainv.p, (const double *)h->bcRhs.p,
              fields(h), h->coarse_c_off, h->coarse_q_off, h->n1, h->ncoarse);
   }
@@ -1226,13 +1229,15 @@ int bsam_kernels_per_vcycle(bsam_hier h, int64_t *count) {
   return BSAM_OK;
 }
 
-int bsam_profile_vcycles(bsam_hier h, int ncycles, double ms[BSAM_NKINDS], int64_t launches[BSAM_NKINDS],
+int bsam_profile_vcycles(bsam_hier h, int ncycles, int level, double ms[BSAM_NKINDS], int64_t launches[BSAM_NKINDS],
                          double bytes[BSAM_NKINDS]) {
-  if (!h || !ms || !launches || !bytes || ncycles < 1) return fail(BSAM_ERR_ARG, "bad argument");
+  if (!h || !ms || !launches || !bytes || ncycles < 1 || level < 0 || level > h->nlev)
+    return fail(BSAM_ERR_ARG, "bad argument");
   int rc = set_device(h);
   if (rc) return rc;
   for (int i = 0; i < BSAM_NKINDS; ++i) { ms[i] = 0; launches[i] = 0; bytes[i] = 0; }
   h->profiling = true;
+  h->profile_level = level;
   h->recs.clear();
   for (int c = 0; c < ncycles && !rc; ++c) rc = launch_iteration(h);
   h->profiling = false;

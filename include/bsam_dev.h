@@ -137,13 +137,15 @@ int bsam_mass_check(bsam_hier h, double out[4]);
 /* Measurement support (no reference counterpart): the CUDA stream the
  * hierarchy's kernels run on (a cudaStream_t), and per-kernel device times
  * of `ncycles` eagerly launched V-cycles, each kernel bracketed by CUDA
- * events on that stream.  kinds: 0 relax, 1 ghost fill, 2 restrict, 3 ring,
- * 4 coarse load, 5 flux corrections, 6 prolong-correct, 7 coarsest,
- * 8 residual; ms[k] = total ms, launches[k], bytes[k] = algorithmic bytes. */
+ * events on that stream, restricted to the kernels of one level (level 0:
+ * all; the residual counts as level 0 only).  kinds: 0 relax, 1 ghost fill,
+ * 2 restrict, 3 ring, 4 coarse load, 5 flux corrections, 6 prolong-correct,
+ * 7 coarsest, 8 residual; ms[k] = total ms, launches[k], bytes[k] =
+ * algorithmic bytes. */
 int bsam_stream(bsam_hier h, void **stream);
 #define BSAM_NKINDS 9
-int bsam_profile_vcycles(bsam_hier h, int ncycles, double ms[BSAM_NKINDS], int64_t launches[BSAM_NKINDS],
-                         double bytes[BSAM_NKINDS]);
+int bsam_profile_vcycles(bsam_hier h, int ncycles, int level, double ms[BSAM_NKINDS],
+                         int64_t launches[BSAM_NKINDS], double bytes[BSAM_NKINDS]);
 
 /* Device-side snapshot of the solution state (Q, QC, F) and its restore,
  * so repeated solves of one resident hierarchy start from the same state
