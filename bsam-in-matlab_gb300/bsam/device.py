@@ -18,7 +18,7 @@ import os
 import numpy as np
 
 from .build import build_dev
-from .flat import flatten, scatter_field, FIELD_Q, FIELD_F, FIELD_QC
+from .flat import flatten, scatter_field, gather_field, FIELD_Q, FIELD_F, FIELD_QC
 
 P, I32, I64, D = C.c_void_p, C.c_int32, C.c_int64, C.c_double
 
@@ -75,6 +75,7 @@ def lib():
         L.bsam_prolong_level.argtypes = [P, C.c_int]
         L.bsam_solve_cycles.argtypes = [P, P, C.c_int, C.POINTER(C.c_int), C.POINTER(D), C.POINTER(I64)]
         L.bsam_vcycle.argtypes = [P]
+        L.bsam_filldown.argtypes = [P]
         L.bsam_comp_residual.argtypes = [P, P]
         L.bsam_composite_mean.argtypes = [P, C.POINTER(D), C.POINTER(D)]
         L.bsam_mass_check.argtypes = [P, P]
@@ -190,6 +191,9 @@ class DevHier:
     def vcycle(self):
         check(lib().bsam_vcycle(self.h))
 
+    def filldown(self):
+        check(lib().bsam_filldown(self.h))
+
     def residual(self):
         out = np.zeros(5)
         check(lib().bsam_comp_residual(self.h, _ptr(out)))
@@ -250,14 +254,22 @@ class DeviceBackend:
         self.ctx = Context(device)
 
     def ensure(self, H):
+        """The resident copy of H: re-uploaded after a structural change,
+        otherwise refreshed with the fields the host has modified."""
         cur = getattr(H, '_dev', None)
         if cur is not None and cur[0] == H.version and cur[1].ctx is self.ctx:
             dh = cur[1]
             dh.set_opts(H.opts)
+            for name in sorted(H.dirty):
+                which = {'Q': BSAM_FIELD_Q, 'F': BSAM_FIELD_F, 'FTrue': BSAM_FIELD_FTRUE,
+                         'QC': BSAM_FIELD_QC}[name]
+                dh.set(which, gather_field(H, dh.fl, which))
+            H.dirty.clear()
             return dh
         fl = flatten(H)
         dh = DevHier(self.ctx, fl, H.opts)
         H._dev = (H.version, dh)
+        H.dirty.clear()
         return dh
 
     def _writeback(self, H, dh):
@@ -273,6 +285,8 @@ class DeviceBackend:
                 dh.fill(op[1])
             elif op[0] == 'prolong':
                 dh.prolong(op[1])
+            elif op[0] == 'filldown':
+                dh.filldown()
             else:
                 raise ValueError(op)
         self._writeback(H, dh)

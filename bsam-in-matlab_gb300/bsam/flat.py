@@ -290,3 +290,25 @@ def scatter_field(H, fl, which, arr):
         elif which == FIELD_FTRUE:
             o = int(r[PD_COFF])
             lev.FTrue[p] = arr[o:o + mx * my].reshape((mx, my), order='F').copy(order='F')
+
+
+def gather_field(H, fl, which):
+    """Flat copy of one field of H in the layout of ``fl`` (the inverse of
+    scatter_field); used to refresh a resident hierarchy after host edits."""
+    sizes = {FIELD_Q: fl.Q.size, FIELD_QC: fl.QC.size, FIELD_F: fl.F.size, FIELD_FTRUE: fl.F.size}
+    out = np.zeros(sizes[which])
+    for (k, p), g in fl.pglob.items():
+        r = fl.patches[g]
+        lev = H.lev[k]
+        if which == FIELD_Q:
+            a, o = lev.Q[p], int(r[PD_QOFF])
+        elif which == FIELD_QC:
+            if k == 1:
+                continue
+            a, o = lev.QC[p], int(r[PD_QCOFF])
+        elif which == FIELD_F:
+            a, o = lev.F[p], int(r[PD_COFF])
+        else:
+            a, o = lev.FTrue[p], int(r[PD_COFF])
+        out[o:o + a.size] = np.asarray(a).ravel(order='F')
+    return out

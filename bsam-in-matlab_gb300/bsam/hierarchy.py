@@ -67,9 +67,14 @@ class Hierarchy:
         self.compatibility = None
         self.version = 0        # bumped on every structural change
         self._dev = None        # resident device copy (bsam.device)
+        self.dirty = set()      # fields edited on the host since the last sync
 
     def touch(self):
         self.version += 1
+
+    def mark_dirty(self, *fields):
+        """Record host edits of Q / F / FTrue / QC for the resident copy."""
+        self.dirty.update(fields)
 
 
 # ---------------------------------------------------------------------------

@@ -1040,6 +1040,16 @@ int bsam_prolong_level(bsam_hier h, int level) {
   return BSAM_OK;
 }
 
+int bsam_filldown(bsam_hier h) {
+  if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
+  int rc = set_device(h);
+  if (rc) return rc;
+  launch_filldown(h);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
 int bsam_comp_residual(bsam_hier h, double out[5]) {
   if (!h || !out) return fail(BSAM_ERR_ARG, "null argument");
   int rc = set_device(h);

@@ -125,6 +125,10 @@ int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles,
  * ebTransfer.m:73-79), force reset included (ebSolveCycles.m:30-34). */
 int bsam_vcycle(bsam_hier h);
 
+/* ebTransfer(H,0,'filldown') alone (ebTransfer.m:73-79): restrict every
+ * level into its parent and refill the parent's ghosts, finest first. */
+int bsam_filldown(bsam_hier h);
+
 /* ebCompResidual (ebCompResidual.m:15-85): out = {linf, l2, fnorm, rel, ncell}. */
 int bsam_comp_residual(bsam_hier h, double out[5]);
 

@@ -139,6 +139,7 @@ class OracleBackend:
         return fl, OracleHier(fl, H.opts)
 
     def _writeback(self, H, fl, oh):
+        H.dirty.clear()
         from bsam.flat import scatter_field, FIELD_Q, FIELD_QC, FIELD_F, FIELD_FTRUE
         scatter_field(H, fl, FIELD_Q, oh.Q)
         scatter_field(H, fl, FIELD_QC, oh.QC)
@@ -151,6 +152,8 @@ class OracleBackend:
                 oh.op('fill_ghosts', op[1])
             elif op[0] == 'prolong':
                 oh.op('correct', op[1], 0)
+            elif op[0] == 'filldown':
+                oh.op('filldown')
             else:
                 raise ValueError(op)
         self._writeback(H, fl, oh)

@@ -1,0 +1,62 @@
+"""Parabolic driver (config 3): BDF2 heat diffusion with regrids.
+
+Pinned to the reference's README heat example (verification/readme-
+examples.txt:23-27: V, rel, levels, cells, mass at steps 10..50) on the
+oracle; on the GPU the whole pipeline (set-up fills, regrid transfers, every
+step's solve) must match the oracle pipeline bit for bit.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from bsam.parabolic import ebpProblem, ebpSolve
+from bsam_oracle import OracleBackend
+from cases import printed_close
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), 'golden', 'reference_outputs.json')))
+
+
+def heat_problem():
+    u0 = lambda x, y: 1 + 0.2 * np.cos(2 * np.pi * x) * np.cos(2 * np.pi * y)
+    return ebpProblem([0, 1, 0, 1], 1, 0, 0, ('neumann', 0), u0)
+
+
+def _step_lines(sol):
+    out = {}
+    for n in (10, 20, 30, 40, 50):
+        out[n] = (int(sol['cycles'][n - 1]), float(sol['relres'][n - 1]), float(sol['mass'][n]))
+    return out
+
+
+def test_heat_readme_example_golden():
+    sol = ebpSolve(heat_problem(), 'Scheme', 'bdf2', 'Dt', 0.002, 'TFinal', 0.1, 'BaseCells', 32,
+                   'MaxLevels', 3, 'RegridEvery', 5, 'StepVerbose', 0, backend=OracleBackend())
+    gold = {g['step']: g for g in GOLD['readme_heat_steps']}
+    lines = _step_lines(sol)
+    for n, g in gold.items():
+        V, rel, mass = lines[n]
+        assert V == g['V'], (n, V, g)
+        assert printed_close(rel, g['rel']), (n, rel, g)
+        assert printed_close(mass, g['mass']), (n, mass, g)
+    # conservative scheme: total composite mass drift below the reference's
+    # regression bound (ParabolicBSAM/tests/runParabolicRegressions.m: 2e-10)
+    assert np.max(np.abs(sol['mass'] - sol['mass'][0])) < 2e-10
+    assert sol['nregrids'] == 9
+
+
+@pytest.mark.gpu
+def test_heat_device_matches_oracle_pipeline():
+    from bsam.device import DeviceBackend
+    kw = dict(Scheme='bdf2', Dt=0.002, TFinal=0.024, BaseCells=32, MaxLevels=3, RegridEvery=5, StepVerbose=0)
+    a = ebpSolve(heat_problem(), *sum(kw.items(), ()), backend=OracleBackend())
+    b = ebpSolve(heat_problem(), *sum(kw.items(), ()), backend=DeviceBackend.get(0))
+    np.testing.assert_array_equal(a['cycles'], b['cycles'])
+    np.testing.assert_array_equal(a['relres'], b['relres'])
+    Ha, Hb = a['H'], b['H']
+    assert Ha.nlev == Hb.nlev
+    for k in range(1, Ha.nlev + 1):
+        for qa, qb in zip(Ha.lev[k].Q, Hb.lev[k].Q):
+            np.testing.assert_array_equal(qa[1:-1, 1:-1], qb[1:-1, 1:-1])
+    np.testing.assert_allclose(a['mass'], b['mass'], rtol=1e-14, atol=0)
