@@ -47,7 +47,8 @@ class HierDesc(C.Structure):
                 ('n_q', I64), ('n_cells', I64), ('n_dew', I64), ('n_dns', I64), ('n_qc', I64), ('n_bcg', I64),
                 ('n_cfd', I64), ('n_pcoef', I64), ('n_same', I64), ('n_ring', I64), ('n_win', I64), ('n_fp', I64),
                 ('n_corr', I64),
-                ('ncoarse', I32), ('singular', I32)]
+                ('ncoarse', I32), ('singular', I32),
+                ('ninst', I32), ('patch_inst', P), ('inst_root', P)]
 
 
 class SolveOpts(C.Structure):
@@ -85,6 +86,8 @@ def lib():
         L.bsam_save_state.argtypes = [P]
         L.bsam_restore_state.argtypes = [P]
         L.bsam_launch_count.argtypes = [P, C.POINTER(I64)]
+        L.bsam_batch_result.argtypes = [P, C.c_int, P, C.c_int, C.POINTER(C.c_int), C.POINTER(D), C.POINTER(I64)]
+        L.bsam_batch_set_stop.argtypes = [P, C.c_int, C.c_int, D]
         _lib = L
     return _lib
 
@@ -125,6 +128,10 @@ def make_desc(fl, keep):
     d.n_same, d.n_ring, d.n_win = fl.same.shape[0], fl.ring.shape[0], fl.win.size
     d.n_fp, d.n_corr = fl.fp.shape[0], fl.corr.size
     d.ncoarse, d.singular = int(fl.bcRhs.size), int(fl.singular)
+    ninst = int(getattr(fl, 'ninst', 1))
+    d.ninst = ninst
+    if ninst > 1:
+        d.patch_inst, d.inst_root = arr(fl.patch_inst, np.int32), arr(fl.inst_root, np.int32)
     return d
 
 
@@ -187,6 +194,20 @@ class DevHier:
         vis = I64(0)
         check(lib().bsam_solve_cycles(self.h, _ptr(hist), hist.size, C.byref(it), C.byref(rel), C.byref(vis)))
         return it.value, hist[:it.value + 1].copy(), rel.value, vis.value
+
+    def batch_result(self, inst, hist_cap):
+        """(vcycles, resHist, finalRel, visibleCells) of one instance of a
+        batch after solve_cycles."""
+        hist = np.zeros(max(hist_cap, 1))
+        it = C.c_int(0)
+        rel = D(0)
+        vis = I64(0)
+        check(lib().bsam_batch_result(self.h, int(inst), _ptr(hist), hist.size, C.byref(it), C.byref(rel),
+                                      C.byref(vis)))
+        return it.value, hist[:it.value + 1].copy(), rel.value, vis.value
+
+    def set_stop(self, inst, max_vcycles, rel_tol):
+        check(lib().bsam_batch_set_stop(self.h, int(inst), int(max_vcycles), float(rel_tol)))
 
     def vcycle(self):
         check(lib().bsam_vcycle(self.h))

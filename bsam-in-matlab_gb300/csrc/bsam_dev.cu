@@ -98,8 +98,6 @@ struct LevelPlan {
   int ring_off = 0, ring_n = 0;
   // corrections contributed by this (fine) level, targets in level k-1
   int ct_off = 0, ct_n = 0;
-  // residual slots of this level (k >= root): main blocks then target blocks
-  int res_slot = 0, res_main_blocks = 0, res_tgt_blocks = 0;
   int64_t ncells = 0;
 };
 
@@ -123,24 +121,36 @@ struct bsam_hier_s {
   std::vector<double> hs;
   std::vector<LevelPlan> lev;     // index 1..nlev
   int64_t n_q = 0, n_cells = 0, n_qc = 0;
-  int64_t ncell_visible = 0;
-  int ncoarse = 0, n1 = 0, coarse_c_off = 0, coarse_q_off = 0;
+  int ninst = 1;                   // instances (a single hierarchy is one instance)
+  std::vector<int> inst_root;
+  std::vector<int64_t> inst_visible;
+  int64_t ncoarse_total = 0;
+  int ncoarse_patches = 0, coarse_max_rows = 0;
   // device arrays
-  DBuf<double> Q, F, FTrue, QC, CC, ID, DeW, DnS, bcg, cfd, pcoef, Ainv, bcRhs, slots, area, partials;
+  DBuf<double> Q, F, FTrue, QC, CC, ID, DeW, DnS, bcg, cfd, pcoef, Ainv, bcRhs, slots, partials, hist;
   DBuf<uint8_t> flags;
-  DBuf<int> win, fp, ring, ints, ct_cell, ct_patch, ct_beg, ct_item, ct_j, level_slot0;
+  DBuf<int> win, fp, ring, ints, ct_cell, ct_patch, ct_beg, ct_item, ct_j, active, iters, ones;
+  DBuf<int> g_inst, ring_inst;     // instance per ghost item / ring entry (batches only)
+  DecompH all_cells;               // every cell of every level (batch force reset)
+  std::vector<InstRes> hir;        // host copy of the per-instance reduction plan
+  // results of the last solve, per instance
+  std::vector<double> res_hist;    // [ninst][hist_stride]
+  std::vector<int> res_iters;
+  std::vector<ResAcc> res_acc;
   DBuf<int8_t> g_type;
   DBuf<int> g_dst, g_a, g_b, g_c, g_d, g_e;
   DBuf<PatchD> patches;
   DBuf<ResAcc> acc;
   DBuf<Rule> perim;                // per-patch perimeter ghost rules (inline)
   DBuf<RelaxChunk> rchunks;        // relax chunk records, all levels
-  DBuf<unsigned char> blk_seg;     // residual block -> segment
-  DBuf<LevelX> levelx;             // per-level descriptors for multi-level kernels
-  DBuf<ResSeg> segs;               // residual launch segments
-  int nseg = 0, nres_blocks = 0;
-  ResAcc *acc_host = nullptr;  // pinned
-  int nslots = 0, nres_levels = 0, npartials = 0;
+  DBuf<LevelX> levelx;             // per-level descriptors for the residual
+  DBuf<ResTask> rtasks;            // residual warp tasks
+  DBuf<InstRes> instres;           // per-instance residual reduction plan
+  DBuf<SlotRange> sranges;
+  DBuf<CoarsestD> coarsest;        // one coarsest operator per instance
+  int nrtasks = 0, nslots = 0, npartials = 0, hist_stride = 0;
+  ResAcc *acc_host = nullptr;      // pinned, ninst entries
+  int *active_host = nullptr;      // pinned, ninst entries
   // graph of one V-cycle + fill-down + residual
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -162,7 +172,7 @@ Fields fields(bsam_hier h) {
   f.Q = h->Q.p; f.F = h->F.p; f.QC = h->QC.p;
   f.FTrue = h->FTrue.p; f.CC = h->CC.p; f.ID = h->ID.p; f.DeW = h->DeW.p; f.DnS = h->DnS.p;
   f.bcg = h->bcg.p; f.cfd = h->cfd.p; f.pcoef = h->pcoef.p; f.flags = h->flags.p;
-  f.win = h->win.p; f.fp = h->fp.p;
+  f.win = h->win.p; f.fp = h->fp.p; f.active = h->active.p;
   return f;
 }
 
@@ -235,7 +245,8 @@ enum { K_RELAX, K_GHOST, K_RESTRICT, K_RING, K_LOAD, K_CORR, K_PROLONG, K_COARSE
 
 // ---------------------------------------------------------------------------
 GhostItems ghost_items(bsam_hier h) {
-  return GhostItems{h->g_type.p, h->g_dst.p, h->g_a.p, h->g_b.p, h->g_c.p, h->g_d.p, h->g_e.p};
+  return GhostItems{h->g_type.p, h->g_dst.p, h->g_a.p, h->g_b.p, h->g_c.p, h->g_d.p, h->g_e.p,
+                    h->ninst > 1 ? h->g_inst.p : nullptr};
 }
 
 void launch_fill(bsam_hier h, int k) {
@@ -243,7 +254,7 @@ void launch_fill(bsam_hier h, int k) {
   if (!L.g1_n) return;
   Launch l(h, K_GHOST, 0, k);
   launch_k(h, k_ghost, nblk(L.g1_n), kBlock, ghost_items(h), L.g1_off, L.g1_n, h->Q.p, h->QC.p,
-           (const double *)h->bcg.p, L.hx, L.hy);
+           (const double *)h->bcg.p, L.hx, L.hy, (const int *)h->active.p);
 }
 
 // ebRelaxLevel (ebRelaxLevel.m:28-38): 2*nsweeps colour passes; the ghost
@@ -289,8 +300,8 @@ void launch_coarse_load(bsam_hier h, int k) {
   const int ntgt = h->opts.mass_correction ? L.ct_n : 0;
   const int grid = nblk(L.ring_n) + D.nblocks + nblk(ntgt);
   Launch l(h, K_LOAD, 50.0 * (double)L.ncells, k);
-  launch_k(h, k_load, grid, kBlock, leveld(h, k), leveld(h, k - 1), D, fields(h), (const int *)h->ring.p, L.ring_off,
-           L.ring_n, corr_csr(h, L), ntgt);
+  launch_k(h, k_load, grid, kBlock, leveld(h, k), leveld(h, k - 1), D, fields(h), (const int *)h->ring.p,
+           (const int *)(h->ninst > 1 ? h->ring_inst.p : nullptr), L.ring_off, L.ring_n, corr_csr(h, L), ntgt);
 }
 
 void launch_prolong(bsam_hier h, int k, int correct) {
@@ -302,9 +313,18 @@ void launch_prolong(bsam_hier h, int k, int correct) {
 
 void launch_coarsest(bsam_hier h) {
   {
-    Launch l(h, K_COARSEST, 8.0 * (double)h->ncoarse * h->ncoarse, 1);
-    launch_k(h, k_coarsest, nblk(h->ncoarse * 32), kBlock, (const double *)h->Ainv.p, (const double *)h->bcRhs.p,
-             fields(h), h->coarse_c_off, h->coarse_q_off, h->n1, h->ncoarse);
+    Launch l(h, K_COARSEST, 8.0 * (double)h->Ainv.n, 1);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)nblk(h->coarse_max_rows * 32), (unsigned)h->ncoarse_patches);
+    cfg.blockDim = dim3(kBlock);
+    cfg.stream = h->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_coarsest, (const double *)h->Ainv.p, (const double *)h->bcRhs.p,
+                       (const CoarsestD *)h->coarsest.p, fields(h));
   }
   launch_fill(h, 1);
 }
@@ -331,28 +351,36 @@ void launch_filldown(bsam_hier h) {
   }
 }
 
-// ebCompResidual (ebCompResidual.m:15-85): one launch over every level, then
-// the final reduction
-void launch_residual(bsam_hier h) {
+// ebCompResidual (ebCompResidual.m:15-85): one launch over every level of
+// every instance, then the per-instance reduction and stop test (mode 0:
+// before the first V-cycle, 1: after one)
+void launch_residual(bsam_hier h, int mode) {
   double bytes = 0;
-  for (int k = h->root; k <= h->nlev; ++k) bytes += 41.0 * (double)h->lev[k].ncells;
+  for (int k = 1; k <= h->nlev; ++k) bytes += 41.0 * (double)h->lev[k].ncells;
   {
     Launch l(h, K_RESID, bytes);
-    launch_k(h, k_residual, h->nres_blocks, kBlock, (const LevelX *)h->levelx.p, (const ResSeg *)h->segs.p,
-             (const unsigned char *)h->blk_seg.p, fields(h), (const int *)h->ring.p, h->slots.p, h->nslots,
-             h->opts.mass_correction);
+    launch_k(h, k_residual, (h->nrtasks + kBlock / 32 - 1) / (kBlock / 32), kBlock, (const LevelX *)h->levelx.p,
+             (const PatchD *)h->patches.p, (const ResTask *)h->rtasks.p, h->nrtasks, fields(h), (const int *)h->ring.p,
+             h->slots.p, h->nslots, h->opts.mass_correction);
   }
   Launch l(h, K_RESID, 0);
-  launch_k(h, k_residual_final, 1, kFinal, h->acc.p, (const double *)h->slots.p, h->nslots,
-           (const int *)h->level_slot0.p, (const double *)h->area.p, h->nres_levels, (double)h->ncell_visible);
+  launch_k(h, k_residual_final, h->ninst, kFinal, (const InstRes *)h->instres.p, (const SlotRange *)h->sranges.p,
+           (const double *)h->slots.p, h->nslots, h->acc.p, h->active.p, h->iters.p, h->hist.p, h->hist_stride, mode);
 }
 
 // one ebSolveCycles iteration body: F = FTrue, V-cycle, fill-down, residual
-int launch_iteration(bsam_hier h) {
-  CK(cudaMemcpyAsync(h->F.p, h->FTrue.p, sizeof(double) * h->n_cells, cudaMemcpyDeviceToDevice, h->stream));
+// (mode 1 inside ebSolveCycles, 2 for an eager V-cycle)
+int launch_iteration(bsam_hier h, int mode) {
+  if (h->ninst == 1) {
+    CK(cudaMemcpyAsync(h->F.p, h->FTrue.p, sizeof(double) * h->n_cells, cudaMemcpyDeviceToDevice, h->stream));
+  } else {
+    Decomp D = decomp(h, h->all_cells);
+    Launch l(h, K_LOAD, 16.0 * (double)h->n_cells);
+    launch_k(h, k_freset, D.nblocks, kBlock, D, (const PatchD *)h->patches.p, fields(h));
+  }
   launch_vcycle(h, h->nlev);
   launch_filldown(h);
-  launch_residual(h);
+  launch_residual(h, mode);
   CK(cudaGetLastError());
   return BSAM_OK;
 }
@@ -361,7 +389,7 @@ int build_graph(bsam_hier h) {
   if (h->gexec) return BSAM_OK;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   const int64_t before = h->launch_count;
-  int rc = launch_iteration(h);
+  int rc = launch_iteration(h, 1);
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   if (rc) return rc;
@@ -379,11 +407,49 @@ void drop_graph(bsam_hier h) {
   h->graph = nullptr;
 }
 
-int read_residual(bsam_hier h, double out[5]) {
-  CK(cudaMemcpyAsync(h->acc_host, h->acc.p, sizeof(ResAcc), cudaMemcpyDeviceToHost, h->stream));
+// per-instance residuals and active flags -> host (pinned); returns the
+// number of instances still iterating
+int read_state(bsam_hier h, int *nactive) {
+  CK(cudaMemcpyAsync(h->acc_host, h->acc.p, sizeof(ResAcc) * h->ninst, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(h->active_host, h->active.p, sizeof(int) * h->ninst, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  for (int i = 0; i < 5; ++i) out[i] = h->acc_host->out[i];
+  int n = 0;
+  for (int i = 0; i < h->ninst; ++i) n += h->active_host[i] != 0;
+  *nactive = n;
   return BSAM_OK;
+}
+
+int read_residual(bsam_hier h, double out[5]) {
+  int na;
+  int rc = read_state(h, &na);
+  if (rc) return rc;
+  for (int i = 0; i < 5; ++i) out[i] = h->acc_host[0].out[i];
+  return BSAM_OK;
+}
+
+// (re)size the per-instance history and upload the reduction plan after a
+// change of the stop tests
+int upload_stops(bsam_hier h) {
+  int rc;
+  int stride = 1;
+  for (const InstRes &r : h->hir) stride = std::max(stride, r.max_vcycles + 1);
+  if (stride != h->hist_stride || !h->hist.p) {
+    h->hist.release();
+    h->hist_stride = stride;
+    if ((rc = h->hist.alloc((size_t)h->ninst * stride))) return rc;
+  }
+  h->instres.release();
+  if ((rc = h->instres.upload(h->hir.data(), h->hir.size(), h->stream))) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
+int apply_opts(bsam_hier h) {
+  for (InstRes &r : h->hir) {
+    r.max_vcycles = h->opts.max_vcycles;
+    r.rel_tol = h->opts.rel_tol;
+  }
+  return upload_stops(h);
 }
 
 // ---------------------------------------------------------------------------
@@ -393,10 +459,11 @@ struct Builder {
   const bsam_hier_desc *d;
   std::vector<int> ints;
   std::vector<int8_t> gt;
-  std::vector<int> gdst, ga, gb, gc, gd, ge;
+  std::vector<int> gdst, ga, gb, gc, gd, ge, gi;
   std::vector<Rule> perim;         // per patch: W(my) E(my) S(mx) N(mx) inline rule (type -1: physical)
   std::vector<RelaxChunk> chunks;  // relax chunk records
   std::vector<int> pe_off;         // per patch offset into perim
+  std::vector<int> pinst;          // per patch instance
 
   const int32_t *P(int p) const { return d->patches + (size_t)p * PDN; }
 
@@ -430,9 +497,11 @@ struct Builder {
   // physical corners last
   int ghosts(int k, LevelPlan &L) {
     std::map<int, size_t> rule;   // dst -> index into tmp
-    struct G { int8_t t; int dst, a, b, c, dd, e; };
+    struct G { int8_t t; int dst, a, b, c, dd, e; int inst = 0; };
     std::vector<G> tmp, ringi, corners;
+    int cur = 0;                  // instance of the patch being planned
     auto put = [&](G g) {
+      g.inst = cur;
       auto it = rule.find(g.dst);
       if (it == rule.end()) {
         rule[g.dst] = tmp.size();
@@ -446,6 +515,7 @@ struct Builder {
       const int32_t *r = P(p);
       const int mx = r[PD_MX], my = r[PD_MY], cmx = mx / 2, cmy = my / 2;
       const int qo = r[PD_QOFF];
+      cur = pinst[p];
       auto Q = [&](int i, int j) { return qo + (i - 1) + (j - 1) * (mx + 2); };
       // 1. coarse-fine: ring refresh + ebInterpCf
       bool any = false;
@@ -457,7 +527,7 @@ struct Builder {
           const int loc = dst - r[PD_QCOFF];
           if (loc < 0 || loc >= (int)qcsrc.size()) return fail(BSAM_ERR_ARG, "ring destination outside QC");
           qcsrc[loc] = src;
-          ringi.push_back({G_RING, dst, src, 0, 0, 0, 0});
+          ringi.push_back({G_RING, dst, src, 0, 0, 0, 0, cur});
         }
         bool bad = false;
         auto QC = [&](int i, int j) {
@@ -537,10 +607,10 @@ struct Builder {
       // physical corners: (face ghost + face ghost) - interior; the face
       // ghosts are referenced by their destination here and resolved to
       // rule indices once the level's rules are final
-      if (r[PD_CCSW] == 1) corners.push_back({G_PHYS_CORNER, Q(1, 1), Q(2, 1), Q(1, 2), Q(2, 2), 0, 0});
-      if (r[PD_CCSE] == 1) corners.push_back({G_PHYS_CORNER, Q(mx + 2, 1), Q(mx + 1, 1), Q(mx + 2, 2), Q(mx + 1, 2), 0, 0});
-      if (r[PD_CCNW] == 1) corners.push_back({G_PHYS_CORNER, Q(1, my + 2), Q(2, my + 2), Q(1, my + 1), Q(2, my + 1), 0, 0});
-      if (r[PD_CCNE] == 1) corners.push_back({G_PHYS_CORNER, Q(mx + 2, my + 2), Q(mx + 1, my + 2), Q(mx + 2, my + 1), Q(mx + 1, my + 1), 0, 0});
+      if (r[PD_CCSW] == 1) corners.push_back({G_PHYS_CORNER, Q(1, 1), Q(2, 1), Q(1, 2), Q(2, 2), 0, 0, cur});
+      if (r[PD_CCSE] == 1) corners.push_back({G_PHYS_CORNER, Q(mx + 2, 1), Q(mx + 1, 1), Q(mx + 2, 2), Q(mx + 1, 2), 0, 0, cur});
+      if (r[PD_CCNW] == 1) corners.push_back({G_PHYS_CORNER, Q(1, my + 2), Q(2, my + 2), Q(1, my + 1), Q(2, my + 1), 0, 0, cur});
+      if (r[PD_CCNE] == 1) corners.push_back({G_PHYS_CORNER, Q(mx + 2, my + 2), Q(mx + 1, my + 2), Q(mx + 2, my + 1), Q(mx + 1, my + 1), 0, 0, cur});
     }
     L.g1_off = (int)gt.size();
     for (G &g : corners) {
@@ -553,7 +623,7 @@ struct Builder {
     auto emit = [&](const std::vector<G> &v) {
       for (const G &g : v) {
         gt.push_back(g.t); gdst.push_back(g.dst); ga.push_back(g.a); gb.push_back(g.b);
-        gc.push_back(g.c); gd.push_back(g.dd); ge.push_back(g.e);
+        gc.push_back(g.c); gd.push_back(g.dd); ge.push_back(g.e); gi.push_back(g.inst);
       }
     };
     emit(tmp);
@@ -593,7 +663,7 @@ struct Builder {
         RelaxChunk c{};
         c.q_off = r[PD_QOFF]; c.c_off = r[PD_COFF]; c.dew_off = r[PD_DEWOFF]; c.dns_off = r[PD_DNSOFF];
         c.bcg_off = r[PD_BCGOFF]; c.pe_off = pe_off[p]; c.mx = r[PD_MX]; c.my = r[PD_MY];
-        c.par0 = r[PD_PAR0]; c.s0 = s0; c.n = std::min(kChunk, ncol - s0); c.pad = 0;
+        c.par0 = r[PD_PAR0]; c.s0 = s0; c.n = std::min(kChunk, ncol - s0); c.inst = pinst[p];
         for (int sd = 0; sd < 4; ++sd) c.bc[sd] = r[PD_BCW + sd];
         chunks.push_back(c);
       }
@@ -636,7 +706,18 @@ int validate(const bsam_hier_desc *d) {
     if (!(d->hs[2 * (k - 1)] > 0) || !(d->hs[2 * (k - 1) + 1] > 0)) return fail(BSAM_ERR_ARG, "bad cell size");
   }
   if (expect_p != d->npatch) return fail(BSAM_ERR_ARG, "patch count mismatch");
-  if (d->levels[LD_P1] - d->levels[LD_P0] != 1) return fail(BSAM_ERR_ARG, "level 1 must be one patch");
+  const int ninst = d->ninst > 1 ? d->ninst : 1;
+  if (d->levels[LD_P1] - d->levels[LD_P0] != ninst)
+    return fail(BSAM_ERR_ARG, "level 1 must hold one patch per instance");
+  if (ninst > 1) {
+    if (!d->patch_inst || !d->inst_root) return fail(BSAM_ERR_ARG, "batch without instance tables");
+    for (int p = 0; p < d->npatch; ++p)
+      if (d->patch_inst[p] < 0 || d->patch_inst[p] >= ninst) return fail(BSAM_ERR_ARG, "patch instance out of range");
+    for (int i = 0; i < ninst; ++i) {
+      if (d->inst_root[i] < 1 || d->inst_root[i] > d->nlev) return fail(BSAM_ERR_ARG, "instance root out of range");
+      if (d->patch_inst[i] != i) return fail(BSAM_ERR_ARG, "level-1 patches must be in instance order");
+    }
+  }
   for (int p = 0; p < d->npatch; ++p) {
     const int32_t *r = d->patches + (size_t)p * PDN;
     const int64_t mx = r[PD_MX], my = r[PD_MY];
@@ -670,8 +751,13 @@ int validate(const bsam_hier_desc *d) {
       return fail(BSAM_ERR_ARG, "footprint table index out of range");
   for (int64_t t = 0; t < d->n_corr; ++t)
     if (d->corr[t] < -1 || d->corr[t] >= d->n_cells) return fail(BSAM_ERR_ARG, "correction target out of range");
-  const int32_t *r1 = d->patches;
-  if ((int64_t)r1[PD_MX] * r1[PD_MY] != d->ncoarse) return fail(BSAM_ERR_ARG, "coarsest size mismatch");
+  int64_t nc = 0;
+  for (int i = 0; i < ninst; ++i) {
+    const int32_t *r1 = d->patches + (size_t)i * PDN;
+    if ((int64_t)r1[PD_MX] * r1[PD_MY] > 16384) return fail(BSAM_ERR_ARG, "coarsest level too large");
+    nc += (int64_t)r1[PD_MX] * r1[PD_MY];
+  }
+  if (nc != d->ncoarse) return fail(BSAM_ERR_ARG, "coarsest size mismatch");
   return BSAM_OK;
 }
 
@@ -688,6 +774,18 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
   h->n_q = d->n_q;
   h->n_cells = d->n_cells;
   h->n_qc = d->n_qc;
+  h->ninst = d->ninst > 1 ? d->ninst : 1;
+  std::vector<int> pinst(d->npatch, 0);
+  h->inst_root.assign(h->ninst, d->root_idx);
+  if (h->ninst > 1) {
+    pinst.assign(d->patch_inst, d->patch_inst + d->npatch);
+    h->inst_root.assign(d->inst_root, d->inst_root + h->ninst);
+  }
+  int64_t asz = 0;
+  for (int i = 0; i < h->ninst; ++i) {
+    const int32_t *r1 = d->patches + (size_t)i * PDN;
+    asz += (int64_t)r1[PD_MX] * r1[PD_MY] * r1[PD_MX] * r1[PD_MY];
+  }
   if ((rc = h->Q.upload(d->Q, d->n_q, s)) || (rc = h->F.upload(d->F, d->n_cells, s)) ||
       (rc = h->FTrue.upload(d->FTrue, d->n_cells, s)) || (rc = h->CC.upload(d->CC, d->n_cells, s)) ||
       (rc = h->ID.upload(d->InvDiagS, d->n_cells, s)) || (rc = h->DeW.upload(d->DeW, d->n_dew, s)) ||
@@ -695,8 +793,7 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
       (rc = h->bcg.upload(d->bcg, d->n_bcg, s)) || (rc = h->cfd.upload(d->cfd, d->n_cfd, s)) ||
       (rc = h->pcoef.upload(d->pcoef, d->n_pcoef, s)) || (rc = h->win.upload(d->win, d->n_win, s)) ||
       (rc = h->fp.upload(d->fp, 2 * d->n_fp, s)) || (rc = h->ring.upload(d->ring, 2 * d->n_ring, s)) ||
-      (rc = h->Ainv.upload(d->Ainv, (size_t)d->ncoarse * d->ncoarse, s)) ||
-      (rc = h->bcRhs.upload(d->bcRhs, d->ncoarse, s)))
+      (rc = h->Ainv.upload(d->Ainv, (size_t)asz, s)) || (rc = h->bcRhs.upload(d->bcRhs, d->ncoarse, s)))
     return rc;
   // patches
   std::vector<PatchD> pd(d->npatch);
@@ -708,10 +805,15 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
     q.qc_off = r[PD_QCOFF]; q.bcg_off = r[PD_BCGOFF]; q.cfd_off = r[PD_CFDOFF]; q.pc_off = r[PD_PCOFF];
     q.win_off = r[PD_WIN0]; q.fp_off = r[PD_FP0]; q.corr_off = r[PD_CORR0]; q.pe_off = 0;
     for (int sd = 0; sd < 4; ++sd) q.bc[sd] = r[PD_BCW + sd];
+    q.inst = pinst[p];
+    const int root = h->inst_root[q.inst];
+    q.pflags = (q.level >= root ? 1 : 0) | (q.level >= std::max(2, root + 1) ? 2 : 0);
+    q.pad0 = q.pad1 = 0;
   }
   // plan
   Builder B{h, d};
   B.pe_off.assign(d->npatch, 0);
+  B.pinst = pinst;
   h->lev.assign(d->nlev + 1, LevelPlan());
   std::vector<uint8_t> flags(d->covered, d->covered + d->n_cells);
   std::vector<int> ct_cell, ct_patch, ct_beg, ct_item, ct_j;
@@ -787,56 +889,97 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
   if ((rc = h->perim.upload(B.perim.data(), B.perim.size(), s)) ||
       (rc = h->rchunks.upload(B.chunks.data(), B.chunks.size(), s)))
     return rc;
-  // covered cells of levels >= root are excluded from the norms
-  int64_t nvis = 0;
-  for (int k = d->root_idx; k <= d->nlev; ++k) {
-    const int32_t *lv = d->levels + (size_t)(k - 1) * LDN;
-    for (int c = lv[LD_CELL0]; c < lv[LD_CELL1]; ++c) nvis += (d->covered[c] == 0);
+  // residual plan: warp tasks, slots in instance order, level by level
+  // (main cells, then the level's correction targets), then the QC refresh
+  // tasks of the levels above each instance's root
+  std::vector<ResTask> tasks;
+  std::vector<SlotRange> ranges;
+  std::vector<InstRes> ir(h->ninst);
+  h->inst_visible.assign(h->ninst, 0);
+  int ns = 0;
+  for (int i = 0; i < h->ninst; ++i) {
+    ir[i].range0 = (int)ranges.size();
+    for (int k = h->inst_root[i]; k <= d->nlev; ++k) {
+      const LevelPlan &L = h->lev[k];
+      const int s0 = ns;
+      for (int p = L.p0; p < L.p1; ++p) {
+        if (pinst[p] != i) continue;
+        const int32_t *r = B.P(p);
+        const int n = r[PD_MX] * r[PD_MY];
+        for (int c = 0; c < n; ++c) h->inst_visible[i] += (d->covered[r[PD_COFF] + c] == 0);
+        for (int b0 = 0; b0 < n; b0 += 32) tasks.push_back(ResTask{0, k, p, b0, std::min(32, n - b0), ns++, 0, 0});
+      }
+      if (k < d->nlev) {
+        const LevelPlan &Lf = h->lev[k + 1];
+        // targets of this instance: a contiguous run (cells are ordered by patch)
+        int t0 = -1, t1 = -1;
+        for (int t = 0; t < Lf.ct_n; ++t)
+          if (pinst[L.p0 + ct_patch[Lf.ct_off + t]] == i) {
+            if (t0 < 0) t0 = t;
+            t1 = t + 1;
+          }
+        for (int t = t0; t0 >= 0 && t < t1; t += 32) tasks.push_back(ResTask{1, k, 0, t, std::min(32, t1 - t), ns++, 0, 0});
+      }
+      ranges.push_back(SlotRange{s0, ns, L.hx * L.hy});
+    }
+    ir[i].range1 = (int)ranges.size();
+    ir[i].max_vcycles = h->opts.max_vcycles;
+    ir[i].pad = 0;
+    ir[i].rel_tol = h->opts.rel_tol;
+    ir[i].ncell = (double)h->inst_visible[i];
   }
-  h->ncell_visible = nvis;
-  // residual launch: segments per level >= root (main cells, then targets,
-  // each with its own slots), then the QC refresh segments of the levels
-  // above the root
-  std::vector<int> slot0;
-  std::vector<double> area;
-  std::vector<ResSeg> segs;
-  int ns = 0, nbk = 0;
-  for (int k = d->root_idx; k <= d->nlev; ++k) {
-    LevelPlan &L = h->lev[k];
-    L.res_slot = ns;
-    L.res_main_blocks = L.cell.nblocks;
-    L.res_tgt_blocks = (k < d->nlev) ? nblk(h->lev[k + 1].ct_n) : 0;
-    slot0.push_back(ns);
-    area.push_back(L.hx * L.hy);
-    segs.push_back(ResSeg{0, k, nbk, ns});
-    nbk += L.res_main_blocks;
-    ns += L.res_main_blocks;
-    if (L.res_tgt_blocks) {
-      segs.push_back(ResSeg{1, k, nbk, ns});
-      nbk += L.res_tgt_blocks;
-      ns += L.res_tgt_blocks;
+  for (int k = 2; k <= d->nlev; ++k) {
+    const LevelPlan &L = h->lev[k];
+    for (int p = L.p0; p < L.p1; ++p) {
+      const int32_t *r = B.P(p);
+      const int root = h->inst_root[pinst[p]];
+      if (k < std::max(2, root + 1)) continue;
+      for (int t = r[PD_RING0]; t < r[PD_RING1]; t += 32)
+        tasks.push_back(ResTask{2, k, t, 0, std::min(32, r[PD_RING1] - t), 0, 0, 0});
+      const int nc = (r[PD_MX] / 2) * (r[PD_MY] / 2);
+      for (int b0 = 0; b0 < nc; b0 += 32) tasks.push_back(ResTask{3, k, p, b0, std::min(32, nc - b0), 0, 0, 0});
     }
   }
-  slot0.push_back(ns);
-  for (int k = std::max(2, d->root_idx + 1); k <= d->nlev; ++k) {
-    LevelPlan &L = h->lev[k];
-    if (L.ring_n) {
-      segs.push_back(ResSeg{2, k, nbk, 0});
-      nbk += nblk(L.ring_n);
+  h->nrtasks = (int)tasks.size();
+  h->nslots = std::max(ns, 1);
+  // the instance's targets must be one run per level
+  for (int k = 2; k <= d->nlev; ++k) {
+    const LevelPlan &L = h->lev[k];
+    for (int t = 1; t < L.ct_n; ++t)
+      if (pinst[h->lev[k - 1].p0 + ct_patch[L.ct_off + t]] < pinst[h->lev[k - 1].p0 + ct_patch[L.ct_off + t - 1]])
+        return fail(BSAM_ERR_ARG, "batch patches of a level must be grouped by instance");
+  }
+  // coarsest: one dense inverse block per instance
+  std::vector<CoarsestD> cds(h->ninst);
+  {
+    long long ao = 0, ro = 0;
+    h->coarse_max_rows = 0;
+    for (int i = 0; i < h->ninst; ++i) {
+      const int32_t *r1 = B.P(i);
+      CoarsestD &c = cds[i];
+      c.c_off = r1[PD_COFF];
+      c.q_off = r1[PD_QOFF];
+      c.n1 = r1[PD_MX];
+      c.N = r1[PD_MX] * r1[PD_MY];
+      c.inst = i;
+      c.pad = 0;
+      c.ainv_off = ao;
+      c.rhs_off = ro;
+      ao += (long long)c.N * c.N;
+      ro += c.N;
+      h->coarse_max_rows = std::max(h->coarse_max_rows, c.N);
     }
-    segs.push_back(ResSeg{3, k, nbk, 0});
-    nbk += L.coarse.nblocks;
+    h->ncoarse_patches = h->ninst;
+    h->ncoarse_total = ro;
   }
-  h->nslots = ns;
-  h->nres_levels = (int)area.size();
-  h->nseg = (int)segs.size();
-  h->nres_blocks = nbk;
-  if (segs.size() > 255) return fail(BSAM_ERR_ARG, "too many residual segments");
-  std::vector<unsigned char> blk_seg(std::max(nbk, 1), 0);
-  for (size_t i = 0; i < segs.size(); ++i) {
-    const int end = (i + 1 < segs.size()) ? segs[i + 1].block0 : nbk;
-    for (int b2 = segs[i].block0; b2 < end; ++b2) blk_seg[b2] = (unsigned char)i;
-  }
+  h->all_cells = B.make_decomp(0, d->npatch, 1);
+  std::vector<int> rinst(std::max<int64_t>(d->n_ring, 1), 0);
+  for (int p = 0; p < d->npatch; ++p)
+    for (int t = B.P(p)[PD_RING0]; t < B.P(p)[PD_RING1]; ++t) rinst[t] = pinst[p];
+  h->hir = ir;
+  h->hist_stride = h->opts.max_vcycles + 1;
+  if ((rc = h->g_inst.upload(B.gi.data(), B.gi.size(), s)) || (rc = h->ring_inst.upload(rinst.data(), rinst.size(), s)))
+    return rc;
   if ((rc = h->flags.upload(flags.data(), flags.size(), s)) || (rc = h->ints.upload(B.ints.data(), B.ints.size(), s)) ||
       (rc = h->g_type.upload(B.gt.data(), B.gt.size(), s)) || (rc = h->g_dst.upload(B.gdst.data(), B.gdst.size(), s)) ||
       (rc = h->g_a.upload(B.ga.data(), B.ga.size(), s)) || (rc = h->g_b.upload(B.gb.data(), B.gb.size(), s)) ||
@@ -845,57 +988,61 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
       (rc = h->ct_patch.upload(ct_patch.data(), ct_patch.size(), s)) ||
       (rc = h->ct_beg.upload(ct_beg.data(), ct_beg.size(), s)) ||
       (rc = h->ct_item.upload(ct_item.data(), ct_item.size(), s)) || (rc = h->ct_j.upload(ct_j.data(), ct_j.size(), s)) ||
-      (rc = h->level_slot0.upload(slot0.data(), slot0.size(), s)) || (rc = h->area.upload(area.data(), area.size(), s)) ||
-      (rc = h->slots.alloc(3 * (size_t)std::max(ns, 1))) || (rc = h->acc.alloc(1)) ||
-      (rc = h->blk_seg.upload(blk_seg.data(), blk_seg.size(), s)) ||
-      (rc = h->segs.upload(segs.data(), segs.size(), s)))
+      (rc = h->rtasks.upload(tasks.data(), tasks.size(), s)) || (rc = h->sranges.upload(ranges.data(), ranges.size(), s)) ||
+      (rc = h->instres.upload(ir.data(), ir.size(), s)) || (rc = h->coarsest.upload(cds.data(), cds.size(), s)) ||
+      (rc = h->slots.alloc(3 * (size_t)h->nslots)) || (rc = h->acc.alloc(h->ninst)) ||
+      (rc = h->iters.alloc(h->ninst)) ||
+      (rc = h->hist.alloc((size_t)h->ninst * h->hist_stride)))
     return rc;
-  // per-level descriptors for the multi-level residual kernel
+  // per-level descriptors for the residual kernel
   {
-    std::vector<LevelX> X(d->nlev + 1);
+    std::vector<LevelX> X(d->nlev + 2);
+    std::memset(X.data(), 0, sizeof(LevelX) * X.size());
     for (int k = 1; k <= d->nlev; ++k) {
       LevelPlan &L = h->lev[k];
       X[k].L = leveld(h, k);
-      X[k].cell = decomp(h, L.cell);
-      X[k].coarse = decomp(h, L.coarse);
       X[k].C = corr_csr(h, L);
       X[k].ct_n = L.ct_n;
-      X[k].ring_off = L.ring_off;
-      X[k].ring_n = L.ring_n;
       X[k].pad = 0;
     }
     if ((rc = h->levelx.upload(X.data(), X.size(), s))) return rc;
   }
-  CK(cudaMemsetAsync(h->acc.p, 0, sizeof(ResAcc), s));
-  // coarsest
-  const int32_t *r1 = d->patches;
-  h->ncoarse = d->ncoarse;
-  h->n1 = r1[PD_MX];
-  h->coarse_c_off = r1[PD_COFF];
-  h->coarse_q_off = r1[PD_QOFF];
+  CK(cudaMemsetAsync(h->acc.p, 0, sizeof(ResAcc) * h->ninst, s));
+  CK(cudaMemsetAsync(h->iters.p, 0, sizeof(int) * h->ninst, s));
+  CK(cudaMemsetAsync(h->hist.p, 0, sizeof(double) * h->hist.n, s));
+  {
+    // every instance starts active: eager operations (ghost fills, prolong,
+    // fill-down) apply to all of them
+    std::vector<int> one(h->ninst, 1);
+    if ((rc = h->active.upload(one.data(), one.size(), s)) || (rc = h->ones.upload(one.data(), one.size(), s))) return rc;
+  }
   // partial sums for composite sums
   int np = 0;
-  for (int k = d->root_idx; k <= d->nlev; ++k) np += h->lev[k].cell.nblocks;
+  for (int k = 1; k <= d->nlev; ++k) np += h->lev[k].cell.nblocks;
   h->npartials = np;
   if ((rc = h->partials.alloc((size_t)4 * std::max(np, 1)))) return rc;
-  if (!h->acc_host) CK(cudaMallocHost(&h->acc_host, sizeof(ResAcc)));
+  CK(cudaMallocHost(&h->acc_host, sizeof(ResAcc) * h->ninst));
+  CK(cudaMallocHost(&h->active_host, sizeof(int) * h->ninst));
   CK(cudaStreamSynchronize(s));
   return BSAM_OK;
 }
 
 void release(bsam_hier h) {
   drop_graph(h);
-  h->Q.release(); h->F.release(); h->FTrue.release(); h->QC.release(); h->CC.release(); h->ID.release();
-  h->DeW.release(); h->DnS.release(); h->bcg.release(); h->cfd.release(); h->pcoef.release(); h->Ainv.release();
-  h->bcRhs.release(); h->slots.release(); h->area.release(); h->partials.release(); h->flags.release();
-  h->win.release(); h->fp.release(); h->ring.release(); h->ints.release(); h->ct_cell.release();
-  h->ct_patch.release(); h->ct_beg.release(); h->ct_item.release(); h->ct_j.release(); h->level_slot0.release();
-  h->g_type.release(); h->g_dst.release(); h->g_a.release(); h->g_b.release(); h->g_c.release(); h->g_d.release();
-  h->g_e.release(); h->patches.release(); h->acc.release(); h->perim.release(); h->levelx.release();
-  h->segs.release(); h->rchunks.release(); h->blk_seg.release();
-  h->saveQ.release(); h->saveQC.release(); h->saveF.release();
+  for (DBuf<double> *b : {&h->Q, &h->F, &h->FTrue, &h->QC, &h->CC, &h->ID, &h->DeW, &h->DnS, &h->bcg, &h->cfd,
+                          &h->pcoef, &h->Ainv, &h->bcRhs, &h->slots, &h->partials, &h->hist, &h->saveQ, &h->saveQC,
+                          &h->saveF})
+    b->release();
+  for (DBuf<int> *b : {&h->win, &h->fp, &h->ring, &h->ints, &h->ct_cell, &h->ct_patch, &h->ct_beg, &h->ct_item,
+                       &h->ct_j, &h->active, &h->iters, &h->ones, &h->g_inst, &h->ring_inst, &h->g_dst, &h->g_a, &h->g_b, &h->g_c, &h->g_d, &h->g_e})
+    b->release();
+  h->flags.release(); h->g_type.release(); h->patches.release(); h->acc.release(); h->perim.release();
+  h->rchunks.release(); h->levelx.release(); h->rtasks.release(); h->instres.release(); h->sranges.release();
+  h->coarsest.release();
   if (h->acc_host) cudaFreeHost(h->acc_host);
+  if (h->active_host) cudaFreeHost(h->active_host);
   h->acc_host = nullptr;
+  h->active_host = nullptr;
 }
 
 int check_opts(const bsam_solve_opts *o) {
@@ -981,7 +1128,9 @@ int bsam_set_opts(bsam_hier h, const bsam_solve_opts *opts) {
   if (replan) return fail(BSAM_ERR_STATE, "GhostInterp is fixed at upload; upload the hierarchy again");
   h->opts = *opts;
   drop_graph(h);
-  return BSAM_OK;
+  rc = set_device(h);
+  if (rc) return rc;
+  return apply_opts(h);
 }
 
 static DBuf<double> *field_buf(bsam_hier h, int which) {
@@ -1054,7 +1203,7 @@ int bsam_comp_residual(bsam_hier h, double out[5]) {
   if (!h || !out) return fail(BSAM_ERR_ARG, "null argument");
   int rc = set_device(h);
   if (rc) return rc;
-  launch_residual(h);
+  launch_residual(h, 2);
   CK(cudaGetLastError());
   return read_residual(h, out);
 }
@@ -1062,7 +1211,7 @@ int bsam_comp_residual(bsam_hier h, double out[5]) {
 int bsam_vcycle(bsam_hier h) {
   if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
   int rc = set_device(h);
-  if (rc || (rc = launch_iteration(h))) return rc;
+  if (rc || (rc = launch_iteration(h, 2))) return rc;
   CK(cudaStreamSynchronize(h->stream));
   return BSAM_OK;
 }
@@ -1073,29 +1222,53 @@ int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles,
   int rc = set_device(h);
   if (rc) return rc;
   for (int k = 1; k <= h->nlev; ++k) launch_fill(h, k);
-  launch_residual(h);
+  launch_residual(h, 0);
   CK(cudaGetLastError());
-  double res[5];
-  if ((rc = read_residual(h, res))) return rc;
-  int nh = 0;
-  if (res_hist && nh < hist_cap) res_hist[nh] = res[0];
-  ++nh;
-  double rel = res[3];
-  int it = 0;
-  if ((rc = build_graph(h))) return rc;
-  while (it < h->opts.max_vcycles && rel > h->opts.rel_tol) {
-    ++it;
+  int nactive = 0;
+  if ((rc = read_state(h, &nactive))) return rc;
+  if (nactive && (rc = build_graph(h))) return rc;
+  // every instance iterates until its own stop test fails; a converged
+  // instance of a batch is frozen (its stores are predicated off) while the
+  // others continue
+  while (nactive) {
     CK(cudaGraphLaunch(h->gexec, h->stream));
     h->graph_launches++;
-    if ((rc = read_residual(h, res))) return rc;
-    if (res_hist && nh < hist_cap) res_hist[nh] = res[0];
-    ++nh;
-    rel = res[3];
+    if ((rc = read_state(h, &nactive))) return rc;
   }
+  h->res_hist.resize((size_t)h->ninst * h->hist_stride);
+  h->res_iters.resize(h->ninst);
+  h->res_acc.assign(h->acc_host, h->acc_host + h->ninst);
+  CK(cudaMemcpyAsync(h->res_hist.data(), h->hist.p, sizeof(double) * h->res_hist.size(), cudaMemcpyDeviceToHost,
+                     h->stream));
+  CK(cudaMemcpyAsync(h->res_iters.data(), h->iters.p, sizeof(int) * h->ninst, cudaMemcpyDeviceToHost, h->stream));
+  // eager operations after the solve act on every instance again
+  CK(cudaMemcpyAsync(h->active.p, h->ones.p, sizeof(int) * h->ninst, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return bsam_batch_result(h, 0, res_hist, hist_cap, vcycles, final_rel, visible_cells);
+}
+
+int bsam_batch_result(bsam_hier h, int inst, double *res_hist, int hist_cap, int *vcycles, double *final_rel,
+                      int64_t *visible_cells) {
+  if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
+  if (inst < 0 || inst >= h->ninst) return fail(BSAM_ERR_ARG, "instance out of range");
+  if (h->res_iters.empty()) return fail(BSAM_ERR_STATE, "no solve has run on this hierarchy");
+  const int it = h->res_iters[inst];
+  for (int i = 0; res_hist && i <= it && i < hist_cap; ++i) res_hist[i] = h->res_hist[(size_t)inst * h->hist_stride + i];
   if (vcycles) *vcycles = it;
-  if (final_rel) *final_rel = rel;
-  if (visible_cells) *visible_cells = (int64_t)res[4];
+  if (final_rel) *final_rel = h->res_acc[inst].out[3];
+  if (visible_cells) *visible_cells = (int64_t)h->res_acc[inst].out[4];
   return BSAM_OK;
+}
+
+int bsam_batch_set_stop(bsam_hier h, int inst, int max_vcycles, double rel_tol) {
+  if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
+  if (inst < 0 || inst >= h->ninst) return fail(BSAM_ERR_ARG, "instance out of range");
+  if (max_vcycles < 0 || !(rel_tol >= 0)) return fail(BSAM_ERR_ARG, "invalid stop test");
+  int rc = set_device(h);
+  if (rc) return rc;
+  h->hir[inst].max_vcycles = max_vcycles;
+  h->hir[inst].rel_tol = rel_tol;
+  return upload_stops(h);
 }
 
 int bsam_composite_mean(bsam_hier h, double *mean, double *area) {
@@ -1249,7 +1422,7 @@ int bsam_profile_vcycles(bsam_hier h, int ncycles, int level, double ms[BSAM_NKI
   h->profiling = true;
   h->profile_level = level;
   h->recs.clear();
-  for (int c = 0; c < ncycles && !rc; ++c) rc = launch_iteration(h);
+  for (int c = 0; c < ncycles && !rc; ++c) rc = launch_iteration(h, 2);
   h->profiling = false;
   cudaError_t e = cudaStreamSynchronize(h->stream);
   for (auto &r : h->recs) {

@@ -41,6 +41,10 @@ struct PatchD {
   int qc_off, bcg_off, cfd_off, pc_off;
   int win_off, fp_off, corr_off, pe_off;   // pe_off: perimeter ghost-rule table
   int bc[4];
+  int inst;                    // instance of a batch (0 for a single hierarchy)
+  int pflags;                  // bit0: level >= the instance's root (in the norms)
+                               // bit1: QC refreshed by the residual (level >= root+1)
+  int pad0, pad1;
 };
 
 struct Fields {
@@ -48,6 +52,7 @@ struct Fields {
   const double *FTrue, *CC, *ID, *DeW, *DnS, *bcg, *cfd, *pcoef;
   const uint8_t *flags;        // bit0 covered by a finer level, bit1 correction target
   const int *win, *fp;         // window gathers, footprint scatters (2 ints/cell)
+  const int *active;           // per instance: 1 while its V-cycles continue
 };
 
 // one level's work decomposition for one kind of item
@@ -97,6 +102,7 @@ enum GhostType : int8_t {
 struct GhostItems {
   const int8_t *type;
   const int *dst, *a, *b, *c, *d, *e;
+  const int *inst;             // instance per item (batches only, else null)
 };
 
 __device__ __forceinline__ double eval_rule(const GhostItems &G, int i, const double *Q, const double *bcg, double hx,
@@ -118,14 +124,16 @@ __device__ __forceinline__ double eval_rule(const GhostItems &G, int i, const do
 
 __global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, double *__restrict__ Q,
                                                   double *__restrict__ QC, const double *__restrict__ bcg,
-                                                  double hx, double hy) {
+                                                  double hx, double hy, const int *__restrict__ active) {
   chain_trigger();
   const int t = blockIdx.x * kBlock + threadIdx.x;
   const int i = off + t;
   const int8_t ty = (t < n) ? G.type[i] : (int8_t)-1;
   const int dst = (t < n) ? G.dst[i] : 0;
+  const int inst = (t < n && G.inst) ? G.inst[i] : -1;
   chain_wait();
   if (t >= n) return;
+  if (inst >= 0 && !active[inst]) return;   // a converged instance of a batch stays frozen
   if (ty == G_RING) {
     QC[dst] = Q[G.a[i]];
   } else if (ty == G_PHYS_CORNER) {
@@ -159,7 +167,7 @@ constexpr int kChunk = 64;
 struct RelaxChunk {
   int q_off, c_off, dew_off, dns_off;
   int bcg_off, pe_off, mx, my;
-  int par0, s0, n, pad;      // first colour-cell index in the patch, cells in the chunk
+  int par0, s0, n, inst;     // first colour-cell index in the patch, cells in the chunk, instance
   int bc[4];
 };
 
@@ -224,6 +232,7 @@ __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__
     else if (fresh) { ky = 3; ry = perim[R.pe_off + 2 * my + sy * mx + li]; }
   }
   chain_wait();
+  const int act = f.active[R.inst];   // a converged instance of a batch stays frozen
   double *__restrict__ Q = f.Q + R.q_off;
   double qe = Q[c + 1], qw = Q[c - 1], qn = Q[c + ldq], qs = Q[c - ldq];
   if (kx > 0) {
@@ -246,6 +255,7 @@ __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__
   t = t + divh<kPow2>(qn * dN, L.hy2, L.ihy2);
   t = t + divh<kPow2>(qs * dS, L.hy2, L.ihy2);
   t = t * idg;
+  if (!act) return;
   if (unit_omega) Q[c] = t;
   else Q[c] = omega * t + (1 - omega) * Q[c];
 }
@@ -272,7 +282,9 @@ __global__ void __launch_bounds__(kBlock) k_restrict(LevelD L, Decomp D, Fields 
   const int s = g - __ldg(D.beg + p);
   const int cj = s / cmx, ci = s - cj * cmx;
   const int dst = to_parent ? __ldg(f.fp + 2 * (P.fp_off + s)) : 0;
+  const int inst = P.inst;
   chain_wait();
+  if (!f.active[inst]) return;
   const double R = restrict_cell(f.Q + q_off, ldq, ci, cj);
   f.QC[qc_off + (ci + 1) + (cj + 1) * (cmx + 2)] = R;
   if (to_parent) f.Q[dst] = R;
@@ -368,19 +380,21 @@ __device__ __forceinline__ double op_pre(double q, double qe, double qw, double 
 }
 
 __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, Fields f, const int *__restrict__ ring,
-                                                 int ring_off, int n_ring, CorrCSR C, int n_tgt) {
+                                                 const int *__restrict__ ring_inst, int ring_off, int n_ring, CorrCSR C,
+                                                 int n_tgt) {
   chain_trigger();
   const int nb_ring = (n_ring + kBlock - 1) / kBlock;
   int b = blockIdx.x;
   if (b < nb_ring) {
     const int t = b * kBlock + threadIdx.x;
-    int src = 0, dst = 0;
+    int src = 0, dst = 0, inst = -1;
     if (t < n_ring) {
       src = __ldg(ring + 2 * (ring_off + t));
       dst = __ldg(ring + 2 * (ring_off + t) + 1);
+      if (ring_inst) inst = __ldg(ring_inst + ring_off + t);
     }
     chain_wait();
-    if (t < n_ring) f.QC[dst] = f.Q[src];
+    if (t < n_ring && (inst < 0 || f.active[inst])) f.QC[dst] = f.Q[src];
     return;
   }
   b -= nb_ring;
@@ -424,7 +438,9 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
     const double pN = __ldg(PDnS + ci + (cj + 1) * cmx), pS = __ldg(PDnS + ci + cj * cmx);
     const double pC = __ldg(PCC + s);
     const int dst = __ldg(f.fp + 2 * (P.fp_off + s) + 1);
+    const int inst = P.inst;
     chain_wait();
+    if (!f.active[inst]) return;
     const double *Qp = f.Q + q_off;
     const double *Fp = f.F + c_off;
     double rf[4];
@@ -449,8 +465,9 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
   b -= D.nblocks;
   const int t = b * kBlock + threadIdx.x;
   const int cell = t < n_tgt ? C.cell[t] : 0;
+  const int inst = t < n_tgt ? Lc.patches[C.patch[t]].inst : 0;
   chain_wait();
-  if (t >= n_tgt) return;
+  if (t >= n_tgt || !f.active[inst]) return;
   f.F[cell] = add_corrections(f.F[cell], C, t, L, Lc, f, false);
 }
 
@@ -478,8 +495,9 @@ __global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, Fields f
   for (int dj = 0; dj < 3; ++dj)
 #pragma unroll
     for (int di = 0; di < 3; ++di) src[dj][di] = __ldg(win + (a + di) + (b + dj) * ldw);
-  const int qc_off = P.qc_off, q_off = P.q_off, ldq = P.mx + 2;
+  const int qc_off = P.qc_off, q_off = P.q_off, ldq = P.mx + 2, inst = P.inst;
   chain_wait();
+  const int act = f.active[inst];
   const double *QC = f.QC + qc_off;
   double E[3][3];
 #pragma unroll
@@ -498,6 +516,7 @@ __global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, Fields f
   double *Q = f.Q + q_off;
   const int c = (2 * a + 1) + (2 * b + 1) * ldq;
   if (correct) {
+    if (!act) return;
     Q[c] = Q[c] + f11;
     Q[c + 1] = Q[c + 1] + f21;
     Q[c + ldq] = Q[c + ldq] + f12;
@@ -513,132 +532,119 @@ __global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, Fields f
 // ---------------------------------------------------------------------------
 // Coarsest solve (ebCoarsest.m:79-91): u = Ainv (F + bcRhs), one warp per
 // row; lane l sums columns l, l+32, ... in order, then a halving tree.
+struct CoarsestD {
+  int c_off, q_off, n1, N, inst, pad;
+  long long ainv_off, rhs_off;
+};
+
 __global__ void __launch_bounds__(kBlock) k_coarsest(const double *__restrict__ Ainv, const double *__restrict__ bcRhs,
-                                                     Fields f, int c_off, int q_off, int n1, int N) {
+                                                     const CoarsestD *__restrict__ cd, Fields f) {
   chain_trigger();
+  const CoarsestD D = cd[blockIdx.y];
+  const int N = D.N;
   const int row = (blockIdx.x * kBlock + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (row >= N) {
     chain_wait();
     return;
   }
-  const double *a = Ainv + (size_t)row * N;
+  const double *a = Ainv + D.ainv_off + (size_t)row * N;
+  const double *rhs = bcRhs + D.rhs_off;
   constexpr int kPre = 8;   // inverse entries held in registers (N <= 256)
   double av[kPre], bv[kPre];
 #pragma unroll
   for (int i = 0; i < kPre; ++i) {
     const int c = lane + 32 * i;
     av[i] = c < N ? __ldg(a + c) : 0.0;
-    bv[i] = c < N ? __ldg(bcRhs + c) : 0.0;
+    bv[i] = c < N ? __ldg(rhs + c) : 0.0;
   }
   chain_wait();
-  const double *F = f.F + c_off;
+  const int act = f.active[D.inst];
+  const double *F = f.F + D.c_off;
   double s = 0.0;
 #pragma unroll
   for (int i = 0; i < kPre; ++i) {
     const int c = lane + 32 * i;
     if (c < N) s = s + av[i] * (F[c] + bv[i]);
   }
-  for (int c = lane + 32 * kPre; c < N; c += 32) s = s + a[c] * (F[c] + bcRhs[c]);
+  for (int c = lane + 32 * kPre; c < N; c += 32) s = s + a[c] * (F[c] + rhs[c]);
 #pragma unroll
   for (int off = 16; off >= 1; off >>= 1) {
     const double o = __shfl_down_sync(0xffffffffu, s, off);
     if (lane < off) s = s + o;
   }
-  if (lane == 0) {
-    const int i = row % n1, j = row / n1;
-    f.Q[q_off + (i + 1) + (j + 1) * (n1 + 2)] = s;
+  if (lane == 0 && act) {
+    const int i = row % D.n1, j = row / D.n1;
+    f.Q[D.q_off + (i + 1) + (j + 1) * (D.n1 + 2)] = s;
   }
 }
 
 // ---------------------------------------------------------------------------
-// Composite residual (ebCompResidual.m:15-85) of every level >= root in one
-// launch.  Segments (block ranges) of four kinds:
-//   0  r = FTrue - op(Q) on the visible cells of a level, correction targets
-//      excluded while the corrections are on
-//   1  r at the level's correction targets, corrections added in order, the
-//      coarse values taken as the refreshed QC holds them
-//   2  QC ring refresh of a level (ebCompResidual.m:25)
-//   3  QC interior refresh of a level (ebCompResidual.m:32-38)
-// Max-norms reduce through an order-free atomic max on the bit pattern of
-// non-negative doubles; the L2 sum keeps one partial per residual block in a
-// fixed slot.
+// Composite residual (ebCompResidual.m:15-85) of every level >= root, for one
+// hierarchy or every instance of a batch, in one launch.  The work is a list
+// of warp tasks, each covering up to 32 items of ONE patch (or of one
+// instance's correction targets), so every warp belongs to one instance:
+//   kind 0  r = FTrue - op(Q) on visible cells of a patch in the norms,
+//           correction targets excluded while the corrections are on
+//   kind 1  r at correction targets of a level, corrections added in order,
+//           the coarse values taken as the refreshed QC holds them
+//   kind 2  QC ring refresh of a patch (ebCompResidual.m:25)
+//   kind 3  QC interior refresh of a patch (ebCompResidual.m:32-38)
+// A residual warp reduces its values (fixed shuffle tree) into one slot;
+// k_residual_final reduces each instance's slots.  Max-norms are order-free,
+// so linf and rel do not depend on the task layout.
 struct ResAcc {
   double out[5];        // linf, l2, fnorm, rel, ncell
 };
 
-struct ResSeg {
-  int kind, level, block0, slot0;
+struct ResTask {
+  int kind, level, a, b, n, slot, pad0, pad1;   // a: patch / CSR level / ring start; b: first item
 };
 
 struct LevelX {
   LevelD L;
-  Decomp cell, coarse;
   CorrCSR C;            // corrections contributed by this (fine) level
-  int ct_n, ring_off, ring_n, pad;
+  int ct_n, pad;
 };
 
-// per residual block: max |r|, sum r^2, max |FTrue| of its 256 cells, in a
-// fixed warp-tree order
-__device__ __forceinline__ void block_reduce_store(double li, double sq, double fn, double *slot_li, double *slot_sq,
-                                                   double *slot_fn) {
-  __shared__ double s_li[kBlock / 32], s_sq[kBlock / 32], s_fn[kBlock / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int off = 16; off >= 1; off >>= 1) {
-    li = fmax(li, __shfl_down_sync(0xffffffffu, li, off));
-    fn = fmax(fn, __shfl_down_sync(0xffffffffu, fn, off));
-    sq = sq + __shfl_down_sync(0xffffffffu, sq, off);
-  }
-  if (lane == 0) { s_li[w] = li; s_sq[w] = sq; s_fn[w] = fn; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double Lm = s_li[0], S = s_sq[0], Fn = s_fn[0];
-    for (int i = 1; i < kBlock / 32; ++i) { Lm = fmax(Lm, s_li[i]); S = S + s_sq[i]; Fn = fmax(Fn, s_fn[i]); }
-    *slot_li = Lm;
-    *slot_sq = S;
-    *slot_fn = Fn;
-  }
-}
-
-__global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ X, const ResSeg *__restrict__ segs,
-                                                     const unsigned char *__restrict__ blk_seg, Fields f,
+__global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ X, const PatchD *__restrict__ patches,
+                                                     const ResTask *__restrict__ tasks, int ntask, Fields f,
                                                      const int *__restrict__ ring, double *slots, int nslots,
                                                      int mass_corr) {
   chain_trigger();
-  const ResSeg S = segs[blk_seg[blockIdx.x]];
-  const int b = blockIdx.x - S.block0;
-  const int g = b * kBlock + threadIdx.x;
-  const LevelX &Xk = X[S.level];
-  if (S.kind >= 2) {
+  const int w = blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= ntask) {
     chain_wait();
-    if (!mass_corr) return;
-    if (S.kind == 2) {
-      if (g < Xk.ring_n) {
-        const int i = Xk.ring_off + g;
-        f.QC[__ldg(ring + 2 * i + 1)] = f.Q[__ldg(ring + 2 * i)];
-      }
+    return;
+  }
+  const ResTask T = tasks[w];
+  const bool have = lane < T.n;
+  if (T.kind >= 2) {
+    chain_wait();
+    if (!mass_corr || !have) return;
+    if (T.kind == 2) {
+      const int i = T.a + lane;
+      f.QC[__ldg(ring + 2 * i + 1)] = f.Q[__ldg(ring + 2 * i)];
       return;
     }
-    if (g >= Xk.coarse.n) return;
-    const int p = find_patch(Xk.coarse, b, g);
-    const PatchD &P = Xk.L.patches[p];
+    const PatchD &P = patches[T.a];
     const int cmx = P.mx >> 1;
-    const int s = g - __ldg(Xk.coarse.beg + p);
+    const int s = T.b + lane;
     const int cj = s / cmx, ci = s - cj * cmx;
     f.QC[P.qc_off + (ci + 1) + (cj + 1) * (cmx + 2)] = restrict_cell(f.Q + P.q_off, P.mx + 2, ci, cj);
     return;
   }
   double li = 0, sq = 0, fn = 0;
-  if (S.kind == 0) {
+  const LevelX &Xk = X[T.level];
+  if (T.kind == 0) {
     bool on = false;
     int c = 0, ldq = 0, q_off = 0;
     double ft = 0, dE = 0, dW = 0, dN = 0, dS = 0, cf = 0;
-    if (g < Xk.cell.n) {
-      const int p = find_patch(Xk.cell, b, g);
-      const PatchD &P = Xk.L.patches[p];
+    if (have) {
+      const PatchD &P = patches[T.a];
       const int mx = P.mx;
-      const int s = g - __ldg(Xk.cell.beg + p);
+      const int s = T.b + lane;
       const int lj = s / mx, lx = s - lj * mx;
       const int cc = P.c_off + s;
       const uint8_t fl = __ldg(f.flags + cc);
@@ -664,10 +670,11 @@ __global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ 
       sq = r * r;
       fn = fabs(ft);
     }
-  } else {
-    chain_wait();   // kind 1: targets of this level, corrections from the level above
-    const LevelX &Xf = X[S.level + 1];
-    if (mass_corr && g < Xf.ct_n) {
+  } else {   // kind 1: targets of this level, corrections from the level above
+    chain_wait();
+    const LevelX &Xf = X[T.level + 1];
+    if (mass_corr && have) {
+      const int g = T.b + lane;
       const int cell = Xf.C.cell[g];
       const PatchD &Pc = Xk.L.patches[Xf.C.patch[g]];
       const int s = cell - Pc.c_off;
@@ -683,25 +690,54 @@ __global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ 
       }
     }
   }
-  const int sl = S.slot0 + b;
-  block_reduce_store(li, sq, fn, slots + sl, slots + nslots + sl, slots + 2 * nslots + sl);
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) {
+    li = fmax(li, __shfl_down_sync(0xffffffffu, li, off));
+    fn = fmax(fn, __shfl_down_sync(0xffffffffu, fn, off));
+    sq = sq + __shfl_down_sync(0xffffffffu, sq, off);
+  }
+  if (lane == 0) {
+    slots[T.slot] = li;
+    slots[nslots + T.slot] = sq;
+    slots[2 * nslots + T.slot] = fn;
+  }
 }
 
-// finish the residual in one block: max-norms over every residual block,
-// L2 per level from that level's block partials in a fixed tree order,
-// weighted by the level's cell area; rel = linf / max(fnorm, realmin)
-constexpr int kFinal = 512;
-__global__ void __launch_bounds__(kFinal) k_residual_final(ResAcc *acc, const double *slots, int nslots,
-                                                          const int *level_slot0, const double *area, int nlevels_res,
-                                                          double ncell) {
+// per instance: the slot ranges of its residual tasks, level by level
+struct InstRes {
+  int range0, range1;   // into the (slot0, slot1, level area) range table
+  int max_vcycles, pad;
+  double rel_tol, ncell;
+};
+
+struct SlotRange {
+  int s0, s1;
+  double area;
+};
+
+// finish the residual of every instance (one block per instance): max-norms
+// over its slots, L2 per level from that level's slots in a fixed tree order
+// weighted by the cell area, rel = linf / max(fnorm, realmin).  mode 0 is
+// the residual before the first V-cycle; mode 1 follows a V-cycle of the
+// instances active during it; mode 2 only reports (an eager call).  The history and the stop test follow
+// ebSolveCycles.m:17-46: an instance stays active while it < MaxVCycles and
+// rel > RelTol.
+constexpr int kFinal = 256;
+__global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__restrict__ ir,
+                                                          const SlotRange *__restrict__ ranges, const double *slots,
+                                                          int nslots, ResAcc *acc, int *active, int *iters,
+                                                          double *hist, int hist_stride, int mode) {
   chain_in();
+  const int inst = blockIdx.x;
+  const InstRes R = ir[inst];
   __shared__ double s_a[kFinal], s_b[kFinal];
   const int t = threadIdx.x;
   double li = 0, fn = 0;
-  for (int i = t; i < nslots; i += kFinal) {
-    li = fmax(li, slots[i]);
-    fn = fmax(fn, slots[2 * nslots + i]);
-  }
+  for (int r = R.range0; r < R.range1; ++r)
+    for (int i = ranges[r].s0 + t; i < ranges[r].s1; i += kFinal) {
+      li = fmax(li, slots[i]);
+      fn = fmax(fn, slots[2 * nslots + i]);
+    }
   s_a[t] = li;
   s_b[t] = fn;
   __syncthreads();
@@ -716,26 +752,58 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(ResAcc *acc, const do
   double fnorm = s_b[0];
   __syncthreads();
   double l2sq = 0;
-  for (int l = 0; l < nlevels_res; ++l) {
-    double s = 0;
-    for (int i = level_slot0[l] + t; i < level_slot0[l + 1]; i += kFinal) s = s + slots[nslots + i];
-    s_a[t] = s;
+  for (int r = R.range0; r < R.range1; ++r) {
+    double sum = 0;
+    for (int i = ranges[r].s0 + t; i < ranges[r].s1; i += kFinal) sum = sum + slots[nslots + i];
+    s_a[t] = sum;
     __syncthreads();
     for (int off = kFinal / 2; off >= 1; off >>= 1) {
       if (t < off) s_a[t] = s_a[t] + s_a[t + off];
       __syncthreads();
     }
-    l2sq = l2sq + s_a[0] * area[l];
+    l2sq = l2sq + s_a[0] * ranges[r].area;
     __syncthreads();
   }
   if (t == 0) {
     fnorm = fnorm > 2.2250738585072014e-308 ? fnorm : 2.2250738585072014e-308;
-    acc->out[0] = linf;
-    acc->out[1] = sqrt(l2sq);
-    acc->out[2] = fnorm;
-    acc->out[3] = linf / fnorm;
-    acc->out[4] = ncell;
+    const double rel = linf / fnorm;
+    ResAcc &A = acc[inst];
+    if (mode == 2 || mode == 0 || active[inst]) {
+      A.out[0] = linf;
+      A.out[1] = sqrt(l2sq);
+      A.out[2] = fnorm;
+      A.out[3] = rel;
+      A.out[4] = R.ncell;
+    }
+    if (mode != 2 && (mode == 0 || active[inst])) {
+      int it = iters[inst];
+      if (mode == 0) it = 0;
+      else it = it + 1;
+      iters[inst] = it;
+      if (it < hist_stride) hist[(size_t)inst * hist_stride + it] = linf;
+      active[inst] = (it < R.max_vcycles && rel > R.rel_tol) ? 1 : 0;
+    }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Force reset F = FTrue (ebSolveCycles.m:30-34) of the active instances of a
+// batch, one thread per cell over every patch of every level (a single
+// hierarchy copies the whole array instead).
+__global__ void __launch_bounds__(kBlock) k_freset(Decomp D, const PatchD *__restrict__ patches, Fields f) {
+  chain_trigger();
+  const int g = blockIdx.x * kBlock + threadIdx.x;
+  if (g >= D.n) {
+    chain_wait();
+    return;
+  }
+  const int p = find_patch(D, blockIdx.x, g);
+  const PatchD &P = patches[p];
+  const int cc = P.c_off + (g - __ldg(D.beg + p));
+  const double v = __ldg(f.FTrue + cc);
+  const int inst = P.inst;
+  chain_wait();
+  if (f.active[inst]) f.F[cc] = v;
 }
 
 // ---------------------------------------------------------------------------

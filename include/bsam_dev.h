@@ -71,7 +71,17 @@ typedef struct {
   const double *bcRhs;      /* [ncoarse]                                    */
   int64_t n_q, n_cells, n_dew, n_dns, n_qc, n_bcg, n_cfd, n_pcoef;
   int64_t n_same, n_ring, n_win, n_fp, n_corr;
-  int32_t ncoarse, singular;
+  int32_t ncoarse, singular;  /* coarsest unknowns (all instances), singular flag */
+  /* A batch of independent instances (ninst >= 2) solved together: every
+   * level k holds the level-k patches of every instance (instance by
+   * instance, all instances sharing the level's cell size); patch_inst
+   * [npatch] gives each patch's 0-based instance, inst_root [ninst] each
+   * instance's root level, and level 1 holds one patch per instance whose
+   * inverse blocks are concatenated in Ainv / bcRhs in instance order.
+   * ninst = 0 or 1 is a single hierarchy (patch_inst, inst_root unused). */
+  int32_t ninst;
+  const int32_t *patch_inst;
+  const int32_t *inst_root;
 } bsam_hier_desc;
 
 /* Solver options: ebOptions.m:44-73 names (NPre, NPost, Omega, GhostInterp,
@@ -120,6 +130,19 @@ int bsam_prolong_level(bsam_hier h, int level);
  * device; read it with bsam_get_field(BSAM_FIELD_Q). */
 int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles, double *final_rel,
                       int64_t *visible_cells);
+
+/* Per-instance results of the last bsam_solve_cycles on a batch (instance
+ * 0 is what bsam_solve_cycles itself reports).  Every instance runs
+ * ebSolveCycles' own loop: it stops at its own RelTol / MaxVCycles and its
+ * state then stays frozen while the other instances continue, so each
+ * instance's solution and history equal those of a solve of it alone.
+ * No reference counterpart (the reference solves one hierarchy per call). */
+int bsam_batch_result(bsam_hier h, int inst, double *res_hist, int hist_cap, int *vcycles, double *final_rel,
+                      int64_t *visible_cells);
+
+/* Stop test (MaxVCycles, RelTol) of one instance of a batch; bsam_set_opts
+ * sets every instance's to the options' values. */
+int bsam_batch_set_stop(bsam_hier h, int inst, int max_vcycles, double rel_tol);
 
 /* One ebVcycle(H, nlev) + ebTransfer(H,0,'filldown') (ebVcycle.m:16-35,
  * ebTransfer.m:73-79), force reset included (ebSolveCycles.m:30-34). */
