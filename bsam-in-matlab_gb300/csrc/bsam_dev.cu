@@ -131,6 +131,7 @@ struct bsam_hier_s {
   DBuf<uint8_t> flags;
   DBuf<int> win, fp, ring, ints, ct_cell, ct_patch, ct_beg, ct_item, ct_j, active, iters, ones;
   DBuf<int> g_inst, ring_inst;     // instance per ghost item / ring entry (batches only)
+  DBuf<int> inst_nlev;             // per instance: its finest level
   DecompH all_cells;               // every cell of every level (batch force reset)
   std::vector<InstRes> hir;        // host copy of the per-instance reduction plan
   // results of the last solve, per instance
@@ -249,12 +250,14 @@ GhostItems ghost_items(bsam_hier h) {
                     h->ninst > 1 ? h->g_inst.p : nullptr};
 }
 
-void launch_fill(bsam_hier h, int k) {
+// ghost fill of level k; `need` > 0 restricts a batch's fill to the
+// instances that have level `need` (the fill after restricting level need)
+void launch_fill(bsam_hier h, int k, int need = 0) {
   const LevelPlan &L = h->lev[k];
   if (!L.g1_n) return;
   Launch l(h, K_GHOST, 0, k);
   launch_k(h, k_ghost, nblk(L.g1_n), kBlock, ghost_items(h), L.g1_off, L.g1_n, h->Q.p, h->QC.p,
-           (const double *)h->bcg.p, L.hx, L.hy, (const int *)h->active.p);
+           (const double *)h->bcg.p, L.hx, L.hy, (const int *)h->active.p, (const int *)h->inst_nlev.p, need);
 }
 
 // ebRelaxLevel (ebRelaxLevel.m:28-38): 2*nsweeps colour passes; the ghost
@@ -336,7 +339,7 @@ void launch_vcycle(bsam_hier h, int k) {
   }
   launch_relax(h, k, h->opts.npre);
   launch_restrict(h, k, 1);
-  launch_fill(h, k - 1);
+  launch_fill(h, k - 1, k);
   launch_coarse_load(h, k);
   launch_vcycle(h, k - 1);
   launch_prolong(h, k, 1);
@@ -347,7 +350,7 @@ void launch_vcycle(bsam_hier h, int k) {
 void launch_filldown(bsam_hier h) {
   for (int kk = h->nlev; kk >= 2; --kk) {
     launch_restrict(h, kk, 1);
-    launch_fill(h, kk - 1);
+    launch_fill(h, kk - 1, kk);
   }
 }
 
@@ -978,7 +981,10 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
     for (int t = B.P(p)[PD_RING0]; t < B.P(p)[PD_RING1]; ++t) rinst[t] = pinst[p];
   h->hir = ir;
   h->hist_stride = h->opts.max_vcycles + 1;
-  if ((rc = h->g_inst.upload(B.gi.data(), B.gi.size(), s)) || (rc = h->ring_inst.upload(rinst.data(), rinst.size(), s)))
+  std::vector<int> inlev(h->ninst, 0);
+  for (int p = 0; p < d->npatch; ++p) inlev[pinst[p]] = std::max(inlev[pinst[p]], (int)B.P(p)[PD_LEVEL]);
+  if ((rc = h->g_inst.upload(B.gi.data(), B.gi.size(), s)) || (rc = h->ring_inst.upload(rinst.data(), rinst.size(), s)) ||
+      (rc = h->inst_nlev.upload(inlev.data(), inlev.size(), s)))
     return rc;
   if ((rc = h->flags.upload(flags.data(), flags.size(), s)) || (rc = h->ints.upload(B.ints.data(), B.ints.size(), s)) ||
       (rc = h->g_type.upload(B.gt.data(), B.gt.size(), s)) || (rc = h->g_dst.upload(B.gdst.data(), B.gdst.size(), s)) ||
@@ -1034,7 +1040,7 @@ void release(bsam_hier h) {
                           &h->saveF})
     b->release();
   for (DBuf<int> *b : {&h->win, &h->fp, &h->ring, &h->ints, &h->ct_cell, &h->ct_patch, &h->ct_beg, &h->ct_item,
-                       &h->ct_j, &h->active, &h->iters, &h->ones, &h->g_inst, &h->ring_inst, &h->g_dst, &h->g_a, &h->g_b, &h->g_c, &h->g_d, &h->g_e})
+                       &h->ct_j, &h->active, &h->iters, &h->ones, &h->g_inst, &h->ring_inst, &h->inst_nlev, &h->g_dst, &h->g_a, &h->g_b, &h->g_c, &h->g_d, &h->g_e})
     b->release();
   h->flags.release(); h->g_type.release(); h->patches.release(); h->acc.release(); h->perim.release();
   h->rchunks.release(); h->levelx.release(); h->rtasks.release(); h->instres.release(); h->sranges.release();

@@ -124,7 +124,8 @@ __device__ __forceinline__ double eval_rule(const GhostItems &G, int i, const do
 
 __global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, double *__restrict__ Q,
                                                   double *__restrict__ QC, const double *__restrict__ bcg,
-                                                  double hx, double hy, const int *__restrict__ active) {
+                                                  double hx, double hy, const int *__restrict__ active,
+                                                  const int *__restrict__ inst_nlev, int need) {
   chain_trigger();
   const int t = blockIdx.x * kBlock + threadIdx.x;
   const int i = off + t;
@@ -133,7 +134,10 @@ __global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, 
   const int inst = (t < n && G.inst) ? G.inst[i] : -1;
   chain_wait();
   if (t >= n) return;
-  if (inst >= 0 && !active[inst]) return;   // a converged instance of a batch stays frozen
+  // a converged instance of a batch stays frozen; a fill that follows the
+  // restriction from level `need` skips the instances without that level
+  // (their own V-cycle starts below it)
+  if (inst >= 0 && (!active[inst] || inst_nlev[inst] < need)) return;
   if (ty == G_RING) {
     QC[dst] = Q[G.a[i]];
   } else if (ty == G_PHYS_CORNER) {

@@ -163,3 +163,36 @@ def test_batch_of_one_equals_solo(parts):
     assert ra[0] == rb[0]
     np.testing.assert_array_equal(ra[1], rb[1])
     np.testing.assert_array_equal(a.get(BSAM_FIELD_Q, p.Q.size), split_field(b, FIELD_Q, bh.get(BSAM_FIELD_Q, b.Q.size), 0))
+
+
+@pytest.mark.gpu
+def test_random_instances_batch_equals_solo():
+    """Seeded instances of the batched-instances workload (uneven depths,
+    roots 2-4, several patches per level): batch == solo bit for bit."""
+    import warnings
+    from bsam.device import DeviceBackend, DevHier, BSAM_FIELD_Q
+    from bsam.instances import random_elliptic, final_stage
+    be = DeviceBackend.get(0)
+    parts, opts = [], None
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        for s in range(1000, 1012):
+            prob, o = random_elliptic(s)
+            fl, H = final_stage(prob, o, be)
+            parts.append(fl)
+            opts = opts or H.opts
+    assert len({p.nlev for p in parts}) > 1 and len({p.rootIdx for p in parts}) > 1
+    solo = []
+    for p in parts:
+        dh = DevHier(be.ctx, p, opts)
+        r = dh.solve_cycles(opts.MaxVCycles + 2)
+        solo.append((r, dh.get(BSAM_FIELD_Q, p.Q.size)))
+    b = merge_flats(parts)
+    bh = DevHier(be.ctx, b, opts)
+    bh.solve_cycles(opts.MaxVCycles + 2)
+    Q = bh.get(BSAM_FIELD_Q, b.Q.size)
+    for i, (r, q) in enumerate(solo):
+        rb = bh.batch_result(i, opts.MaxVCycles + 2)
+        assert rb[0] == r[0], (i, rb[0], r[0])
+        np.testing.assert_array_equal(rb[1], r[1])
+        np.testing.assert_array_equal(split_field(b, FIELD_Q, Q, i), q)
