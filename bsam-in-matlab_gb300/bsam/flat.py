@@ -312,3 +312,28 @@ def gather_field(H, fl, which):
             a, o = lev.FTrue[p], int(r[PD_COFF])
         out[o:o + a.size] = np.asarray(a).ravel(order='F')
     return out
+
+
+def visible_q_index(fl):
+    """Q indices of the visible cells (levels >= root, not covered by a finer
+    level), in cell order: the cells the composite norms run over."""
+    out = []
+    for g in range(fl.npatch):
+        r = fl.patches[g]
+        if int(r[PD_LEVEL]) < fl.rootIdx:
+            continue
+        mx, my = int(r[PD_MX]), int(r[PD_MY])
+        co, qo = int(r[PD_COFF]), int(r[PD_QOFF])
+        ii, jj = np.meshgrid(np.arange(mx), np.arange(my), indexing='ij')
+        q = (qo + (ii + 1) + (jj + 1) * (mx + 2)).ravel(order='F')
+        vis = fl.covered[co:co + mx * my] == 0
+        out.append(q[vis])
+    return np.concatenate(out) if out else np.zeros(0, dtype=np.int64)
+
+
+def rel_errors(a, b, idx):
+    """(relative L2, relative max) difference of a against b over idx."""
+    d = a[idx] - b[idx]
+    nb2 = float(np.linalg.norm(b[idx]))
+    nbm = float(np.max(np.abs(b[idx]))) if idx.size else 0.0
+    return (float(np.linalg.norm(d)) / max(nb2, 1e-300), float(np.max(np.abs(d))) / max(nbm, 1e-300) if idx.size else 0.0)

@@ -132,6 +132,10 @@ struct bsam_hier_s {
   DBuf<int> win, fp, ring, ints, ct_cell, ct_patch, ct_beg, ct_item, ct_j, active, iters, ones;
   DBuf<int> g_inst, ring_inst;     // instance per ghost item / ring entry (batches only)
   DBuf<int> inst_nlev;             // per instance: its finest level
+  // mixed form: FP32 correction, its right-hand side and coarse shadows,
+  // FP32 coefficient copies (homogeneous boundary data)
+  DBuf<float> E, F32, QC32, DeW32, DnS32, CC32, ID32, pcoef32, cfd32, bcg32;
+  bool f32_dirty = true;
   DecompH all_cells;               // every cell of every level (batch force reset)
   std::vector<InstRes> hir;        // host copy of the per-instance reduction plan
   // results of the last solve, per instance
@@ -250,23 +254,41 @@ GhostItems ghost_items(bsam_hier h) {
                     h->ninst > 1 ? h->g_inst.p : nullptr};
 }
 
+// the arrays of the FP64 solve or of the FP32 correction cycle
+template <class T> FieldsT<T> fields_t(bsam_hier h);
+template <> Fields fields_t<double>(bsam_hier h) { return fields(h); }
+template <> FieldsT<float> fields_t<float>(bsam_hier h) {
+  FieldsT<float> f;
+  f.Q = h->E.p; f.F = h->F32.p; f.QC = h->QC32.p;
+  f.FTrue = h->FTrue.p; f.CC = h->CC32.p; f.ID = h->ID32.p; f.DeW = h->DeW32.p; f.DnS = h->DnS32.p;
+  f.bcg = h->bcg32.p; f.cfd = h->cfd32.p; f.pcoef = h->pcoef32.p; f.flags = h->flags.p;
+  f.win = h->win.p; f.fp = h->fp.p; f.active = h->active.p;
+  return f;
+}
+
+// algorithmic bytes scale with the value type (FP64 figures x size/8)
+template <class T> constexpr double tscale() { return (double)sizeof(T) / 8.0; }
+
 // ghost fill of level k; `need` > 0 restricts a batch's fill to the
 // instances that have level `need` (the fill after restricting level need)
+template <class T = double>
 void launch_fill(bsam_hier h, int k, int need = 0) {
   const LevelPlan &L = h->lev[k];
   if (!L.g1_n) return;
+  FieldsT<T> f = fields_t<T>(h);
   Launch l(h, K_GHOST, 0, k);
-  launch_k(h, k_ghost, nblk(L.g1_n), kBlock, ghost_items(h), L.g1_off, L.g1_n, h->Q.p, h->QC.p,
-           (const double *)h->bcg.p, L.hx, L.hy, (const int *)h->active.p, (const int *)h->inst_nlev.p, need);
+  launch_k(h, k_ghost<T>, nblk(L.g1_n), kBlock, ghost_items(h), L.g1_off, L.g1_n, f.Q, f.QC, f.bcg, L.hx, L.hy,
+           (const int *)h->active.p, (const int *)h->inst_nlev.p, need);
 }
 
 // ebRelaxLevel (ebRelaxLevel.m:28-38): 2*nsweeps colour passes; the ghost
 // refill after every colour is folded into the next pass (k_relax `fresh`),
 // and one fill after the last pass leaves the ghost frame as the reference's.
+template <class T = double>
 void launch_relax(bsam_hier h, int k, int nsweeps) {
   if (nsweeps <= 0) return;
   const LevelPlan &L = h->lev[k];
-  Fields f = fields(h);
+  FieldsT<T> f = fields_t<T>(h);
   LevelD ld = leveld(h, k);
   const RelaxChunk *ch = h->rchunks.p + L.rc_off;
   const int grid = (L.rc_n + kBlock / kChunk - 1) / (kBlock / kChunk);
@@ -274,22 +296,23 @@ void launch_relax(bsam_hier h, int k, int nsweeps) {
   for (int s = 0; s < nsweeps; ++s)
     for (int m = 0; m < 2; ++m) {
       const int fresh = (s > 0 || m > 0) ? 1 : 0;
-      Launch l(h, K_RELAX, 24.0 * (double)L.ncells, k);
+      Launch l(h, K_RELAX, 24.0 * tscale<T>() * (double)L.ncells, k);
       if (L.pow2)
-        launch_k(h, k_relax<true>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m, h->opts.omega, unit,
-                 fresh);
+        launch_k(h, k_relax<T, true>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m, h->opts.omega,
+                 unit, fresh);
       else
-        launch_k(h, k_relax<false>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m, h->opts.omega, unit,
-                 fresh);
+        launch_k(h, k_relax<T, false>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m, h->opts.omega,
+                 unit, fresh);
     }
-  launch_fill(h, k);
+  launch_fill<T>(h, k);
 }
 
+template <class T = double>
 void launch_restrict(bsam_hier h, int k, int to_parent) {
   const LevelPlan &L = h->lev[k];
   Decomp D = decomp(h, L.coarse);
-  Launch l(h, K_RESTRICT, 12.0 * (double)L.ncells, k);
-  launch_k(h, k_restrict, D.nblocks, kBlock, leveld(h, k), D, fields(h), to_parent);
+  Launch l(h, K_RESTRICT, 12.0 * tscale<T>() * (double)L.ncells, k);
+  launch_k(h, k_restrict<T>, D.nblocks, kBlock, leveld(h, k), D, fields_t<T>(h), to_parent);
 }
 
 CorrCSR corr_csr(bsam_hier h, const LevelPlan &L) {
@@ -297,23 +320,27 @@ CorrCSR corr_csr(bsam_hier h, const LevelPlan &L) {
 }
 
 // ebTransfer 'ring' + ebCoarseLoad (ebVcycle.m:28-29) in one launch
+template <class T = double>
 void launch_coarse_load(bsam_hier h, int k) {
   const LevelPlan &L = h->lev[k];
   Decomp D = decomp(h, L.coarse);
   const int ntgt = h->opts.mass_correction ? L.ct_n : 0;
   const int grid = nblk(L.ring_n) + D.nblocks + nblk(ntgt);
-  Launch l(h, K_LOAD, 50.0 * (double)L.ncells, k);
-  launch_k(h, k_load, grid, kBlock, leveld(h, k), leveld(h, k - 1), D, fields(h), (const int *)h->ring.p,
+  Launch l(h, K_LOAD, 50.0 * tscale<T>() * (double)L.ncells, k);
+  launch_k(h, k_load<T>, grid, kBlock, leveld(h, k), leveld(h, k - 1), D, fields_t<T>(h), (const int *)h->ring.p,
            (const int *)(h->ninst > 1 ? h->ring_inst.p : nullptr), L.ring_off, L.ring_n, corr_csr(h, L), ntgt);
 }
 
+template <class T = double>
 void launch_prolong(bsam_hier h, int k, int correct) {
   const LevelPlan &L = h->lev[k];
   Decomp D = decomp(h, L.coarse);
-  Launch l(h, K_PROLONG, 20.0 * (double)L.ncells, k);
-  launch_k(h, k_prolong, D.nblocks, kBlock, leveld(h, k), D, fields(h), correct);
+  Launch l(h, K_PROLONG, 20.0 * tscale<T>() * (double)L.ncells, k);
+  launch_k(h, k_prolong<T>, D.nblocks, kBlock, leveld(h, k), D, fields_t<T>(h), correct);
 }
 
+// the FP32 correction cycle solves a homogeneous problem: no boundary rhs
+template <class T = double>
 void launch_coarsest(bsam_hier h) {
   {
     Launch l(h, K_COARSEST, 8.0 * (double)h->Ainv.n, 1);
@@ -326,25 +353,27 @@ void launch_coarsest(bsam_hier h) {
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, k_coarsest, (const double *)h->Ainv.p, (const double *)h->bcRhs.p,
-                       (const CoarsestD *)h->coarsest.p, fields(h));
+    const double *rhs = sizeof(T) == sizeof(double) ? (const double *)h->bcRhs.p : nullptr;
+    cudaLaunchKernelEx(&cfg, k_coarsest<T>, (const double *)h->Ainv.p, rhs, (const CoarsestD *)h->coarsest.p,
+                       fields_t<T>(h));
   }
-  launch_fill(h, 1);
+  launch_fill<T>(h, 1);
 }
 
+template <class T = double>
 void launch_vcycle(bsam_hier h, int k) {
   if (k == 1) {
-    launch_coarsest(h);
+    launch_coarsest<T>(h);
     return;
   }
-  launch_relax(h, k, h->opts.npre);
-  launch_restrict(h, k, 1);
-  launch_fill(h, k - 1, k);
-  launch_coarse_load(h, k);
-  launch_vcycle(h, k - 1);
-  launch_prolong(h, k, 1);
-  launch_fill(h, k);
-  launch_relax(h, k, h->opts.npost);
+  launch_relax<T>(h, k, h->opts.npre);
+  launch_restrict<T>(h, k, 1);
+  launch_fill<T>(h, k - 1, k);
+  launch_coarse_load<T>(h, k);
+  launch_vcycle<T>(h, k - 1);
+  launch_prolong<T>(h, k, 1);
+  launch_fill<T>(h, k);
+  launch_relax<T>(h, k, h->opts.npost);
 }
 
 void launch_filldown(bsam_hier h) {
@@ -354,9 +383,12 @@ void launch_filldown(bsam_hier h) {
   }
 }
 
+bool mixed(bsam_hier h) { return h->opts.precision == 1; }
+
 // ebCompResidual (ebCompResidual.m:15-85): one launch over every level of
 // every instance, then the per-instance reduction and stop test (mode 0:
-// before the first V-cycle, 1: after one)
+// before the first V-cycle, 1: after one, 2: report only).  The mixed form
+// also stores r (FP32) as the right-hand side of the next correction cycle.
 void launch_residual(bsam_hier h, int mode) {
   double bytes = 0;
   for (int k = 1; k <= h->nlev; ++k) bytes += 41.0 * (double)h->lev[k].ncells;
@@ -364,16 +396,43 @@ void launch_residual(bsam_hier h, int mode) {
     Launch l(h, K_RESID, bytes);
     launch_k(h, k_residual, (h->nrtasks + kBlock / 32 - 1) / (kBlock / 32), kBlock, (const LevelX *)h->levelx.p,
              (const PatchD *)h->patches.p, (const ResTask *)h->rtasks.p, h->nrtasks, fields(h), (const int *)h->ring.p,
-             h->slots.p, h->nslots, h->opts.mass_correction);
+             h->slots.p, h->nslots, h->opts.mass_correction, mixed(h) ? h->F32.p : (float *)nullptr);
   }
   Launch l(h, K_RESID, 0);
   launch_k(h, k_residual_final, h->ninst, kFinal, (const InstRes *)h->instres.p, (const SlotRange *)h->sranges.p,
            (const double *)h->slots.p, h->nslots, h->acc.p, h->active.p, h->iters.p, h->hist.p, h->hist_stride, mode);
 }
 
-// one ebSolveCycles iteration body: F = FTrue, V-cycle, fill-down, residual
-// (mode 1 inside ebSolveCycles, 2 for an eager V-cycle)
+// Mixed form: after Q changed on every level at once (or before the first
+// correction, when a new level's parent still holds its old values under
+// the footprint), restrict finest first, then refill the ghosts coarsest
+// first, so every fill reads parent cells (ghosts included) that are up to
+// date and the composite residual sees a consistent hierarchy.
+void launch_consistent(bsam_hier h) {
+  for (int kk = h->nlev; kk >= 2; --kk) launch_restrict(h, kk, 1);
+  for (int k = 1; k <= h->nlev; ++k) launch_fill(h, k);
+}
+
+// one ebSolveCycles iteration body (mode 1 inside ebSolveCycles, 2 for an
+// eager V-cycle).  FP64: F = FTrue, V-cycle, fill-down, residual.  Mixed:
+// the FP32 correction E = 0, one FP32 FAS V-cycle of E against the stored
+// residual, Q += E in FP64, restriction and ghost fill in FP64, FP64
+// residual.
 int launch_iteration(bsam_hier h, int mode) {
+  if (mixed(h)) {
+    CK(cudaMemsetAsync(h->E.p, 0, sizeof(float) * h->E.n, h->stream));
+    launch_vcycle<float>(h, h->nlev);
+    {
+      Decomp D = decomp(h, h->all_cells);
+      Launch l(h, K_PROLONG, 20.0 * (double)h->n_cells);
+      launch_k(h, k_update, D.nblocks, kBlock, D, (const PatchD *)h->patches.p, h->Q.p, (const float *)h->E.p,
+               (const int *)h->active.p);
+    }
+    launch_consistent(h);
+    launch_residual(h, mode);
+    CK(cudaGetLastError());
+    return BSAM_OK;
+  }
   if (h->ninst == 1) {
     CK(cudaMemcpyAsync(h->F.p, h->FTrue.p, sizeof(double) * h->n_cells, cudaMemcpyDeviceToDevice, h->stream));
   } else {
@@ -385,6 +444,34 @@ int launch_iteration(bsam_hier h, int mode) {
   launch_filldown(h);
   launch_residual(h, mode);
   CK(cudaGetLastError());
+  return BSAM_OK;
+}
+
+// FP32 arrays of the mixed form: allocated on first use, coefficient copies
+// refreshed whenever the FP64 coefficients changed
+int ensure_f32(bsam_hier h) {
+  if (!mixed(h)) return BSAM_OK;
+  int rc;
+  if (!h->E.p) {
+    if ((rc = h->E.alloc(h->Q.n)) || (rc = h->F32.alloc(h->F.n)) || (rc = h->QC32.alloc(std::max<size_t>(h->QC.n, 1))) ||
+        (rc = h->DeW32.alloc(h->DeW.n)) || (rc = h->DnS32.alloc(h->DnS.n)) || (rc = h->CC32.alloc(h->CC.n)) ||
+        (rc = h->ID32.alloc(h->ID.n)) || (rc = h->pcoef32.alloc(std::max<size_t>(h->pcoef.n, 1))) ||
+        (rc = h->cfd32.alloc(std::max<size_t>(h->cfd.n, 1))) || (rc = h->bcg32.alloc(std::max<size_t>(h->bcg.n, 1))))
+      return rc;
+    CK(cudaMemsetAsync(h->F32.p, 0, sizeof(float) * h->F32.n, h->stream));
+    CK(cudaMemsetAsync(h->QC32.p, 0, sizeof(float) * h->QC32.n, h->stream));
+    CK(cudaMemsetAsync(h->bcg32.p, 0, sizeof(float) * h->bcg32.n, h->stream));
+    h->f32_dirty = true;
+  }
+  if (h->f32_dirty) {
+    const std::pair<DBuf<double> *, DBuf<float> *> cv[] = {{&h->DeW, &h->DeW32}, {&h->DnS, &h->DnS32},
+                                                           {&h->CC, &h->CC32},   {&h->ID, &h->ID32},
+                                                           {&h->pcoef, &h->pcoef32}, {&h->cfd, &h->cfd32}};
+    for (const auto &c : cv)
+      if (c.first->n) launch_k(h, k_to_f32, 4 * 152, kBlock, (const double *)c.first->p, c.second->p, (long long)c.first->n);
+    CK(cudaGetLastError());
+    h->f32_dirty = false;
+  }
   return BSAM_OK;
 }
 
@@ -1039,6 +1126,9 @@ void release(bsam_hier h) {
                           &h->pcoef, &h->Ainv, &h->bcRhs, &h->slots, &h->partials, &h->hist, &h->saveQ, &h->saveQC,
                           &h->saveF})
     b->release();
+  for (DBuf<float> *b : {&h->E, &h->F32, &h->QC32, &h->DeW32, &h->DnS32, &h->CC32, &h->ID32, &h->pcoef32, &h->cfd32,
+                         &h->bcg32})
+    b->release();
   for (DBuf<int> *b : {&h->win, &h->fp, &h->ring, &h->ints, &h->ct_cell, &h->ct_patch, &h->ct_beg, &h->ct_item,
                        &h->ct_j, &h->active, &h->iters, &h->ones, &h->g_inst, &h->ring_inst, &h->inst_nlev, &h->g_dst, &h->g_a, &h->g_b, &h->g_c, &h->g_d, &h->g_e})
     b->release();
@@ -1160,6 +1250,7 @@ int bsam_set_field(bsam_hier h, int which, const double *host, int64_t n) {
   if (rc) return rc;
   if (n) CK(cudaMemcpyAsync(b->p, host, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  if (which == BSAM_FIELD_CC || which == BSAM_FIELD_INVDIAG) h->f32_dirty = true;
   return BSAM_OK;
 }
 
@@ -1217,7 +1308,12 @@ int bsam_comp_residual(bsam_hier h, double out[5]) {
 int bsam_vcycle(bsam_hier h) {
   if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
   int rc = set_device(h);
-  if (rc || (rc = launch_iteration(h, 2))) return rc;
+  if (rc || (rc = ensure_f32(h))) return rc;
+  if (mixed(h)) {   // the correction cycle's right-hand side
+    launch_consistent(h);
+    launch_residual(h, 2);
+  }
+  if ((rc = launch_iteration(h, 2))) return rc;
   CK(cudaStreamSynchronize(h->stream));
   return BSAM_OK;
 }
@@ -1227,11 +1323,18 @@ int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles,
   if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
   int rc = set_device(h);
   if (rc) return rc;
+  if ((rc = ensure_f32(h))) return rc;
   for (int k = 1; k <= h->nlev; ++k) launch_fill(h, k);
   launch_residual(h, 0);
   CK(cudaGetLastError());
   int nactive = 0;
   if ((rc = read_state(h, &nactive))) return rc;
+  if (nactive && mixed(h)) {
+    // the history starts with the reference's own initial residual; the
+    // first correction's right-hand side is the consistent hierarchy's
+    launch_consistent(h);
+    launch_residual(h, 2);
+  }
   if (nactive && (rc = build_graph(h))) return rc;
   // every instance iterates until its own stop test fails; a converged
   // instance of a batch is frozen (its stores are predicated off) while the
@@ -1425,6 +1528,11 @@ int bsam_profile_vcycles(bsam_hier h, int ncycles, int level, double ms[BSAM_NKI
   int rc = set_device(h);
   if (rc) return rc;
   for (int i = 0; i < BSAM_NKINDS; ++i) { ms[i] = 0; launches[i] = 0; bytes[i] = 0; }
+  if ((rc = ensure_f32(h))) return rc;
+  if (mixed(h)) {
+    launch_consistent(h);
+    launch_residual(h, 2);
+  }
   h->profiling = true;
   h->profile_level = level;
   h->recs.clear();

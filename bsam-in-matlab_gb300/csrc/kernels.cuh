@@ -47,13 +47,23 @@ struct PatchD {
   int pad0, pad1;
 };
 
-struct Fields {
-  double *Q, *F, *QC;
-  const double *FTrue, *CC, *ID, *DeW, *DnS, *bcg, *cfd, *pcoef;
+// the arrays one V-cycle works on, in its value type T: the FP64 solve
+// (T = double) or the FP32 correction cycle of the mixed form (T = float:
+// Q is the correction, F its right-hand side, coefficients FP32 copies)
+template <class T>
+struct FieldsT {
+  T *Q, *F, *QC;
+  const double *FTrue;         // FP64 source (residual only)
+  const T *CC, *ID, *DeW, *DnS, *bcg, *cfd, *pcoef;
   const uint8_t *flags;        // bit0 covered by a finer level, bit1 correction target
   const int *win, *fp;         // window gathers, footprint scatters (2 ints/cell)
   const int *active;           // per instance: 1 while its V-cycles continue
 };
+using Fields = FieldsT<double>;
+
+// FP64 view of a value of either type (a no-op for double)
+template <class T>
+__device__ __forceinline__ double dbl(T x) { return (double)x; }
 
 // one level's work decomposition for one kind of item
 struct Decomp {
@@ -105,26 +115,28 @@ struct GhostItems {
   const int *inst;             // instance per item (batches only, else null)
 };
 
-__device__ __forceinline__ double eval_rule(const GhostItems &G, int i, const double *Q, const double *bcg, double hx,
-                                            double hy) {
-  constexpr double A1 = -1.0 / 5.0, A2 = 2.0 / 3.0, A3 = 8.0 / 15.0;
-  constexpr double B1 = 5.0 / 32.0, B2 = 15.0 / 16.0, B3 = -3.0 / 32.0;
+template <class T>
+__device__ __forceinline__ T eval_rule(const GhostItems &G, int i, const T *Q, const T *bcg, T hx, T hy) {
+  const T A1 = T(-1.0 / 5.0), A2 = T(2.0 / 3.0), A3 = T(8.0 / 15.0);
+  const T B1 = T(5.0 / 32.0), B2 = T(15.0 / 16.0), B3 = T(-3.0 / 32.0);
+  const T c23 = T(2.0 / 3.0), c13 = T(1.0 / 3.0), c83 = T(8.0 / 3.0);
   const int a = G.a[i];
   switch (G.type[i]) {
     case G_COPY: return Q[a];
     case G_QIF: return (A1 * Q[a] + A2 * Q[G.b[i]]) + A3 * Q[G.c[i]];
     case G_QIF_END:
       return (A1 * Q[a] + A2 * Q[G.b[i]]) + A3 * ((B1 * Q[G.c[i]] + B2 * Q[G.d[i]]) + B3 * Q[G.e[i]]);
-    case G_LIF: return ((2.0 / 3.0) * Q[G.c[i]] + (2.0 / 3.0) * Q[a]) - (1.0 / 3.0) * Q[G.b[i]];
-    case G_LIF_CORNER: return (2.0 / 3.0) * Q[G.c[i]] + (1.0 / 3.0) * Q[a];
-    case G_DIRICHLET: return ((8.0 / 3.0) * bcg[G.e[i]] - 2 * Q[a]) + (1.0 / 3.0) * Q[G.b[i]];
+    case G_LIF: return (c23 * Q[G.c[i]] + c23 * Q[a]) - c13 * Q[G.b[i]];
+    case G_LIF_CORNER: return c23 * Q[G.c[i]] + c13 * Q[a];
+    case G_DIRICHLET: return (c83 * bcg[G.e[i]] - 2 * Q[a]) + c13 * Q[G.b[i]];
     default: return Q[a] + (G.b[i] ? hy : hx) * bcg[G.e[i]];   // G_NEUMANN
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, double *__restrict__ Q,
-                                                  double *__restrict__ QC, const double *__restrict__ bcg,
-                                                  double hx, double hy, const int *__restrict__ active,
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, T *__restrict__ Q, T *__restrict__ QC,
+                                                  const T *__restrict__ bcg, double hx_, double hy_,
+                                                  const int *__restrict__ active,
                                                   const int *__restrict__ inst_nlev, int need) {
   chain_trigger();
   const int t = blockIdx.x * kBlock + threadIdx.x;
@@ -138,16 +150,17 @@ __global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, 
   // restriction from level `need` skips the instances without that level
   // (their own V-cycle starts below it)
   if (inst >= 0 && (!active[inst] || inst_nlev[inst] < need)) return;
+  const T hx = T(hx_), hy = T(hy_);
   if (ty == G_RING) {
     QC[dst] = Q[G.a[i]];
   } else if (ty == G_PHYS_CORNER) {
     // (face ghost 1 + face ghost 2) - interior, the face ghosts evaluated by
     // their own final rules (ebFillGhosts.m:84-89 reads them after stage 3)
-    const double v1 = eval_rule(G, G.a[i], Q, bcg, hx, hy);
-    const double v2 = eval_rule(G, G.b[i], Q, bcg, hx, hy);
+    const T v1 = eval_rule<T>(G, G.a[i], Q, bcg, hx, hy);
+    const T v2 = eval_rule<T>(G, G.b[i], Q, bcg, hx, hy);
     Q[dst] = (v1 + v2) - Q[G.c[i]];
   } else {
-    Q[dst] = eval_rule(G, i, Q, bcg, hx, hy);
+    Q[dst] = eval_rule<T>(G, i, Q, bcg, hx, hy);
   }
 }
 
@@ -179,21 +192,23 @@ struct Rule {                // one ghost rule, inline (perimeter table)
   int type, a, b, c, d, e;
 };
 
-__device__ __forceinline__ double eval_inline(const Rule &R, const double *Q) {
-  constexpr double A1 = -1.0 / 5.0, A2 = 2.0 / 3.0, A3 = 8.0 / 15.0;
-  constexpr double B1 = 5.0 / 32.0, B2 = 15.0 / 16.0, B3 = -3.0 / 32.0;
+template <class T>
+__device__ __forceinline__ T eval_inline(const Rule &R, const T *Q) {
+  const T A1 = T(-1.0 / 5.0), A2 = T(2.0 / 3.0), A3 = T(8.0 / 15.0);
+  const T B1 = T(5.0 / 32.0), B2 = T(15.0 / 16.0), B3 = T(-3.0 / 32.0);
+  const T c23 = T(2.0 / 3.0), c13 = T(1.0 / 3.0);
   switch (R.type) {
     case G_COPY: return Q[R.a];
     case G_QIF: return (A1 * Q[R.a] + A2 * Q[R.b]) + A3 * Q[R.c];
     case G_QIF_END: return (A1 * Q[R.a] + A2 * Q[R.b]) + A3 * ((B1 * Q[R.c] + B2 * Q[R.d]) + B3 * Q[R.e]);
-    default: return ((2.0 / 3.0) * Q[R.c] + (2.0 / 3.0) * Q[R.a]) - (1.0 / 3.0) * Q[R.b];   // G_LIF
+    default: return (c23 * Q[R.c] + c23 * Q[R.a]) - c13 * Q[R.b];   // G_LIF
   }
 }
 
-template <bool kPow2>
-__global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__restrict__ chunks, int nchunks, Fields f,
-                                                  const Rule *__restrict__ perim, int m, double omega, int unit_omega,
-                                                  int fresh) {
+template <class T, bool kPow2>
+__global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__restrict__ chunks, int nchunks,
+                                                  FieldsT<T> f, const Rule *__restrict__ perim, int m, double omega_,
+                                                  int unit_omega, int fresh) {
   chain_trigger();
   const int ch = blockIdx.x * (kBlock / kChunk) + threadIdx.x / kChunk;
   bool ok = ch < nchunks;
@@ -212,16 +227,16 @@ __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__
   const int c = (li + 1) + (lj + 1) * ldq;
   const int cc = R.c_off + li + lj * mx;
   // static operands: coefficients, diagonal, boundary data, ghost rules
-  const double *__restrict__ DeW = f.DeW + R.dew_off;
-  const double *__restrict__ DnS = f.DnS + R.dns_off;
-  const double dE = __ldg(DeW + (li + 1) + lj * (mx + 1)), dW = __ldg(DeW + li + lj * (mx + 1));
-  const double dN = __ldg(DnS + li + (lj + 1) * mx), dS = __ldg(DnS + li + lj * mx);
-  const double idg = __ldg(f.ID + cc);
-  const double *__restrict__ g4 = f.bcg + R.bcg_off;
+  const T *__restrict__ DeW = f.DeW + R.dew_off;
+  const T *__restrict__ DnS = f.DnS + R.dns_off;
+  const T dE = __ldg(DeW + (li + 1) + lj * (mx + 1)), dW = __ldg(DeW + li + lj * (mx + 1));
+  const T dN = __ldg(DnS + li + (lj + 1) * mx), dS = __ldg(DnS + li + lj * mx);
+  const T idg = __ldg(f.ID + cc);
+  const T *__restrict__ g4 = f.bcg + R.bcg_off;
   // a cell touches at most one x side (W or E) and one y side (S or N):
   // kind 0 interior neighbour, 1 Dirichlet, 2 Neumann, 3 ghost rule
   int kx = 0, ky = 0, sx = 0, sy = 0;       // sx: 0 west 1 east; sy: 0 south 1 north
-  double gx = 0, gy = 0;
+  T gx = 0, gy = 0;
   Rule rx, ry;
   if (li == 0 || li == mx - 1) {
     sx = (li == 0) ? 0 : 1;
@@ -237,29 +252,32 @@ __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__
   }
   chain_wait();
   const int act = f.active[R.inst];   // a converged instance of a batch stays frozen
-  double *__restrict__ Q = f.Q + R.q_off;
-  double qe = Q[c + 1], qw = Q[c - 1], qn = Q[c + ldq], qs = Q[c - ldq];
+  const T c83 = T(8.0 / 3.0), c13 = T(1.0 / 3.0);
+  T *__restrict__ Q = f.Q + R.q_off;
+  T qe = Q[c + 1], qw = Q[c - 1], qn = Q[c + ldq], qs = Q[c - ldq];
   if (kx > 0) {
-    double v;
-    if (kx == 1) v = (8.0 / 3.0) * gx + (1.0 / 3.0) * Q[sx ? c - 1 : c + 1];
-    else if (kx == 2) v = L.hx * gx;
-    else v = eval_inline(rx, f.Q);
+    T v;
+    if (kx == 1) v = c83 * gx + c13 * Q[sx ? c - 1 : c + 1];
+    else if (kx == 2) v = T(L.hx) * gx;
+    else v = eval_inline<T>(rx, f.Q);
     if (sx) qe = v; else qw = v;
   }
   if (ky > 0) {
-    double v;
-    if (ky == 1) v = (8.0 / 3.0) * gy + (1.0 / 3.0) * Q[sy ? c - ldq : c + ldq];
-    else if (ky == 2) v = L.hy * gy;
-    else v = eval_inline(ry, f.Q);
+    T v;
+    if (ky == 1) v = c83 * gy + c13 * Q[sy ? c - ldq : c + ldq];
+    else if (ky == 2) v = T(L.hy) * gy;
+    else v = eval_inline<T>(ry, f.Q);
     if (sy) qn = v; else qs = v;
   }
-  double t = f.F[cc];
-  t = t + divh<kPow2>(qe * dE, L.hx2, L.ihx2);
-  t = t + divh<kPow2>(qw * dW, L.hx2, L.ihx2);
-  t = t + divh<kPow2>(qn * dN, L.hy2, L.ihy2);
-  t = t + divh<kPow2>(qs * dS, L.hy2, L.ihy2);
+  const T hx2 = T(L.hx2), ihx2 = T(L.ihx2), hy2 = T(L.hy2), ihy2 = T(L.ihy2);
+  T t = f.F[cc];
+  t = t + divh<kPow2>(qe * dE, hx2, ihx2);
+  t = t + divh<kPow2>(qw * dW, hx2, ihx2);
+  t = t + divh<kPow2>(qn * dN, hy2, ihy2);
+  t = t + divh<kPow2>(qs * dS, hy2, ihy2);
   t = t * idg;
   if (!act) return;
+  const T omega = T(omega_);
   if (unit_omega) Q[c] = t;
   else Q[c] = omega * t + (1 - omega) * Q[c];
 }
@@ -268,12 +286,14 @@ __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__
 // restrict2 (ebKernels.m:98-102) of each patch interior into its QC interior
 // and, for 'restrict' (ebTransfer.m:10-33), into the parent's Q over the
 // footprint.  One thread per coarse cell.
-__device__ __forceinline__ double restrict_cell(const double *Q, int ldq, int ci, int cj) {
+template <class T>
+__device__ __forceinline__ T restrict_cell(const T *Q, int ldq, int ci, int cj) {
   const int c = (2 * ci + 1) + (2 * cj + 1) * ldq;
-  return 0.25 * (((Q[c] + Q[c + 1]) + Q[c + ldq]) + Q[c + ldq + 1]);
+  return T(0.25) * (((Q[c] + Q[c + 1]) + Q[c + ldq]) + Q[c + ldq + 1]);
 }
 
-__global__ void __launch_bounds__(kBlock) k_restrict(LevelD L, Decomp D, Fields f, int to_parent) {
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_restrict(LevelD L, Decomp D, FieldsT<T> f, int to_parent) {
   chain_trigger();
   const int g = blockIdx.x * kBlock + threadIdx.x;
   if (g >= D.n) {
@@ -289,7 +309,7 @@ __global__ void __launch_bounds__(kBlock) k_restrict(LevelD L, Decomp D, Fields 
   const int inst = P.inst;
   chain_wait();
   if (!f.active[inst]) return;
-  const double R = restrict_cell(f.Q + q_off, ldq, ci, cj);
+  const T R = restrict_cell<T>(f.Q + q_off, ldq, ci, cj);
   f.QC[qc_off + (ci + 1) + (cj + 1) * (cmx + 2)] = R;
   if (to_parent) f.Q[dst] = R;
 }
@@ -300,47 +320,52 @@ __global__ void __launch_bounds__(kBlock) k_restrict(LevelD L, Decomp D, Fields 
 // parent's Q through the window table, the inner cell from QC's interior
 // (`qc_inner` false) or recomputed as the restriction of its four fine cells
 // (`qc_inner` true: the residual's refresh, ebCompResidual.m:32-38).
-__device__ __forceinline__ double face_corr(const PatchD &P, const Fields &f, int fc, int j, double hc2, double ihc2,
-                                            int pow2, bool qc_inner) {
+// The arithmetic is FP64 for either value type (the reflux of the mixed
+// form stays FP64).
+template <class T>
+__device__ __forceinline__ double face_corr(const PatchD &P, const FieldsT<T> &f, int fc, int j, double hc2,
+                                            double ihc2, int pow2, bool qc_inner) {
   const int mx = P.mx, my = P.my, cmx = mx >> 1, cmy = my >> 1;
   const int ldq = mx + 2, ldc = cmx + 2;
-  const double *Q = f.Q + P.q_off, *QC = f.QC + P.qc_off;
+  const T *Q = f.Q + P.q_off, *QC = f.QC + P.qc_off;
   const int *win = f.win + P.win_off;
-  const double *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off, *cfd = f.cfd + P.cfd_off;
+  const T *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off, *cfd = f.cfd + P.cfd_off;
+  auto q = [&](int i) { return dbl(Q[i]); };
   double v;
   switch (fc) {
     case 0: {
       const int r1 = 2 * j + 1, r2 = 2 * j + 2;
-      const double out = f.Q[win[(j + 1) * ldc]];
-      const double in = qc_inner ? restrict_cell(Q, ldq, 0, j) : QC[1 + (j + 1) * ldc];
-      v = (DeW[(2 * j) * (mx + 1)] * (Q[1 + r1 * ldq] - Q[r1 * ldq]) +
-           DeW[(2 * j + 1) * (mx + 1)] * (Q[1 + r2 * ldq] - Q[r2 * ldq])) +
-          cfd[j] * (out - in);
+      const double out = dbl(f.Q[win[(j + 1) * ldc]]);
+      const double in = dbl(qc_inner ? restrict_cell<T>(Q, ldq, 0, j) : QC[1 + (j + 1) * ldc]);
+      v = (dbl(DeW[(2 * j) * (mx + 1)]) * (q(1 + r1 * ldq) - q(r1 * ldq)) +
+           dbl(DeW[(2 * j + 1) * (mx + 1)]) * (q(1 + r2 * ldq) - q(r2 * ldq))) +
+          dbl(cfd[j]) * (out - in);
       break;
     }
     case 1: {
       const int r1 = 2 * j + 1, r2 = 2 * j + 2;
-      const double out = f.Q[win[cmx + 1 + (j + 1) * ldc]];
-      const double in = qc_inner ? restrict_cell(Q, ldq, cmx - 1, j) : QC[cmx + (j + 1) * ldc];
-      v = (DeW[mx + (2 * j) * (mx + 1)] * (Q[mx + r1 * ldq] - Q[mx + 1 + r1 * ldq]) +
-           DeW[mx + (2 * j + 1) * (mx + 1)] * (Q[mx + r2 * ldq] - Q[mx + 1 + r2 * ldq])) +
-          cfd[cmy + j] * (out - in);
+      const double out = dbl(f.Q[win[cmx + 1 + (j + 1) * ldc]]);
+      const double in = dbl(qc_inner ? restrict_cell<T>(Q, ldq, cmx - 1, j) : QC[cmx + (j + 1) * ldc]);
+      v = (dbl(DeW[mx + (2 * j) * (mx + 1)]) * (q(mx + r1 * ldq) - q(mx + 1 + r1 * ldq)) +
+           dbl(DeW[mx + (2 * j + 1) * (mx + 1)]) * (q(mx + r2 * ldq) - q(mx + 1 + r2 * ldq))) +
+          dbl(cfd[cmy + j]) * (out - in);
       break;
     }
     case 2: {
       const int c1 = 2 * j + 1, c2 = 2 * j + 2;
-      const double out = f.Q[win[j + 1]];
-      const double in = qc_inner ? restrict_cell(Q, ldq, j, 0) : QC[j + 1 + ldc];
-      v = (DnS[2 * j] * (Q[c1 + ldq] - Q[c1]) + DnS[2 * j + 1] * (Q[c2 + ldq] - Q[c2])) + cfd[2 * cmy + j] * (out - in);
+      const double out = dbl(f.Q[win[j + 1]]);
+      const double in = dbl(qc_inner ? restrict_cell<T>(Q, ldq, j, 0) : QC[j + 1 + ldc]);
+      v = (dbl(DnS[2 * j]) * (q(c1 + ldq) - q(c1)) + dbl(DnS[2 * j + 1]) * (q(c2 + ldq) - q(c2))) +
+          dbl(cfd[2 * cmy + j]) * (out - in);
       break;
     }
     default: {
       const int c1 = 2 * j + 1, c2 = 2 * j + 2;
-      const double out = f.Q[win[j + 1 + (cmy + 1) * ldc]];
-      const double in = qc_inner ? restrict_cell(Q, ldq, j, cmy - 1) : QC[j + 1 + cmy * ldc];
-      v = (DnS[2 * j + my * mx] * (Q[c1 + my * ldq] - Q[c1 + (my + 1) * ldq]) +
-           DnS[2 * j + 1 + my * mx] * (Q[c2 + my * ldq] - Q[c2 + (my + 1) * ldq])) +
-          cfd[2 * cmy + cmx + j] * (out - in);
+      const double out = dbl(f.Q[win[j + 1 + (cmy + 1) * ldc]]);
+      const double in = dbl(qc_inner ? restrict_cell<T>(Q, ldq, j, cmy - 1) : QC[j + 1 + cmy * ldc]);
+      v = (dbl(DnS[2 * j + my * mx]) * (q(c1 + my * ldq) - q(c1 + (my + 1) * ldq)) +
+           dbl(DnS[2 * j + 1 + my * mx]) * (q(c2 + my * ldq) - q(c2 + (my + 1) * ldq))) +
+          dbl(cfd[2 * cmy + cmx + j]) * (out - in);
       break;
     }
   }
@@ -353,8 +378,9 @@ struct CorrCSR {
   const int *cell, *patch, *beg, *item, *jj;   // item = (level-local fine patch << 2) | face
 };
 
+template <class T>
 __device__ __forceinline__ double add_corrections(double v, const CorrCSR &C, int t, const LevelD &Lf, const LevelD &Lc,
-                                                  const Fields &f, bool qc_inner) {
+                                                  const FieldsT<T> &f, bool qc_inner) {
   for (int i = C.beg[t]; i < C.beg[t + 1]; ++i) {
     const int it = C.item[i];
     const int fc = it & 3;
@@ -383,7 +409,8 @@ __device__ __forceinline__ double op_pre(double q, double qe, double qw, double 
   return (divr(-(feE - feW), L.hx2, L.ihx2, L.pow2) - divr(fnN - fnS, L.hy2, L.ihy2, L.pow2)) + cc * q;
 }
 
-__global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, Fields f, const int *__restrict__ ring,
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, FieldsT<T> f, const int *__restrict__ ring,
                                                  const int *__restrict__ ring_inst, int ring_off, int n_ring, CorrCSR C,
                                                  int n_tgt) {
   chain_trigger();
@@ -416,16 +443,16 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
     const int q_off = P.q_off, c_off = P.c_off, qc_off = P.qc_off;
     // static operands of the four fine cells (restrict2 order) and of the
     // coarse operator
-    const double *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off, *CC = f.CC + c_off;
+    const T *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off, *CC = f.CC + c_off;
     double dE[4], dW[4], dN[4], dS[4], cf[4];
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int li = 2 * ci + (t & 1), lj = 2 * cj + (t >> 1);
-      dE[t] = __ldg(DeW + (li + 1) + lj * (mx + 1));
-      dW[t] = __ldg(DeW + li + lj * (mx + 1));
-      dN[t] = __ldg(DnS + li + (lj + 1) * mx);
-      dS[t] = __ldg(DnS + li + lj * mx);
-      cf[t] = __ldg(CC + li + lj * mx);
+      dE[t] = dbl(__ldg(DeW + (li + 1) + lj * (mx + 1)));
+      dW[t] = dbl(__ldg(DeW + li + lj * (mx + 1)));
+      dN[t] = dbl(__ldg(DnS + li + (lj + 1) * mx));
+      dS[t] = dbl(__ldg(DnS + li + lj * mx));
+      cf[t] = dbl(__ldg(CC + li + lj * mx));
     }
     const int ldc = cmx + 2;
     const int *win = f.win + P.win_off;
@@ -435,35 +462,35 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
     const int sw = (ci == 0) ? __ldg(win + w - 1) : -1;
     const int sn = (cj == cmy - 1) ? __ldg(win + w + ldc) : -1;
     const int ss = (cj == 0) ? __ldg(win + w - ldc) : -1;
-    const double *PDeW = f.pcoef + P.pc_off;
-    const double *PDnS = PDeW + (cmx + 1) * cmy;
-    const double *PCC = PDnS + cmx * (cmy + 1);
-    const double pE = __ldg(PDeW + (ci + 1) + cj * (cmx + 1)), pW = __ldg(PDeW + ci + cj * (cmx + 1));
-    const double pN = __ldg(PDnS + ci + (cj + 1) * cmx), pS = __ldg(PDnS + ci + cj * cmx);
-    const double pC = __ldg(PCC + s);
+    const T *PDeW = f.pcoef + P.pc_off;
+    const T *PDnS = PDeW + (cmx + 1) * cmy;
+    const T *PCC = PDnS + cmx * (cmy + 1);
+    const double pE = dbl(__ldg(PDeW + (ci + 1) + cj * (cmx + 1))), pW = dbl(__ldg(PDeW + ci + cj * (cmx + 1)));
+    const double pN = dbl(__ldg(PDnS + ci + (cj + 1) * cmx)), pS = dbl(__ldg(PDnS + ci + cj * cmx));
+    const double pC = dbl(__ldg(PCC + s));
     const int dst = __ldg(f.fp + 2 * (P.fp_off + s) + 1);
     const int inst = P.inst;
     chain_wait();
     if (!f.active[inst]) return;
-    const double *Qp = f.Q + q_off;
-    const double *Fp = f.F + c_off;
+    const T *Qp = f.Q + q_off;
+    const T *Fp = f.F + c_off;
     double rf[4];
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int li = 2 * ci + (t & 1), lj = 2 * cj + (t >> 1);
       const int c = (li + 1) + (lj + 1) * ldq;
-      rf[t] = Fp[li + lj * mx] - op_pre(Qp[c], Qp[c + 1], Qp[c - 1], Qp[c + ldq], Qp[c - ldq], dE[t], dW[t], dN[t],
-                                        dS[t], cf[t], L);
+      rf[t] = dbl(Fp[li + lj * mx]) - op_pre(dbl(Qp[c]), dbl(Qp[c + 1]), dbl(Qp[c - 1]), dbl(Qp[c + ldq]),
+                                             dbl(Qp[c - ldq]), dE[t], dW[t], dN[t], dS[t], cf[t], L);
     }
     const double rr = 0.25 * (((rf[0] + rf[1]) + rf[2]) + rf[3]);
-    const double *QC = f.QC + qc_off;
-    const double q = QC[w];
-    const double qe = se >= 0 ? f.Q[se] : QC[w + 1];
-    const double qw = sw >= 0 ? f.Q[sw] : QC[w - 1];
-    const double qn = sn >= 0 ? f.Q[sn] : QC[w + ldc];
-    const double qs = ss >= 0 ? f.Q[ss] : QC[w - ldc];
+    const T *QC = f.QC + qc_off;
+    const double q = dbl(QC[w]);
+    const double qe = dbl(se >= 0 ? f.Q[se] : QC[w + 1]);
+    const double qw = dbl(sw >= 0 ? f.Q[sw] : QC[w - 1]);
+    const double qn = dbl(sn >= 0 ? f.Q[sn] : QC[w + ldc]);
+    const double qs = dbl(ss >= 0 ? f.Q[ss] : QC[w - ldc]);
     const double lc = op_pre(q, qe, qw, qn, qs, pE, pW, pN, pS, pC, Lc);
-    f.F[dst] = rr + lc;
+    f.F[dst] = T(rr + lc);
     return;
   }
   b -= D.nblocks;
@@ -472,7 +499,7 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
   const int inst = t < n_tgt ? Lc.patches[C.patch[t]].inst : 0;
   chain_wait();
   if (t >= n_tgt || !f.active[inst]) return;
-  f.F[cell] = add_corrections(f.F[cell], C, t, L, Lc, f, false);
+  f.F[cell] = T(add_corrections<T>(dbl(f.F[cell]), C, t, L, Lc, f, false));
 }
 
 // ---------------------------------------------------------------------------
@@ -480,7 +507,8 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
 // (ebTransfer.m:57-71) adds P(W - QC) to the interior; mode 0 writes P(W)
 // (new-level initial guess, ebAddLevel.m:26-31).  One thread per coarse cell
 // writes its four fine cells.
-__global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, Fields f, int correct) {
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, FieldsT<T> f, int correct) {
   chain_trigger();
   const int g = blockIdx.x * kBlock + threadIdx.x;
   if (g >= D.n) {
@@ -502,22 +530,22 @@ __global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, Fields f
   const int qc_off = P.qc_off, q_off = P.q_off, ldq = P.mx + 2, inst = P.inst;
   chain_wait();
   const int act = f.active[inst];
-  const double *QC = f.QC + qc_off;
-  double E[3][3];
+  const T *QC = f.QC + qc_off;
+  T E[3][3];
 #pragma unroll
   for (int dj = 0; dj < 3; ++dj)
 #pragma unroll
     for (int di = 0; di < 3; ++di) {
       const int w = (a + di) + (b + dj) * ldw;
-      const double wv = f.Q[src[dj][di]];
+      const T wv = f.Q[src[dj][di]];
       E[dj][di] = correct ? wv - QC[w] : wv;
     }
-  const double C = E[1][1], Wm = E[1][0], Wp = E[1][2], Sm = E[0][1], Sp = E[2][1];
-  const double f11 = (((9 * C + 3 * Wm) + 3 * Sm) + E[0][0]) / 16;
-  const double f21 = (((9 * C + 3 * Wp) + 3 * Sm) + E[0][2]) / 16;
-  const double f12 = (((9 * C + 3 * Wm) + 3 * Sp) + E[2][0]) / 16;
-  const double f22 = (((9 * C + 3 * Wp) + 3 * Sp) + E[2][2]) / 16;
-  double *Q = f.Q + q_off;
+  const T C = E[1][1], Wm = E[1][0], Wp = E[1][2], Sm = E[0][1], Sp = E[2][1];
+  const T f11 = (((9 * C + 3 * Wm) + 3 * Sm) + E[0][0]) / 16;
+  const T f21 = (((9 * C + 3 * Wp) + 3 * Sm) + E[0][2]) / 16;
+  const T f12 = (((9 * C + 3 * Wm) + 3 * Sp) + E[2][0]) / 16;
+  const T f22 = (((9 * C + 3 * Wp) + 3 * Sp) + E[2][2]) / 16;
+  T *Q = f.Q + q_off;
   const int c = (2 * a + 1) + (2 * b + 1) * ldq;
   if (correct) {
     if (!act) return;
@@ -541,8 +569,11 @@ struct CoarsestD {
   long long ainv_off, rhs_off;
 };
 
+// bcRhs null: a homogeneous problem (the correction cycle of the mixed
+// form), whose F is FP32 while the solve itself stays FP64.
+template <class T>
 __global__ void __launch_bounds__(kBlock) k_coarsest(const double *__restrict__ Ainv, const double *__restrict__ bcRhs,
-                                                     const CoarsestD *__restrict__ cd, Fields f) {
+                                                     const CoarsestD *__restrict__ cd, FieldsT<T> f) {
   chain_trigger();
   const CoarsestD D = cd[blockIdx.y];
   const int N = D.N;
@@ -553,25 +584,25 @@ __global__ void __launch_bounds__(kBlock) k_coarsest(const double *__restrict__ 
     return;
   }
   const double *a = Ainv + D.ainv_off + (size_t)row * N;
-  const double *rhs = bcRhs + D.rhs_off;
+  const double *rhs = bcRhs ? bcRhs + D.rhs_off : nullptr;
   constexpr int kPre = 8;   // inverse entries held in registers (N <= 256)
   double av[kPre], bv[kPre];
 #pragma unroll
   for (int i = 0; i < kPre; ++i) {
     const int c = lane + 32 * i;
     av[i] = c < N ? __ldg(a + c) : 0.0;
-    bv[i] = c < N ? __ldg(rhs + c) : 0.0;
+    bv[i] = (c < N && rhs) ? __ldg(rhs + c) : 0.0;
   }
   chain_wait();
   const int act = f.active[D.inst];
-  const double *F = f.F + D.c_off;
+  const T *F = f.F + D.c_off;
   double s = 0.0;
 #pragma unroll
   for (int i = 0; i < kPre; ++i) {
     const int c = lane + 32 * i;
-    if (c < N) s = s + av[i] * (F[c] + bv[i]);
+    if (c < N) s = s + av[i] * (dbl(F[c]) + bv[i]);
   }
-  for (int c = lane + 32 * kPre; c < N; c += 32) s = s + a[c] * (F[c] + rhs[c]);
+  for (int c = lane + 32 * kPre; c < N; c += 32) s = s + a[c] * (dbl(F[c]) + (rhs ? rhs[c] : 0.0));
 #pragma unroll
   for (int off = 16; off >= 1; off >>= 1) {
     const double o = __shfl_down_sync(0xffffffffu, s, off);
@@ -579,7 +610,7 @@ __global__ void __launch_bounds__(kBlock) k_coarsest(const double *__restrict__ 
   }
   if (lane == 0 && act) {
     const int i = row % D.n1, j = row / D.n1;
-    f.Q[D.q_off + (i + 1) + (j + 1) * (D.n1 + 2)] = s;
+    f.Q[D.q_off + (i + 1) + (j + 1) * (D.n1 + 2)] = T(s);
   }
 }
 
@@ -614,7 +645,7 @@ struct LevelX {
 __global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ X, const PatchD *__restrict__ patches,
                                                      const ResTask *__restrict__ tasks, int ntask, Fields f,
                                                      const int *__restrict__ ring, double *slots, int nslots,
-                                                     int mass_corr) {
+                                                     int mass_corr, float *__restrict__ rout) {
   chain_trigger();
   const int w = blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -643,7 +674,7 @@ __global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ 
   const LevelX &Xk = X[T.level];
   if (T.kind == 0) {
     bool on = false;
-    int c = 0, ldq = 0, q_off = 0;
+    int c = 0, ldq = 0, q_off = 0, cc_out = 0;
     double ft = 0, dE = 0, dW = 0, dN = 0, dS = 0, cf = 0;
     if (have) {
       const PatchD &P = patches[T.a];
@@ -664,6 +695,7 @@ __global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ 
         ldq = mx + 2;
         q_off = P.q_off;
         c = (lx + 1) + (lj + 1) * ldq;
+        cc_out = cc;
       }
     }
     chain_wait();
@@ -673,6 +705,7 @@ __global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ 
       li = fabs(r);
       sq = r * r;
       fn = fabs(ft);
+      if (rout) rout[cc_out] = (float)r;
     }
   } else {   // kind 1: targets of this level, corrections from the level above
     chain_wait();
@@ -687,6 +720,7 @@ __global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ 
       double r = ft - op_cell_r(f.Q + Pc.q_off, Pc.mx + 2, f.DeW + Pc.dew_off, f.DnS + Pc.dns_off, f.CC[cell], Pc.mx,
                                 lx, lj, Xk.L);
       r = add_corrections(r, Xf.C, g, Xf.L, Xk.L, f, true);
+      if (rout) rout[cell] = (float)r;
       if (!(f.flags[cell] & 1)) {
         li = fabs(r);
         sq = r * r;
@@ -808,6 +842,34 @@ __global__ void __launch_bounds__(kBlock) k_freset(Decomp D, const PatchD *__res
   const int inst = P.inst;
   chain_wait();
   if (f.active[inst]) f.F[cc] = v;
+}
+
+// ---------------------------------------------------------------------------
+// Defect correction of the mixed form: Q += E (FP64 += FP32) on the interior
+// cells of every patch of the active instances.
+__global__ void __launch_bounds__(kBlock) k_update(Decomp D, const PatchD *__restrict__ patches, double *Q,
+                                                   const float *__restrict__ E, const int *__restrict__ active) {
+  chain_trigger();
+  const int g = blockIdx.x * kBlock + threadIdx.x;
+  if (g >= D.n) {
+    chain_wait();
+    return;
+  }
+  const int p = find_patch(D, blockIdx.x, g);
+  const PatchD &P = patches[p];
+  const int s = g - __ldg(D.beg + p);
+  const int lj = s / P.mx, lx = s - lj * P.mx;
+  const int qi = P.q_off + (lx + 1) + (lj + 1) * (P.mx + 2);
+  const int inst = P.inst;
+  chain_wait();
+  if (active[inst]) Q[qi] = Q[qi] + (double)E[qi];
+}
+
+// FP32 copy of an FP64 array (coefficient copies of the mixed form)
+__global__ void __launch_bounds__(kBlock) k_to_f32(const double *__restrict__ a, float *__restrict__ b, long long n) {
+  chain_in();
+  for (long long i = blockIdx.x * (long long)kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock)
+    b[i] = (float)a[i];
 }
 
 // ---------------------------------------------------------------------------

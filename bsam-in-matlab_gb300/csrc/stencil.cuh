@@ -9,8 +9,8 @@ constexpr int kBlock = 256;
 
 // x / h2: a true division, or a multiplication by the exact reciprocal when
 // h2 is a power of two (then both round identically)
-template <bool kPow2>
-__device__ __forceinline__ double divh(double x, double h2, double ih2) {
+template <bool kPow2, class T>
+__device__ __forceinline__ T divh(T x, T h2, T ih2) {
   return kPow2 ? x * ih2 : x / h2;
 }
 
