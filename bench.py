@@ -21,6 +21,17 @@ composite residual 1e-10 (10 cycles).
   cpu_baseline  the C oracle (a restatement of the reference's MATLAB path)
           on the host cores, a bounded sample of whole solves.
 
+  forms   beside the plain FP64 path (same JSON line, key "forms"):
+          mixed   the starfish solve in the mixed-precision form (FP32
+                  correction V-cycles inside FP64 defect correction, same FP64
+                  stop test), with its relative L2 / max difference from the
+                  FP64 solution;
+          batched 256 seeded random elliptic instances (BaseCells {32,64,128},
+                  MaxLevels {2,3,4}, TagThreshold 1e-2), the last ebSolve stage
+                  of each: solved one after another on the plain path, then as
+                  one batch in FP64 (checked bit for bit against the solo
+                  solves) and in the mixed form.
+
 `--impl reference` times the reference's CPU path instead: MATLAB is not
 available, so the C oracle restatement runs on all host cores.
 With several ranks (torchrun) every rank solves its own replica; the
@@ -177,6 +188,119 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def time_device_solves(dh, opts, steps, warmup, stream, flush):
+    """Per-solve device times (CUDA events on the library stream, L2
+    flushed before each solve, state restored on the device)."""
+    import torch
+    dh.save_state()
+    for _ in range(warmup):
+        dh.restore_state()
+        r = dh.solve_cycles(opts.MaxVCycles + 2)
+    ms = []
+    for _ in range(steps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            a.record(stream)
+        dh.restore_state()
+        r = dh.solve_cycles(opts.MaxVCycles + 2)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    return np.array(ms), r
+
+
+def mixed_form(backend, fl, opts, ref_Q, steps, warmup, flush, local):
+    """Precision form on the starfish hierarchy: FP32 correction cycles in
+    an FP64 defect-correction loop, to the same FP64 stop test."""
+    import torch
+    from bsam.device import DevHier, BSAM_FIELD_Q
+    from bsam.flat import visible_q_index, rel_errors
+    om = opts.copy()
+    om['Precision'] = 'mixed'
+    dh = DevHier(backend.ctx, fl, om)
+    stream = torch.cuda.ExternalStream(dh.stream(), device=torch.device('cuda', local))
+    ms, r = time_device_solves(dh, om, steps, warmup, stream, flush)
+    l2, mx = rel_errors(dh.get(BSAM_FIELD_Q, fl.Q.size), ref_Q, visible_q_index(fl))
+    return {'value': steps / (ms.sum() / 1e3), 'unit': 'solves/s', 'ms_per_solve': float(ms.mean()),
+            'p50_ms': float(np.percentile(ms, 50)), 'p99_ms': float(np.percentile(ms, 99)),
+            'vcycles': r[0], 'final_rel': r[2], 'rel_l2_vs_fp64': l2, 'rel_max_vs_fp64': mx,
+            'dtype': 'f32 smoothing / f64 defect correction',
+            'note': 'error against the FP64 path, which equals the C oracle bit for bit'}
+
+
+def batched_form(backend, n, steps, warmup, flush, local):
+    """Batching form: n seeded random elliptic instances (BaseCells
+    {32,64,128}, MaxLevels {2,3,4}, TagThreshold 1e-2), each taken through
+    ebSolve's solution-driven pipeline to its last stage; that last solve of
+    every instance runs (a) alone, one after another (the plain FP64 path),
+    (b) as one batch in FP64, (c) as one batch in the mixed form."""
+    import torch
+    import warnings
+    from bsam.device import DevHier, BSAM_FIELD_Q
+    from bsam.instances import random_elliptic, final_stage
+    from bsam.batch import merge_flats, split_field
+    from bsam.flat import FIELD_Q, visible_q_index, rel_errors
+    t0 = time.perf_counter()
+    parts, opts = [], None
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        for s in range(n):
+            prob, o = random_elliptic(1000 + s)
+            fl, H = final_stage(prob, o, backend)
+            parts.append(fl)
+            opts = opts or H.opts
+    setup_s = time.perf_counter() - t0
+    dev = torch.device('cuda', local)
+    # (a) solo, plain FP64
+    solo_ms, solo = [], []
+    for p in parts:
+        dh = DevHier(backend.ctx, p, opts)
+        st = torch.cuda.ExternalStream(dh.stream(), device=dev)
+        ms, r = time_device_solves(dh, opts, 1, 1, st, flush)
+        solo_ms.append(float(ms[0]))
+        solo.append((r, dh.get(BSAM_FIELD_Q, p.Q.size)))
+        del dh
+    solo_total = sum(solo_ms)
+    out = {'workload': f'{n} seeded random elliptic instances on [0,1]^2 (log D: 16 Fourier modes, C in [0,1], '
+                       f'f: 4 Gaussian bumps; BaseCells {{32,64,128}}, MaxLevels {{2,3,4}}, TagThreshold 1e-2), '
+                       f'last ebSolve stage of each, RelTol 1e-10',
+           'instances': n, 'stored_cells': int(sum(p.F.size for p in parts)), 'setup_s': setup_s,
+           'solo_fp64': {'value': n / (solo_total / 1e3), 'unit': 'solves/s', 'ms_total': solo_total,
+                         'p50_ms': float(np.percentile(solo_ms, 50)), 'p99_ms': float(np.percentile(solo_ms, 99))}}
+    b = merge_flats(parts)
+    for prec in ('fp64', 'mixed'):
+        ob = opts.copy()
+        ob['Precision'] = prec
+        bh = DevHier(backend.ctx, b, ob)
+        st = torch.cuda.ExternalStream(bh.stream(), device=dev)
+        ms, _ = time_device_solves(bh, ob, steps, warmup, st, flush)
+        Q = bh.get(BSAM_FIELD_Q, b.Q.size)
+        equal, worst_l2, worst_max, maxit = True, 0.0, 0.0, 0
+        for i, (r, q) in enumerate(solo):
+            rb = bh.batch_result(i, ob.MaxVCycles + 2)
+            maxit = max(maxit, rb[0])
+            qi = split_field(b, FIELD_Q, Q, i)
+            if prec == 'fp64':
+                equal &= rb[0] == r[0] and np.array_equal(rb[1], r[1]) and np.array_equal(qi, q)
+            else:
+                l2, mx = rel_errors(qi, q, visible_q_index(parts[i]))
+                worst_l2, worst_max = max(worst_l2, l2), max(worst_max, mx)
+        d = {'value': n * steps / (ms.sum() / 1e3), 'unit': 'solves/s', 'ms_per_batch': float(ms.mean()),
+             'p50_ms': float(np.percentile(ms, 50)), 'p99_ms': float(np.percentile(ms, 99)),
+             'vcycles_slowest': maxit, 'kernels_per_vcycle': bh.kernels_per_vcycle()}
+        if prec == 'fp64':
+            d['equal_to_solo_bitwise'] = bool(equal)
+        else:
+            d['worst_rel_l2_vs_fp64'] = worst_l2
+            d['worst_rel_max_vs_fp64'] = worst_max
+        out['batch_' + prec] = d
+        del bh
+    out['speedup_batch_mixed_vs_solo_fp64'] = out['batch_mixed']['value'] / out['solo_fp64']['value']
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -184,6 +308,8 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='native', choices=['native', 'reference'])
     ap.add_argument('--cpu-budget', type=float, default=15.0)
+    ap.add_argument('--batch', type=int, default=256, help='instances of the batching form (0: skip)')
+    ap.add_argument('--no-forms', action='store_true', help='skip the mixed and batching forms')
     args = ap.parse_args()
     rank = int(os.environ.get('RANK', 0))
     world = int(os.environ.get('WORLD_SIZE', 1))
@@ -280,6 +406,17 @@ def main():
     achieved_all = ra['bytes'] / (ra['ms'] / 1e3) / 1e9
     per_kind = {k: {'ms_per_cycle': v['ms'] / 3, 'launches_per_cycle': v['launches'] / 3} for k, v in prof.items()}
 
+    # ---- forms beside the plain FP64 path -----------------------------------
+    forms = None
+    if not args.no_forms:
+        dh.restore_state()
+        dh.solve_cycles(opts.MaxVCycles + 2)
+        ref_Q = dh.get(BSAM_FIELD_Q, fl.Q.size)
+        forms = {'mixed': mixed_form(backend, fl, opts, ref_Q, args.steps, args.warmup, flush, local)}
+        forms['mixed']['speedup_vs_fp64'] = forms['mixed']['value'] / value
+        if args.batch > 0:
+            forms['batched'] = batched_form(backend, args.batch, max(3, args.steps // 4), args.warmup, flush, local)
+
     if rank == 0:
         cpu = None
         try:
@@ -313,6 +450,7 @@ def main():
                          'all_levels': {'achieved': achieved_all, 'frac': achieved_all / peak,
                                         'avg_launch_us': 1e3 * ra['ms'] / max(ra['launches'], 1)}},
             'cpu_baseline': cpu,
+            'forms': forms,
             'gpu_launches': int(launches),
             'clocks': clk.summary(),
         }
