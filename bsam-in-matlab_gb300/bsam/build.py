@@ -20,7 +20,7 @@ INCLUDE = os.path.join(REPO, 'include')
 HOST_LIB = os.path.join(LIBDIR, 'libbsam_host.so')
 DEV_LIB = os.path.join(LIBDIR, 'libbsam_dev.so')
 
-DEV_SOURCES = ['bsam_dev.cu', 'bsam_noalloc.cu']
+DEV_SOURCES = ['bsam_dev.cu', 'bsam_noalloc.cu', 'bsam_geom.cu']
 NVCC_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a', '-O3', '-lineinfo', '-std=c++17',
               '--fmad=false', '-Xcompiler', '-fPIC,-ffp-contract=off', '-shared']
 

@@ -28,13 +28,15 @@ class StarGeometry:
     """Closed polygon r(theta) = s0 (s1 + s2 sin(k theta + th0)) with n
     points (last = first), signed distance positive inside."""
 
-    def __init__(self, n=3000, s0=0.9, s1=1.2, s2=0.7, k=5.0, th0=0.0, name=None):
+    def __init__(self, n=3000, s0=0.9, s1=1.2, s2=0.7, k=5.0, th0=0.0, name=None, device=None):
         if n < 32:
             raise ValueError('dd_starfish:n: n must be an integer >= 32')
         self.n = int(n)
         self.params = (s0, s1, s2, k, th0)
         self._h = hostlib.lib().bsam_starfish_new(int(n), float(s0), float(s1), float(s2), float(k), float(th0))
         self.name = name or f'star: r = {s0}({s1} + {s2} sin({k} theta + {th0}))'
+        self.device = device          # a bsam.device.Context: the segment minimum runs on the GPU
+        self._cache = []              # recent (key, d): phi, delta, D, C, F sample the same points
 
     def __del__(self):
         try:
@@ -56,9 +58,24 @@ class StarGeometry:
             raise ValueError('X and Y must have equal size.')
         x = np.ascontiguousarray(X.ravel(order='F'))
         y = np.ascontiguousarray(Y.ravel(order='F'))
-        d = np.empty_like(x)
-        hostlib.lib().bsam_starfish_distance(self._h, x.ctypes.data, y.ctypes.data, d.ctypes.data, x.size)
-        return d.reshape(X.shape, order='F')
+        key = (x.size, hash(x.tobytes()), hash(y.tobytes()))
+        for k, (kk, xx, yy, dd) in enumerate(self._cache):
+            if kk == key and np.array_equal(xx, x) and np.array_equal(yy, y):
+                return dd.reshape(X.shape, order='F').copy()
+        if self.device is None:
+            d = np.empty_like(x)
+            hostlib.lib().bsam_starfish_distance(self._h, x.ctypes.data, y.ctypes.data, d.ctypes.data, x.size)
+        else:
+            from .device import polygon_dist2
+            best = np.empty_like(x)
+            sign = np.empty_like(x)
+            hostlib.lib().bsam_starfish_init_sign(self._h, x.ctypes.data, y.ctypes.data, best.ctypes.data,
+                                                  sign.ctypes.data, x.size)
+            polygon_dist2(self.device, self.vertices, x, y, best)
+            d = sign * np.sqrt(best)
+        self._cache.insert(0, (key, x, y, d))
+        del self._cache[6:]
+        return d.reshape(X.shape, order='F').copy()
 
     def psi(self, X, Y):
         return -self.signedDistance(X, Y)

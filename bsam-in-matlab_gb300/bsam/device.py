@@ -88,6 +88,9 @@ def lib():
         L.bsam_launch_count.argtypes = [P, C.POINTER(I64)]
         L.bsam_batch_result.argtypes = [P, C.c_int, P, C.c_int, C.POINTER(C.c_int), C.POINTER(D), C.POINTER(I64)]
         L.bsam_batch_set_stop.argtypes = [P, C.c_int, C.c_int, D]
+        L.bsam_polygon_dist2.argtypes = [P, P, C.c_int, P, P, P, I64]
+        L.bsam_device_memory.argtypes = [C.c_int, C.POINTER(I64), C.POINTER(I64)]
+        L.bsam_setup_levels.argtypes = [P]
         _lib = L
     return _lib
 
@@ -209,6 +212,10 @@ class DevHier:
     def set_stop(self, inst, max_vcycles, rel_tol):
         check(lib().bsam_batch_set_stop(self.h, int(inst), int(max_vcycles), float(rel_tol)))
 
+    def setup_levels(self):
+        """Run the deferred set-up steps (new-level prolongations, fills)."""
+        check(lib().bsam_setup_levels(self.h))
+
     def vcycle(self):
         check(lib().bsam_vcycle(self.h))
 
@@ -257,6 +264,38 @@ class DevHier:
         n = I64(0)
         check(lib().bsam_kernels_per_vcycle(self.h, C.byref(n)))
         return n.value
+
+
+def memory_info(device=0):
+    """(free, total) device memory in bytes."""
+    f, t = I64(0), I64(0)
+    check(lib().bsam_device_memory(int(device), C.byref(f), C.byref(t)))
+    return f.value, t.value
+
+
+def polygon_dist2(ctx, verts, x, y, best):
+    """best <- min(best, squared distance of (x, y) to the closed polygon
+    verts [n, 2]), on the device (in place; float64 contiguous arrays)."""
+    verts = np.ascontiguousarray(verts, dtype=np.float64)
+    check(lib().bsam_polygon_dist2(ctx.h, _ptr(verts), int(verts.shape[0]), _ptr(x), _ptr(y), _ptr(best),
+                                   int(best.size)))
+    return best
+
+
+class DeferredBackend:
+    """Set-up backend of a host without a device: the set-up's device steps
+    (ghost fills, new-level prolongations) are left to bsam_setup_levels on
+    the uploaded hierarchy, which runs them in the same order."""
+
+    name = 'deferred'
+
+    def run(self, H, ops):
+        for op in ops:
+            if op[0] not in ('fill', 'prolong'):
+                raise ValueError(f'bsam_device:deferred: set-up step {op[0]} cannot be deferred')
+
+    def solve_cycles(self, H):
+        raise RuntimeError('bsam_device:deferred: a deferred set-up has no solve; upload the hierarchy')
 
 
 class DeviceBackend:

@@ -26,6 +26,7 @@ def lib():
         L.bsam_starfish_nvert.argtypes = [P]
         L.bsam_starfish_vertices.argtypes = [P, P]
         L.bsam_starfish_distance.argtypes = [P, P, P, P, I64]
+        L.bsam_starfish_init_sign.argtypes = [P, P, P, P, P, I64]
         _lib = L
     return _lib
 

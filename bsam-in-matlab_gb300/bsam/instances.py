@@ -5,12 +5,12 @@ workload: -div(D grad u) + C u = f on [0,1]^2 with homogeneous Dirichlet
 data, where
 
   * log D is a sum of 16 Fourier modes cos(2 pi (kx x + ky y) + phase) with
-    wavenumbers kx, ky drawn from 1..8 and amplitudes N(0, 0.5^2), so D
-    lies roughly in [0.1, 10];
+    wavenumbers kx, ky drawn from 1..8 and amplitudes N(0, 0.5^2), clipped
+    to [ln 0.1, ln 10], so D lies in [0.1, 10];
   * C is the same mode recipe (an independent draw) squashed into [0, 1]
     by 0.5 (1 + tanh(.));
   * f is a sum of 4 Gaussian bumps with widths U[0.02, 0.1], centres
-    U[0.1, 0.9]^2 and amplitudes N(0, 100) (standard deviation 10);
+    U[0.1, 0.9]^2 and amplitudes N(0, 100^2);
   * BaseCells is drawn from {32, 64, 128} and MaxLevels from {2, 3, 4}.
 
 Every instance has a 16x16 coarsest grid on the unit square, so any set of
@@ -49,11 +49,11 @@ def random_elliptic(seed):
     w = rng.uniform(0.02, 0.1, 4)
     cx = rng.uniform(0.1, 0.9, 4)
     cy = rng.uniform(0.1, 0.9, 4)
-    amp = rng.normal(0.0, 10.0, 4)
+    amp = rng.normal(0.0, 100.0, 4)
     base = int(rng.choice([32, 64, 128]))
     maxlev = int(rng.choice([2, 3, 4]))
 
-    D = lambda X, Y: np.exp(logd(X, Y))
+    D = lambda X, Y: np.exp(np.clip(logd(X, Y), np.log(0.1), np.log(10.0)))
     C = lambda X, Y: 0.5 * (1 + np.tanh(cs(X, Y)))
 
     def f(X, Y):

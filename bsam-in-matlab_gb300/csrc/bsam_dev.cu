@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "bsam_dev.h"
+#include "internal.h"
 #include "kernels.cuh"
 
 using namespace bsam;
@@ -106,10 +107,6 @@ struct LevelPlan {
 // error reporting shared with the other translation units of the library
 int bsam_internal_set_error(int code, const std::string &msg) { return fail(code, msg); }
 
-struct bsam_ctx_s {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-};
 
 struct bsam_hier_s {
   bsam_ctx ctx = nullptr;
@@ -1182,9 +1179,24 @@ int bsam_ctx_create(int device, bsam_ctx *out) {
   return BSAM_OK;
 }
 
+int bsam_device_memory(int device, int64_t *free_bytes, int64_t *total_bytes) {
+  if (!free_bytes || !total_bytes) return fail(BSAM_ERR_ARG, "null output");
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n)
+    return fail(BSAM_ERR_NODEV, "no such CUDA device");
+  CK(cudaSetDevice(device));
+  size_t f = 0, t = 0;
+  CK(cudaMemGetInfo(&f, &t));
+  *free_bytes = (int64_t)f;
+  *total_bytes = (int64_t)t;
+  return BSAM_OK;
+}
+
 int bsam_ctx_destroy(bsam_ctx ctx) {
   if (!ctx) return BSAM_OK;
   cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->scratch) cudaFree(ctx->scratch);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return BSAM_OK;
@@ -1303,6 +1315,32 @@ int bsam_comp_residual(bsam_hier h, double out[5]) {
   launch_residual(h, 2);
   CK(cudaGetLastError());
   return read_residual(h, out);
+}
+
+int bsam_setup_levels(bsam_hier h) {
+  if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
+  int rc = set_device(h);
+  if (rc) return rc;
+  std::vector<int> mask(h->ninst);
+  for (int k = 1; k <= h->nlev; ++k) {
+    bool any = false;
+    for (int i = 0; i < h->ninst; ++i) {
+      mask[i] = k > h->inst_root[i] ? 1 : 0;
+      any = any || mask[i];
+    }
+    if (any && k > 1) {
+      // mask staged through the pinned per-instance buffer, stream-ordered
+      CK(cudaStreamSynchronize(h->stream));
+      std::copy(mask.begin(), mask.end(), h->active_host);
+      CK(cudaMemcpyAsync(h->active.p, h->active_host, sizeof(int) * h->ninst, cudaMemcpyHostToDevice, h->stream));
+      launch_prolong(h, k, 0);
+      CK(cudaMemcpyAsync(h->active.p, h->ones.p, sizeof(int) * h->ninst, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    launch_fill(h, k);
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
 }
 
 int bsam_vcycle(bsam_hier h) {

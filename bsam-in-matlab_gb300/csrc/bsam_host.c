@@ -169,3 +169,25 @@ void bsam_starfish_distance(void *p, const double *X, const double *Y, double *d
     d[i] = s * sqrt(best);
   }
 }
+
+/* The O(n) parts of bsam_starfish_distance for a device minimum: per point
+   the starting candidate (squared distance to the first vertex of the
+   segment the polar angle falls in) and the sign (+1 inside, -1 outside). */
+void bsam_starfish_init_sign(void *p, const double *X, const double *Y, double *init, double *sign, int64_t n) {
+  const Starfish *g = (const Starfish *)p;
+  const double twopi = 2 * M_PI;
+  const int ns = g->ns;
+  for (int64_t i = 0; i < n; ++i) {
+    const double x = X[i], y = Y[i];
+    double ang = atan2(y, x);
+    ang = ang - floor(ang / twopi) * twopi;
+    int seg = (int)floor(ang * ns / twopi) + 1;
+    if (seg > ns) seg = ns;
+    const double ax = g->a[2 * (seg - 1)], ay = g->a[2 * (seg - 1) + 1];
+    init[i] = (x - ax) * (x - ax) + (y - ay) * (y - ay);
+    const double ux = cos(ang), uy = sin(ang);
+    const double ex = g->e[2 * (seg - 1)], ey = g->e[2 * (seg - 1) + 1];
+    const double radius = (ax * ey - ay * ex) / (ux * ey - uy * ex);
+    sign[i] = (hypot(x, y) > radius) ? -1.0 : 1.0;
+  }
+}

@@ -1,0 +1,19 @@
+// internal.h -- state shared by the library's translation units (not part
+// of the C-ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+// one device and one stream; `scratch` is reusable device memory for calls
+// that stage host arrays (the geometry sampling), grown on demand and freed
+// with the context
+struct bsam_ctx_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  void *scratch = nullptr;
+  size_t scratch_bytes = 0;
+};
+
+// records the message of a failed call for bsam_last_error(); returns code
+int bsam_internal_set_error(int code, const std::string &msg);

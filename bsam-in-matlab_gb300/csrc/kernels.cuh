@@ -547,8 +547,8 @@ __global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, FieldsT<
   const T f22 = (((9 * C + 3 * Wp) + 3 * Sp) + E[2][2]) / 16;
   T *Q = f.Q + q_off;
   const int c = (2 * a + 1) + (2 * b + 1) * ldq;
+  if (!act) return;   // frozen instance, or an instance whose level k is not new
   if (correct) {
-    if (!act) return;
     Q[c] = Q[c] + f11;
     Q[c + 1] = Q[c + 1] + f21;
     Q[c + ldq] = Q[c + ldq] + f12;

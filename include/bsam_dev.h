@@ -101,6 +101,10 @@ typedef struct {
 int bsam_ctx_create(int device, bsam_ctx *out);
 int bsam_ctx_destroy(bsam_ctx ctx);
 
+/* Free and total memory of a device (admission control of the serving
+ * loop; no reference counterpart). */
+int bsam_device_memory(int device, int64_t *free_bytes, int64_t *total_bytes);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char *bsam_last_error(void);
 
@@ -123,6 +127,15 @@ int bsam_fill_ghosts(bsam_hier h, int level);
 /* Initial guess of a new level by bilinear prolongation of the parent
  * window (ebAddLevel.m:26-31): Q_k interior = prolongBilin(W). */
 int bsam_prolong_level(bsam_hier h, int level);
+
+/* The device steps of the hierarchy set-up, deferred: for every level k =
+ * 1..nlev in order, the new-level prolongation (ebAddLevel.m:26-31) of the
+ * instances whose level k lies above their root, then the ghost fill of
+ * level k (ebSetup.m:66, ebAddLevel.m:29-31).  A host that builds the
+ * hierarchy without a device (the serving loop's builder processes) uploads
+ * the pre-step fields and calls this once; the result equals running the
+ * steps as the set-up goes.  No reference counterpart as one call. */
+int bsam_setup_levels(bsam_hier h);
 
 /* H = ebSolveCycles(H) (ebSolveCycles.m:8-70): ghost fill, residual r_0,
  * then V-cycles until rel <= RelTol or MaxVCycles.  res_hist receives
@@ -205,6 +218,17 @@ int bsam_kernels_per_vcycle(bsam_hier h, int64_t *count);
  * overlap on the GPU race and must be serialised by the caller.  The first
  * call on each device looks up the array's device address with that device
  * current; make it before any stream capture. */
+/* Diffuse-domain coefficient sampling on the device (the O(n x segments)
+ * part of DiffuseDomainBSAM/src/ddStarfishGeometry.m:140-177): for each of
+ * the n points (x[i], y[i]), best[i] <- min(best[i], min_j dd_j) where dd_j
+ * is the squared distance to segment j of the closed polygon verts
+ * [nverts][2] (x, y interleaved, last vertex = first), computed with the
+ * reference's per-segment formula.  best[i] comes in holding the host's
+ * starting candidate; the host applies the sign and the square root.  All
+ * arrays are host memory; the call is synchronous. */
+int bsam_polygon_dist2(bsam_ctx ctx, const double *verts, int nverts, const double *x, const double *y, double *best,
+                       int64_t n);
+
 #define BSAM_NOALLOC_MAX_BLOCKS 16384
 int bsam_patch_residual_noalloc(const double *Q, const double *FTrue, const double *DeW, const double *DnS,
                                 const double *CC, const uint8_t *covered, int mx, int my, double hx, double hy,
