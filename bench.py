@@ -30,7 +30,10 @@ composite residual 1e-10 (10 cycles).
                   MaxLevels {2,3,4}, TagThreshold 1e-2), the last ebSolve stage
                   of each: solved one after another on the plain path, then as
                   one batch in FP64 (checked bit for bit against the solo
-                  solves) and in the mixed form.
+                  solves) and in the mixed form;
+          serving Poisson streams of diffuse-domain star requests at a few
+                  offered rates through the continuous-batching server
+                  (bsam.serve): solves/s and p50/p99 latency.
 
 `--impl reference` times the reference's CPU path instead: MATLAB is not
 available, so the C oracle restatement runs on all host cores.
@@ -301,6 +304,34 @@ def batched_form(backend, n, steps, warmup, flush, local):
     return out
 
 
+def serving_form(rates, per_rate):
+    """Serving form: Poisson streams of diffuse-domain star requests (k in
+    {3..7}, b, a0, theta0, eps drawn per request, base 64^2, MaxLevels
+    {3,4,5}, mixed precision, RelTol 1e-10) through the continuous-batching
+    server; p50/p99 latency from submission to the solution on the host."""
+    from bsam.serve import Server, star_request, run_stream, summarize
+    t0 = time.perf_counter()
+    srv = Server(waves=3, wave_size=64)
+    start_s = time.perf_counter() - t0
+    warm, _ = run_stream(srv, [star_request(90000 + i) for i in range(srv.nbuild)], rate=100.0, seed=9)
+    out = {'workload': 'served diffuse-domain star requests (Poisson arrivals), base 64^2, MaxLevels U{3,4,5}, '
+                       'mixed precision, RelTol 1e-10',
+           'builders': srv.nbuild, 'wave_slots': len(srv.ctxs), 'server_start_s': start_s, 'rates': []}
+    for rate in rates:
+        n = int(max(per_rate, round(rate * 3)))
+        specs = [star_request(int(rate * 1000) + i) for i in range(n)]
+        w0 = len(srv.waves_run)
+        res, wall = run_stream(srv, specs, rate=rate, seed=int(rate))
+        d = summarize(res, wall)
+        d['offered_rate'] = rate
+        sizes = [w['size'] for w in srv.waves_run[w0:]]
+        d['waves'] = len(sizes)
+        d['mean_wave_size'] = float(np.mean(sizes)) if sizes else 0.0
+        out['rates'].append(d)
+    srv.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -309,7 +340,8 @@ def main():
     ap.add_argument('--impl', default='native', choices=['native', 'reference'])
     ap.add_argument('--cpu-budget', type=float, default=15.0)
     ap.add_argument('--batch', type=int, default=256, help='instances of the batching form (0: skip)')
-    ap.add_argument('--no-forms', action='store_true', help='skip the mixed and batching forms')
+    ap.add_argument('--no-forms', action='store_true', help='skip the mixed, batching and serving forms')
+    ap.add_argument('--serve-rates', default='5,10,20', help='offered request rates of the serving form')
     args = ap.parse_args()
     rank = int(os.environ.get('RANK', 0))
     world = int(os.environ.get('WORLD_SIZE', 1))
@@ -361,12 +393,10 @@ def main():
         torch.cuda.synchronize()
     launches = dh.launch_count() - n0
     per = np.array([a.elapsed_time(b) for a, b in zip(starts, ends)])
-    total_ms = float(per.sum())
-    if dist:
-        t = torch.tensor([total_ms], device=f'cuda:{local}')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps / (total_ms / 1e3)
+    from bsam.replicas import job_rate
+    # replicas: the job time is the slowest rank's (no data-path collective)
+    value, total_s = job_rate(args.steps, float(per.sum()) / 1e3, dist, torch.device('cuda', local))
+    total_ms = 1e3 * total_s
 
     # ---- end to end through the C-ABI with host buffers ---------------------
     Q0 = torch.from_numpy(fl.Q.copy()).pin_memory().numpy()
@@ -389,12 +419,7 @@ def main():
         check(L.bsam_get_field(dh.h, BSAM_FIELD_Q, Qout.ctypes.data, Qout.size))
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     assert rel2 <= 1e-10
-    e2e_total = sum(e2e_ms)
-    if dist:
-        t = torch.tensor([e2e_total], device=f'cuda:{local}')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * args.steps / (e2e_total / 1e3)
+    e2e_value, _ = job_rate(args.steps, sum(e2e_ms) / 1e3, dist, torch.device('cuda', local))
 
     # ---- roofline of the smoother -------------------------------------------
     prof = dh.profile(3)
@@ -416,6 +441,9 @@ def main():
         forms['mixed']['speedup_vs_fp64'] = forms['mixed']['value'] / value
         if args.batch > 0:
             forms['batched'] = batched_form(backend, args.batch, max(3, args.steps // 4), args.warmup, flush, local)
+        rates = [float(r) for r in args.serve_rates.split(',') if r.strip()]
+        if rates and rank == 0:
+            forms['serving'] = serving_form(rates, 20)
 
     if rank == 0:
         cpu = None
