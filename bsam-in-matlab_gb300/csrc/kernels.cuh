@@ -57,8 +57,14 @@ struct FieldsT {
   const T *CC, *ID, *DeW, *DnS, *bcg, *cfd, *pcoef;
   const uint8_t *flags;        // bit0 covered by a finer level, bit1 correction target
   const int *win, *fp;         // window gathers, footprint scatters (2 ints/cell)
-  const int *active;           // per instance: 1 while its V-cycles continue
+  const int *active;           // per instance: 1 while its V-cycles continue (below)
 };
+// `active` is written only by k_residual_final, the last kernel of a launch
+// chain, and the host synchronises before the next chain (or writes it with
+// a stream-ordered copy).  Within a chain no kernel can still be in its
+// pre-wait part when k_residual_final's body runs (every kernel completes
+// only after its predecessor), so kernels read `active` before
+// griddepcontrol.wait and the blocks of a frozen instance skip their loads.
 using Fields = FieldsT<double>;
 
 // FP64 view of a value of either type (a no-op for double)
@@ -141,15 +147,15 @@ __global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, 
   chain_trigger();
   const int t = blockIdx.x * kBlock + threadIdx.x;
   const int i = off + t;
-  const int8_t ty = (t < n) ? G.type[i] : (int8_t)-1;
-  const int dst = (t < n) ? G.dst[i] : 0;
-  const int inst = (t < n && G.inst) ? G.inst[i] : -1;
-  chain_wait();
-  if (t >= n) return;
   // a converged instance of a batch stays frozen; a fill that follows the
   // restriction from level `need` skips the instances without that level
   // (their own V-cycle starts below it)
-  if (inst >= 0 && (!active[inst] || inst_nlev[inst] < need)) return;
+  const int inst = (t < n && G.inst) ? G.inst[i] : -1;
+  const bool skip = t >= n || (inst >= 0 && (!active[inst] || inst_nlev[inst] < need));
+  const int8_t ty = skip ? (int8_t)-1 : G.type[i];
+  const int dst = skip ? 0 : G.dst[i];
+  chain_wait();
+  if (skip) return;
   const T hx = T(hx_), hy = T(hy_);
   if (ty == G_RING) {
     QC[dst] = Q[G.a[i]];
@@ -215,7 +221,7 @@ __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__
   RelaxChunk R;
   if (ok) R = chunks[ch];
   const int s = ok ? R.s0 + (threadIdx.x & (kChunk - 1)) : 0;
-  ok = ok && s < R.s0 + R.n;
+  ok = ok && s < R.s0 + R.n && f.active[R.inst];
   if (!ok) {
     chain_wait();
     return;
@@ -251,7 +257,6 @@ __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__
     else if (fresh) { ky = 3; ry = perim[R.pe_off + 2 * my + sy * mx + li]; }
   }
   chain_wait();
-  const int act = f.active[R.inst];   // a converged instance of a batch stays frozen
   const T c83 = T(8.0 / 3.0), c13 = T(1.0 / 3.0);
   T *__restrict__ Q = f.Q + R.q_off;
   T qe = Q[c + 1], qw = Q[c - 1], qn = Q[c + ldq], qs = Q[c - ldq];
@@ -276,7 +281,6 @@ __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__
   t = t + divh<kPow2>(qn * dN, hy2, ihy2);
   t = t + divh<kPow2>(qs * dS, hy2, ihy2);
   t = t * idg;
-  if (!act) return;
   const T omega = T(omega_);
   if (unit_omega) Q[c] = t;
   else Q[c] = omega * t + (1 - omega) * Q[c];
@@ -302,13 +306,15 @@ __global__ void __launch_bounds__(kBlock) k_restrict(LevelD L, Decomp D, FieldsT
   }
   const int p = find_patch(D, blockIdx.x, g);
   const PatchD &P = L.patches[p];
+  if (!f.active[P.inst]) {
+    chain_wait();
+    return;
+  }
   const int cmx = P.mx >> 1, q_off = P.q_off, ldq = P.mx + 2, qc_off = P.qc_off;
   const int s = g - __ldg(D.beg + p);
   const int cj = s / cmx, ci = s - cj * cmx;
   const int dst = to_parent ? __ldg(f.fp + 2 * (P.fp_off + s)) : 0;
-  const int inst = P.inst;
   chain_wait();
-  if (!f.active[inst]) return;
   const T R = restrict_cell<T>(f.Q + q_off, ldq, ci, cj);
   f.QC[qc_off + (ci + 1) + (cj + 1) * (cmx + 2)] = R;
   if (to_parent) f.Q[dst] = R;
@@ -418,14 +424,14 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
   int b = blockIdx.x;
   if (b < nb_ring) {
     const int t = b * kBlock + threadIdx.x;
-    int src = 0, dst = 0, inst = -1;
-    if (t < n_ring) {
+    int src = 0, dst = 0;
+    bool on = t < n_ring && (!ring_inst || f.active[__ldg(ring_inst + ring_off + t)]);
+    if (on) {
       src = __ldg(ring + 2 * (ring_off + t));
       dst = __ldg(ring + 2 * (ring_off + t) + 1);
-      if (ring_inst) inst = __ldg(ring_inst + ring_off + t);
     }
     chain_wait();
-    if (t < n_ring && (inst < 0 || f.active[inst])) f.QC[dst] = f.Q[src];
+    if (on) f.QC[dst] = f.Q[src];
     return;
   }
   b -= nb_ring;
@@ -437,6 +443,10 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
     }
     const int p = find_patch(D, b, g);
     const PatchD &P = L.patches[p];
+    if (!f.active[P.inst]) {
+      chain_wait();
+      return;
+    }
     const int mx = P.mx, cmx = mx >> 1, cmy = P.my >> 1, ldq = mx + 2;
     const int s = g - __ldg(D.beg + p);
     const int cj = s / cmx, ci = s - cj * cmx;
@@ -469,9 +479,7 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
     const double pN = dbl(__ldg(PDnS + ci + (cj + 1) * cmx)), pS = dbl(__ldg(PDnS + ci + cj * cmx));
     const double pC = dbl(__ldg(PCC + s));
     const int dst = __ldg(f.fp + 2 * (P.fp_off + s) + 1);
-    const int inst = P.inst;
     chain_wait();
-    if (!f.active[inst]) return;
     const T *Qp = f.Q + q_off;
     const T *Fp = f.F + c_off;
     double rf[4];
@@ -495,10 +503,10 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
   }
   b -= D.nblocks;
   const int t = b * kBlock + threadIdx.x;
-  const int cell = t < n_tgt ? C.cell[t] : 0;
-  const int inst = t < n_tgt ? Lc.patches[C.patch[t]].inst : 0;
+  const bool on = t < n_tgt && f.active[Lc.patches[C.patch[t]].inst];
+  const int cell = on ? C.cell[t] : 0;
   chain_wait();
-  if (t >= n_tgt || !f.active[inst]) return;
+  if (!on) return;
   f.F[cell] = T(add_corrections<T>(dbl(f.F[cell]), C, t, L, Lc, f, false));
 }
 
@@ -517,6 +525,10 @@ __global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, FieldsT<
   }
   const int p = find_patch(D, blockIdx.x, g);
   const PatchD &P = L.patches[p];
+  if (!f.active[P.inst]) {   // frozen instance, or an instance whose level k is not new
+    chain_wait();
+    return;
+  }
   const int cm = P.mx >> 1;
   const int s = g - __ldg(D.beg + p);
   const int b = s / cm, a = s - b * cm;
@@ -527,9 +539,8 @@ __global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, FieldsT<
   for (int dj = 0; dj < 3; ++dj)
 #pragma unroll
     for (int di = 0; di < 3; ++di) src[dj][di] = __ldg(win + (a + di) + (b + dj) * ldw);
-  const int qc_off = P.qc_off, q_off = P.q_off, ldq = P.mx + 2, inst = P.inst;
+  const int qc_off = P.qc_off, q_off = P.q_off, ldq = P.mx + 2;
   chain_wait();
-  const int act = f.active[inst];
   const T *QC = f.QC + qc_off;
   T E[3][3];
 #pragma unroll
@@ -547,7 +558,6 @@ __global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, FieldsT<
   const T f22 = (((9 * C + 3 * Wp) + 3 * Sp) + E[2][2]) / 16;
   T *Q = f.Q + q_off;
   const int c = (2 * a + 1) + (2 * b + 1) * ldq;
-  if (!act) return;   // frozen instance, or an instance whose level k is not new
   if (correct) {
     Q[c] = Q[c] + f11;
     Q[c + 1] = Q[c + 1] + f21;
@@ -579,7 +589,7 @@ __global__ void __launch_bounds__(kBlock) k_coarsest(const double *__restrict__ 
   const int N = D.N;
   const int row = (blockIdx.x * kBlock + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (row >= N) {
+  if (row >= N || !f.active[D.inst]) {
     chain_wait();
     return;
   }
@@ -594,7 +604,6 @@ __global__ void __launch_bounds__(kBlock) k_coarsest(const double *__restrict__ 
     bv[i] = (c < N && rhs) ? __ldg(rhs + c) : 0.0;
   }
   chain_wait();
-  const int act = f.active[D.inst];
   const T *F = f.F + D.c_off;
   double s = 0.0;
 #pragma unroll
@@ -608,7 +617,7 @@ __global__ void __launch_bounds__(kBlock) k_coarsest(const double *__restrict__ 
     const double o = __shfl_down_sync(0xffffffffu, s, off);
     if (lane < off) s = s + o;
   }
-  if (lane == 0 && act) {
+  if (lane == 0) {
     const int i = row % D.n1, j = row / D.n1;
     f.Q[D.q_off + (i + 1) + (j + 1) * (D.n1 + 2)] = T(s);
   }
@@ -633,7 +642,7 @@ struct ResAcc {
 };
 
 struct ResTask {
-  int kind, level, a, b, n, slot, pad0, pad1;   // a: patch / CSR level / ring start; b: first item
+  int kind, level, a, b, n, slot, inst, pad;   // a: patch / CSR level / ring start; b: first item
 };
 
 struct LevelX {
@@ -649,7 +658,9 @@ __global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ 
   chain_trigger();
   const int w = blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (w >= ntask) {
+  // a frozen instance's residual is neither reported nor needed (its QC
+  // refresh would rewrite the same values), so its warps only wait
+  if (w >= ntask || !f.active[tasks[w].inst]) {
     chain_wait();
     return;
   }
@@ -837,11 +848,14 @@ __global__ void __launch_bounds__(kBlock) k_freset(Decomp D, const PatchD *__res
   }
   const int p = find_patch(D, blockIdx.x, g);
   const PatchD &P = patches[p];
+  if (!f.active[P.inst]) {
+    chain_wait();
+    return;
+  }
   const int cc = P.c_off + (g - __ldg(D.beg + p));
   const double v = __ldg(f.FTrue + cc);
-  const int inst = P.inst;
   chain_wait();
-  if (f.active[inst]) f.F[cc] = v;
+  f.F[cc] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -857,12 +871,15 @@ __global__ void __launch_bounds__(kBlock) k_update(Decomp D, const PatchD *__res
   }
   const int p = find_patch(D, blockIdx.x, g);
   const PatchD &P = patches[p];
+  if (!active[P.inst]) {
+    chain_wait();
+    return;
+  }
   const int s = g - __ldg(D.beg + p);
   const int lj = s / P.mx, lx = s - lj * P.mx;
   const int qi = P.q_off + (lx + 1) + (lj + 1) * (P.mx + 2);
-  const int inst = P.inst;
   chain_wait();
-  if (active[inst]) Q[qi] = Q[qi] + (double)E[qi];
+  Q[qi] = Q[qi] + (double)E[qi];
 }
 
 // FP32 copy of an FP64 array (coefficient copies of the mixed form)
