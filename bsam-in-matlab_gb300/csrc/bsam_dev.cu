@@ -131,7 +131,10 @@ struct bsam_hier_s {
   DBuf<int> inst_nlev;             // per instance: its finest level
   // mixed form: FP32 correction, its right-hand side and coarse shadows,
   // FP32 coefficient copies (homogeneous boundary data)
-  DBuf<float> E, F32, QC32, DeW32, DnS32, CC32, ID32, pcoef32, cfd32, bcg32;
+  DBuf<float> E, F32, QC32, DeW32, DnS32, CC32, ID32, pcoef32, cfd32, bcg32, DeWr32, DnSr32;
+  // the smoother's face coefficients: on levels whose h^2 is a power of two
+  // pre-multiplied by the exact 1/h^2 (k_relax<T, true>), else as uploaded
+  DBuf<double> DeWr, DnSr;
   bool f32_dirty = true;
   DecompH all_cells;               // every cell of every level (batch force reset)
   std::vector<InstRes> hir;        // host copy of the per-instance reduction plan
@@ -186,6 +189,7 @@ LevelD leveld(bsam_hier h, int k) {
   d.hx2 = L.hx * L.hx; d.hy2 = L.hy * L.hy;
   d.ihx2 = 1.0 / d.hx2; d.ihy2 = 1.0 / d.hy2;
   d.pow2 = L.pow2 ? 1 : 0;
+  d.fhx = (float)d.hx; d.fhy = (float)d.hy; d.fhx2 = (float)d.hx2; d.fhy2 = (float)d.hy2;
   return d;
 }
 
@@ -263,6 +267,21 @@ template <> FieldsT<float> fields_t<float>(bsam_hier h) {
   return f;
 }
 
+// the smoother's arrays: face coefficients pre-scaled on power-of-two levels
+template <class T> FieldsT<T> relax_fields(bsam_hier h);
+template <> Fields relax_fields<double>(bsam_hier h) {
+  Fields f = fields(h);
+  f.DeW = h->DeWr.p;
+  f.DnS = h->DnSr.p;
+  return f;
+}
+template <> FieldsT<float> relax_fields<float>(bsam_hier h) {
+  FieldsT<float> f = fields_t<float>(h);
+  f.DeW = h->DeWr32.p;
+  f.DnS = h->DnSr32.p;
+  return f;
+}
+
 // algorithmic bytes scale with the value type (FP64 figures x size/8)
 template <class T> constexpr double tscale() { return (double)sizeof(T) / 8.0; }
 
@@ -285,7 +304,7 @@ template <class T = double>
 void launch_relax(bsam_hier h, int k, int nsweeps) {
   if (nsweeps <= 0) return;
   const LevelPlan &L = h->lev[k];
-  FieldsT<T> f = fields_t<T>(h);
+  FieldsT<T> f = relax_fields<T>(h);
   LevelD ld = leveld(h, k);
   const RelaxChunk *ch = h->rchunks.p + L.rc_off;
   const int grid = (L.rc_n + kBlock / kChunk - 1) / (kBlock / kChunk);
@@ -295,11 +314,11 @@ void launch_relax(bsam_hier h, int k, int nsweeps) {
       const int fresh = (s > 0 || m > 0) ? 1 : 0;
       Launch l(h, K_RELAX, 24.0 * tscale<T>() * (double)L.ncells, k);
       if (L.pow2)
-        launch_k(h, k_relax<T, true>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m, h->opts.omega,
-                 unit, fresh);
+        launch_k(h, k_relax<T, true>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m,
+                 (T)h->opts.omega, unit, fresh);
       else
-        launch_k(h, k_relax<T, false>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m, h->opts.omega,
-                 unit, fresh);
+        launch_k(h, k_relax<T, false>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m,
+                 (T)h->opts.omega, unit, fresh);
     }
   launch_fill<T>(h, k);
 }
@@ -453,7 +472,8 @@ int ensure_f32(bsam_hier h) {
     if ((rc = h->E.alloc(h->Q.n)) || (rc = h->F32.alloc(h->F.n)) || (rc = h->QC32.alloc(std::max<size_t>(h->QC.n, 1))) ||
         (rc = h->DeW32.alloc(h->DeW.n)) || (rc = h->DnS32.alloc(h->DnS.n)) || (rc = h->CC32.alloc(h->CC.n)) ||
         (rc = h->ID32.alloc(h->ID.n)) || (rc = h->pcoef32.alloc(std::max<size_t>(h->pcoef.n, 1))) ||
-        (rc = h->cfd32.alloc(std::max<size_t>(h->cfd.n, 1))) || (rc = h->bcg32.alloc(std::max<size_t>(h->bcg.n, 1))))
+        (rc = h->cfd32.alloc(std::max<size_t>(h->cfd.n, 1))) || (rc = h->bcg32.alloc(std::max<size_t>(h->bcg.n, 1))) ||
+        (rc = h->DeWr32.alloc(h->DeW.n)) || (rc = h->DnSr32.alloc(h->DnS.n)))
       return rc;
     CK(cudaMemsetAsync(h->F32.p, 0, sizeof(float) * h->F32.n, h->stream));
     CK(cudaMemsetAsync(h->QC32.p, 0, sizeof(float) * h->QC32.n, h->stream));
@@ -463,7 +483,8 @@ int ensure_f32(bsam_hier h) {
   if (h->f32_dirty) {
     const std::pair<DBuf<double> *, DBuf<float> *> cv[] = {{&h->DeW, &h->DeW32}, {&h->DnS, &h->DnS32},
                                                            {&h->CC, &h->CC32},   {&h->ID, &h->ID32},
-                                                           {&h->pcoef, &h->pcoef32}, {&h->cfd, &h->cfd32}};
+                                                           {&h->pcoef, &h->pcoef32}, {&h->cfd, &h->cfd32},
+                                                           {&h->DeWr, &h->DeWr32}, {&h->DnSr, &h->DnSr32}};
     for (const auto &c : cv)
       if (c.first->n) launch_k(h, k_to_f32, 4 * 152, kBlock, (const double *)c.first->p, c.second->p, (long long)c.first->n);
     CK(cudaGetLastError());
@@ -976,6 +997,23 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
   if ((rc = h->perim.upload(B.perim.data(), B.perim.size(), s)) ||
       (rc = h->rchunks.upload(B.chunks.data(), B.chunks.size(), s)))
     return rc;
+  // smoother coefficients, exactly scaled by 1/h^2 on power-of-two levels
+  {
+    std::vector<double> dew(d->DeW, d->DeW + d->n_dew), dns(d->DnS, d->DnS + d->n_dns);
+    for (int k = 1; k <= d->nlev; ++k) {
+      const LevelPlan &L = h->lev[k];
+      if (!L.pow2) continue;
+      const double ix = 1.0 / (L.hx * L.hx), iy = 1.0 / (L.hy * L.hy);
+      for (int p = L.p0; p < L.p1; ++p) {
+        const int32_t *r = B.P(p);
+        const int64_t mx = r[PD_MX], my = r[PD_MY];
+        for (int64_t i = 0; i < (mx + 1) * my; ++i) dew[r[PD_DEWOFF] + i] *= ix;
+        for (int64_t i = 0; i < mx * (my + 1); ++i) dns[r[PD_DNSOFF] + i] *= iy;
+      }
+    }
+    if ((rc = h->DeWr.upload(dew.data(), dew.size(), s)) || (rc = h->DnSr.upload(dns.data(), dns.size(), s))) return rc;
+    CK(cudaStreamSynchronize(s));
+  }
   // residual plan: warp tasks, slots in instance order, level by level
   // (main cells, then the level's correction targets), then the QC refresh
   // tasks of the levels above each instance's root
@@ -1120,11 +1158,11 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
 void release(bsam_hier h) {
   drop_graph(h);
   for (DBuf<double> *b : {&h->Q, &h->F, &h->FTrue, &h->QC, &h->CC, &h->ID, &h->DeW, &h->DnS, &h->bcg, &h->cfd,
-                          &h->pcoef, &h->Ainv, &h->bcRhs, &h->slots, &h->partials, &h->hist, &h->saveQ, &h->saveQC,
+                          &h->pcoef, &h->Ainv, &h->bcRhs, &h->slots, &h->partials, &h->hist, &h->saveQ, &h->saveQC, &h->DeWr, &h->DnSr,
                           &h->saveF})
     b->release();
   for (DBuf<float> *b : {&h->E, &h->F32, &h->QC32, &h->DeW32, &h->DnS32, &h->CC32, &h->ID32, &h->pcoef32, &h->cfd32,
-                         &h->bcg32})
+                         &h->bcg32, &h->DeWr32, &h->DnSr32})
     b->release();
   for (DBuf<int> *b : {&h->win, &h->fp, &h->ring, &h->ints, &h->ct_cell, &h->ct_patch, &h->ct_beg, &h->ct_item,
                        &h->ct_j, &h->active, &h->iters, &h->ones, &h->g_inst, &h->ring_inst, &h->inst_nlev, &h->g_dst, &h->g_a, &h->g_b, &h->g_c, &h->g_d, &h->g_e})

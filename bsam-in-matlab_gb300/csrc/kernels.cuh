@@ -82,7 +82,15 @@ struct LevelD {
   const PatchD *patches;       // this level's patches
   double hx, hy, hx2, hy2, ihx2, ihy2;   // ihx2 = 1/hx2 (used only when exact)
   int pow2;                    // hx2 and hy2 are powers of two
+  float fhx, fhy, fhx2, fhy2;  // FP32 copies for the correction cycle
 };
+
+// the level's cell sizes in the cycle's value type
+template <class T> struct LevelH {
+  T hx, hy, hx2, hy2;
+};
+__device__ __forceinline__ LevelH<double> level_h(const LevelD &L, double) { return {L.hx, L.hy, L.hx2, L.hy2}; }
+__device__ __forceinline__ LevelH<float> level_h(const LevelD &L, float) { return {L.fhx, L.fhy, L.fhx2, L.fhy2}; }
 
 // `b` is the block index within the decomposition
 __device__ __forceinline__ int find_patch(const Decomp &D, int b, int g) {
@@ -156,7 +164,7 @@ __global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, 
   const int dst = skip ? 0 : G.dst[i];
   chain_wait();
   if (skip) return;
-  const T hx = T(hx_), hy = T(hy_);
+  const T hx = T(hx_), hy = T(hy_);   // once per thread, outside the relaxation
   if (ty == G_RING) {
     QC[dst] = Q[G.a[i]];
   } else if (ty == G_PHYS_CORNER) {
@@ -213,7 +221,7 @@ __device__ __forceinline__ T eval_inline(const Rule &R, const T *Q) {
 
 template <class T, bool kPow2>
 __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__restrict__ chunks, int nchunks,
-                                                  FieldsT<T> f, const Rule *__restrict__ perim, int m, double omega_,
+                                                  FieldsT<T> f, const Rule *__restrict__ perim, int m, T omega,
                                                   int unit_omega, int fresh) {
   chain_trigger();
   const int ch = blockIdx.x * (kBlock / kChunk) + threadIdx.x / kChunk;
@@ -246,42 +254,51 @@ __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__
   Rule rx, ry;
   if (li == 0 || li == mx - 1) {
     sx = (li == 0) ? 0 : 1;
-    const int bc = R.bc[sx];
+    const int bc = sx ? R.bc[1] : R.bc[0];   // selects, not an indexed (local-memory) array
     if (bc) { kx = bc; gx = __ldg(g4 + sx * my + lj); }
     else if (fresh) { kx = 3; rx = perim[R.pe_off + sx * my + lj]; }
   }
   if (lj == 0 || lj == my - 1) {
     sy = (lj == 0) ? 0 : 1;
-    const int bc = R.bc[2 + sy];
+    const int bc = sy ? R.bc[3] : R.bc[2];
     if (bc) { ky = bc; gy = __ldg(g4 + 2 * my + sy * mx + li); }
     else if (fresh) { ky = 3; ry = perim[R.pe_off + 2 * my + sy * mx + li]; }
   }
   chain_wait();
   const T c83 = T(8.0 / 3.0), c13 = T(1.0 / 3.0);
+  const LevelH<T> H = level_h(L, T(0));
   T *__restrict__ Q = f.Q + R.q_off;
   T qe = Q[c + 1], qw = Q[c - 1], qn = Q[c + ldq], qs = Q[c - ldq];
   if (kx > 0) {
     T v;
     if (kx == 1) v = c83 * gx + c13 * Q[sx ? c - 1 : c + 1];
-    else if (kx == 2) v = T(L.hx) * gx;
+    else if (kx == 2) v = H.hx * gx;
     else v = eval_inline<T>(rx, f.Q);
     if (sx) qe = v; else qw = v;
   }
   if (ky > 0) {
     T v;
     if (ky == 1) v = c83 * gy + c13 * Q[sy ? c - ldq : c + ldq];
-    else if (ky == 2) v = T(L.hy) * gy;
+    else if (ky == 2) v = H.hy * gy;
     else v = eval_inline<T>(ry, f.Q);
     if (sy) qn = v; else qs = v;
   }
-  const T hx2 = T(L.hx2), ihx2 = T(L.ihx2), hy2 = T(L.hy2), ihy2 = T(L.ihy2);
+  // kPow2: the coefficients arrive pre-scaled by the exact 1/h^2 (a power of
+  // two), and (q D) 2^-k == q (D 2^-k) in floating point, so one product
+  // per neighbour gives the reference's (q D)/h^2 bit for bit
   T t = f.F[cc];
-  t = t + divh<kPow2>(qe * dE, hx2, ihx2);
-  t = t + divh<kPow2>(qw * dW, hx2, ihx2);
-  t = t + divh<kPow2>(qn * dN, hy2, ihy2);
-  t = t + divh<kPow2>(qs * dS, hy2, ihy2);
+  if (kPow2) {
+    t = t + qe * dE;
+    t = t + qw * dW;
+    t = t + qn * dN;
+    t = t + qs * dS;
+  } else {
+    t = t + (qe * dE) / H.hx2;
+    t = t + (qw * dW) / H.hx2;
+    t = t + (qn * dN) / H.hy2;
+    t = t + (qs * dS) / H.hy2;
+  }
   t = t * idg;
-  const T omega = T(omega_);
   if (unit_omega) Q[c] = t;
   else Q[c] = omega * t + (1 - omega) * Q[c];
 }
@@ -771,7 +788,7 @@ struct SlotRange {
 // instances active during it; mode 2 only reports (an eager call).  The history and the stop test follow
 // ebSolveCycles.m:17-46: an instance stays active while it < MaxVCycles and
 // rel > RelTol.
-constexpr int kFinal = 256;
+constexpr int kFinal = 512;
 __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__restrict__ ir,
                                                           const SlotRange *__restrict__ ranges, const double *slots,
                                                           int nslots, ResAcc *acc, int *active, int *iters,
@@ -781,12 +798,23 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__rest
   const InstRes R = ir[inst];
   __shared__ double s_a[kFinal], s_b[kFinal];
   const int t = threadIdx.x;
+  // four independent loads in flight per thread (max is order-free)
   double li = 0, fn = 0;
-  for (int r = R.range0; r < R.range1; ++r)
-    for (int i = ranges[r].s0 + t; i < ranges[r].s1; i += kFinal) {
+  for (int r = R.range0; r < R.range1; ++r) {
+    const int s0 = ranges[r].s0, s1 = ranges[r].s1;
+    int i = s0 + t;
+    for (; i + 3 * kFinal < s1; i += 4 * kFinal) {
+      const double a0 = slots[i], a1 = slots[i + kFinal], a2 = slots[i + 2 * kFinal], a3 = slots[i + 3 * kFinal];
+      const double b0 = slots[2 * nslots + i], b1 = slots[2 * nslots + i + kFinal];
+      const double b2 = slots[2 * nslots + i + 2 * kFinal], b3 = slots[2 * nslots + i + 3 * kFinal];
+      li = fmax(li, fmax(fmax(a0, a1), fmax(a2, a3)));
+      fn = fmax(fn, fmax(fmax(b0, b1), fmax(b2, b3)));
+    }
+    for (; i < s1; i += kFinal) {
       li = fmax(li, slots[i]);
       fn = fmax(fn, slots[2 * nslots + i]);
     }
+  }
   s_a[t] = li;
   s_b[t] = fn;
   __syncthreads();
@@ -802,8 +830,18 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__rest
   __syncthreads();
   double l2sq = 0;
   for (int r = R.range0; r < R.range1; ++r) {
-    double sum = 0;
-    for (int i = ranges[r].s0 + t; i < ranges[r].s1; i += kFinal) sum = sum + slots[nslots + i];
+    // fixed order: four strided partial sums per thread, then their sum
+    const int s0 = ranges[r].s0, s1 = ranges[r].s1;
+    double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+    int i = s0 + t;
+    for (; i + 3 * kFinal < s1; i += 4 * kFinal) {
+      p0 = p0 + slots[nslots + i];
+      p1 = p1 + slots[nslots + i + kFinal];
+      p2 = p2 + slots[nslots + i + 2 * kFinal];
+      p3 = p3 + slots[nslots + i + 3 * kFinal];
+    }
+    for (; i < s1; i += kFinal) p0 = p0 + slots[nslots + i];
+    const double sum = (p0 + p1) + (p2 + p3);
     s_a[t] = sum;
     __syncthreads();
     for (int off = kFinal / 2; off >= 1; off >>= 1) {
