@@ -332,6 +332,31 @@ def serving_form(rates, per_rate):
     return out
 
 
+def parabolic_form(backend):
+    """Config 3: the README heat example (BDF2, Dt 0.002, TFinal 0.1,
+    RegridEvery 5) at BaseCells 32 / MaxLevels 3 and 128 / MaxLevels 4, with
+    the solution, source and BDF2 history resident on the device between
+    steps; composite mass drift per step."""
+    from bsam.parabolic import ebpProblem, ebpSolve
+    u0 = lambda x, y: 1 + 0.2 * np.cos(2 * np.pi * x) * np.cos(2 * np.pi * y)
+    prob = ebpProblem([0, 1, 0, 1], 1, 0, 0, ('neumann', 0), u0)
+    out = []
+    for base, ml in ((32, 3), (128, 4)):
+        t0 = time.perf_counter()
+        sol = ebpSolve(prob, 'Scheme', 'bdf2', 'Dt', 0.002, 'TFinal', 0.1, 'BaseCells', base, 'MaxLevels', ml,
+                       'RegridEvery', 5, 'StepVerbose', 0, backend=backend)
+        wall = time.perf_counter() - t0
+        m = sol['mass']
+        out.append({'BaseCells': base, 'MaxLevels': ml, 'steps': len(sol['cycles']), 'wall_s': wall,
+                    'steps_per_s': len(sol['cycles']) / wall, 'vcycles_total': int(np.sum(sol['cycles'])),
+                    'max_step_rel': float(np.max(sol['relres'])), 'regrids': sol['nregrids'],
+                    'mass_drift_per_step_max': float(np.max(np.abs(np.diff(m)))),
+                    'mass_drift_total': float(abs(m[-1] - m[0])),
+                    'final_levels': [lv['np'] for lv in sol['levels']]})
+    return {'workload': 'README heat example, BDF2, Dt 0.002, TFinal 0.1, RegridEvery 5 (wall time includes the '
+                        'host regrids)', 'runs': out}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -441,6 +466,7 @@ def main():
         forms['mixed']['speedup_vs_fp64'] = forms['mixed']['value'] / value
         if args.batch > 0:
             forms['batched'] = batched_form(backend, args.batch, max(3, args.steps // 4), args.warmup, flush, local)
+        forms['parabolic'] = parabolic_form(backend)
         rates = [float(r) for r in args.serve_rates.split(',') if r.strip()]
         if rates and rank == 0:
             forms['serving'] = serving_form(rates, 20)

@@ -23,6 +23,12 @@ from .flat import flatten, scatter_field, gather_field, FIELD_Q, FIELD_F, FIELD_
 P, I32, I64, D = C.c_void_p, C.c_int32, C.c_int64, C.c_double
 
 BSAM_FIELD_Q, BSAM_FIELD_F, BSAM_FIELD_FTRUE, BSAM_FIELD_QC, BSAM_FIELD_CC, BSAM_FIELD_INVDIAG = range(6)
+(BSAM_FIELD_DEW, BSAM_FIELD_DNS, BSAM_FIELD_PCOEF, BSAM_FIELD_CFD, BSAM_FIELD_BCG, BSAM_FIELD_AINV,
+ BSAM_FIELD_BCRHS, BSAM_FIELD_UO, BSAM_FIELD_UOO) = range(6, 15)
+# coefficient arrays of the flat tables replaced by an incremental upload
+COEF_FIELDS = (('DeW', BSAM_FIELD_DEW), ('DnS', BSAM_FIELD_DNS), ('CC', BSAM_FIELD_CC),
+               ('InvDiagS', BSAM_FIELD_INVDIAG), ('pcoef', BSAM_FIELD_PCOEF), ('cfd', BSAM_FIELD_CFD),
+               ('bcg', BSAM_FIELD_BCG), ('Ainv', BSAM_FIELD_AINV), ('bcRhs', BSAM_FIELD_BCRHS))
 NKINDS = 9
 KIND_NAMES = ['relax', 'ghost', 'restrict', 'ring', 'coarse_load', 'corrections', 'prolong', 'coarsest', 'residual']
 ERRNAMES = {1: 'arg', 2: 'cuda', 3: 'nomem', 4: 'state', 5: 'nodev'}
@@ -91,6 +97,8 @@ def lib():
         L.bsam_polygon_dist2.argtypes = [P, P, C.c_int, P, P, P, I64]
         L.bsam_device_memory.argtypes = [C.c_int, C.POINTER(I64), C.POINTER(I64)]
         L.bsam_setup_levels.argtypes = [P]
+        L.bsam_parabolic_rhs.argtypes = [P, C.c_int, D, P, I64]
+        L.bsam_history_push.argtypes = [P]
         _lib = L
     return _lib
 
@@ -212,6 +220,15 @@ class DevHier:
     def set_stop(self, inst, max_vcycles, rel_tol):
         check(lib().bsam_batch_set_stop(self.h, int(inst), int(max_vcycles), float(rel_tol)))
 
+    def parabolic_rhs(self, scheme, dt, f=None):
+        """FTrue of a BE (0) / BDF2 (1) step from the resident history."""
+        if f is not None:
+            f = np.ascontiguousarray(f, dtype=np.float64)
+        check(lib().bsam_parabolic_rhs(self.h, int(scheme), float(dt), _ptr(f), 0 if f is None else f.size))
+
+    def history_push(self):
+        check(lib().bsam_history_push(self.h))
+
     def setup_levels(self):
         """Run the deferred set-up steps (new-level prolongations, fills)."""
         check(lib().bsam_setup_levels(self.h))
@@ -310,22 +327,34 @@ class DeviceBackend:
             cls._instances[device] = cls(device)
         return cls._instances[device]
 
+    # the parabolic driver keeps its state (solution, BDF2 history, source)
+    # on the device between steps
+    resident = True
+
     def __init__(self, device=0):
         self.ctx = Context(device)
 
     def ensure(self, H):
         """The resident copy of H: re-uploaded after a structural change,
-        otherwise refreshed with the fields the host has modified."""
+        otherwise refreshed with the fields the host has modified ('coef':
+        every coefficient array, an incremental upload with no new plan)."""
         cur = getattr(H, '_dev', None)
         if cur is not None and cur[0] == H.version and cur[1].ctx is self.ctx:
             dh = cur[1]
             dh.set_opts(H.opts)
             for name in sorted(H.dirty):
+                if name == 'coef':
+                    fl = flatten(H)
+                    for attr, which in COEF_FIELDS:
+                        dh.set(which, np.asarray(getattr(fl, attr), dtype=np.float64).ravel())
+                    continue
                 which = {'Q': BSAM_FIELD_Q, 'F': BSAM_FIELD_F, 'FTrue': BSAM_FIELD_FTRUE,
                          'QC': BSAM_FIELD_QC}[name]
                 dh.set(which, gather_field(H, dh.fl, which))
             H.dirty.clear()
             return dh
+        if getattr(H, 'host_stale', False):
+            raise RuntimeError('bsam_device:stale: the host copy is older than the device state; sync_host first')
         fl = flatten(H)
         dh = DevHier(self.ctx, fl, H.opts)
         H._dev = (H.version, dh)
@@ -333,10 +362,67 @@ class DeviceBackend:
         return dh
 
     def _writeback(self, H, dh):
+        if H.par.get('resident') if isinstance(getattr(H, 'par', None), dict) else False:
+            H.host_stale = True          # the state stays on the device
+            return
         fl = dh.fl
         scatter_field(H, fl, FIELD_Q, dh.get(BSAM_FIELD_Q, fl.Q.size))
         scatter_field(H, fl, FIELD_QC, dh.get(BSAM_FIELD_QC, fl.QC.size))
         scatter_field(H, fl, FIELD_F, dh.get(BSAM_FIELD_F, fl.F.size))
+        H.host_stale = False
+
+    def sync_host(self, H):
+        """Copy the device state of a resident hierarchy back to H."""
+        if not getattr(H, 'host_stale', False):
+            return
+        dh = H._dev[1]
+        fl = dh.fl
+        scatter_field(H, fl, FIELD_Q, dh.get(BSAM_FIELD_Q, fl.Q.size))
+        scatter_field(H, fl, FIELD_QC, dh.get(BSAM_FIELD_QC, fl.QC.size))
+        scatter_field(H, fl, FIELD_F, dh.get(BSAM_FIELD_F, fl.F.size))
+        scatter_field(H, fl, 2, dh.get(BSAM_FIELD_FTRUE, fl.F.size))
+        H.host_stale = False
+
+    # ---- parabolic steps on the resident hierarchy --------------------------
+    def _cells(self, H, dh, arrays):
+        """Flat cell array from per-patch arrays {(k, p): (mx, my)}."""
+        from .flat import PD_COFF
+        out = np.zeros(dh.fl.F.size)
+        for (k, p), g in dh.fl.pglob.items():
+            a = arrays.get((k, p))
+            if a is None:
+                continue
+            o = int(dh.fl.patches[g][PD_COFF])
+            out[o:o + a.size] = np.asarray(a, dtype=np.float64).ravel(order='F')
+        return out
+
+    def parabolic_rhs(self, H, scheme, dt, f_patches=None):
+        dh = self.ensure(H)
+        f = None if f_patches is None else self._cells(H, dh, f_patches)
+        dh.parabolic_rhs({'be': 0, 'bdf2': 1}[scheme], dt, f)
+
+    def history_push(self, H):
+        self.ensure(H).history_push()
+
+    def history_get(self, H):
+        """(Uo, Uoo) as per-patch arrays {(k, p): (mx, my)}."""
+        from .flat import PD_COFF, PD_MX, PD_MY
+        dh = self.ensure(H)
+        out = []
+        for which in (BSAM_FIELD_UO, BSAM_FIELD_UOO):
+            v = dh.get(which, dh.fl.F.size)
+            d = {}
+            for (k, p), g in dh.fl.pglob.items():
+                r = dh.fl.patches[g]
+                mx, my, o = int(r[PD_MX]), int(r[PD_MY]), int(r[PD_COFF])
+                d[(k, p)] = v[o:o + mx * my].reshape((mx, my), order='F').copy(order='F')
+            out.append(d)
+        return out[0], out[1]
+
+    def history_set(self, H, Uo, Uoo):
+        dh = self.ensure(H)
+        dh.set(BSAM_FIELD_UO, self._cells(H, dh, Uo))
+        dh.set(BSAM_FIELD_UOO, self._cells(H, dh, Uoo or {}))
 
     def run(self, H, ops):
         dh = self.ensure(H)

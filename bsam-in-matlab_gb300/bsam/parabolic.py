@@ -49,6 +49,7 @@ def ebpProblem(domain, D, C, f, bc, u0, exact=None) -> Problem:
     p.D, p.tdD = _wrapT(D, 'D')
     p.C, p.tdC = _wrapT(C, 'C')
     p.f, p.tdF = _wrapT(f, 'f')
+    p.fzero = np.isscalar(f) and float(f) == 0.0    # lets a device step skip sampling f
     if isinstance(bc, (list, tuple)) and len(bc) == 2 and isinstance(bc[0], str):
         bc = {s: bc for s in SIDES}
     p.tdBC = False
@@ -251,7 +252,8 @@ def ebpSetTime(H, pprob, t, aDt, force=False):
     hier.coarsest_assemble(H)
     H.par['stateKey'] = key
     H.par['aDt'] = aDt
-    H.touch()
+    # same hierarchy, new coefficients: an incremental upload, no new plan
+    H.mark_dirty('coef')
     return H
 
 
@@ -378,6 +380,23 @@ def ebpSolve(pprob, *args, backend=None, **kwargs):
     Dt = opts.TFinal / nsteps
     scheme1 = 'be' if opts.Scheme == 'bdf2' else opts.Scheme
     H = ebpInit(pprob, opts, _alpha(scheme1) / Dt, backend)
+    # a device backend keeps the solution, the source and the BDF2 history
+    # resident between steps; they come to the host only for a regrid, a
+    # callback, a Crank-Nicolson right-hand side and the result
+    dev = getattr(backend, 'resident', False)
+
+    def to_device(H):
+        H.par['resident'] = True
+        backend.history_set(H, H.par['Uo'], H.par['Uoo'])
+
+    def to_host(H):
+        backend.sync_host(H)
+        H.par['Uo'], uoo = backend.history_get(H)
+        H.par['Uoo'] = uoo if H.par.get('hasUoo') else None
+        H.par['resident'] = False
+
+    if dev:
+        to_device(H)
 
     def comp_mass(H):
         m, vol = backend.composite_mean(H)
@@ -391,25 +410,53 @@ def ebpSolve(pprob, *args, backend=None, **kwargs):
     for n in range(1, nsteps + 1):
         t1 = n * Dt
         scheme = scheme1 if n == 1 else opts.Scheme
-        H = ebpRhs(H, pprob, t1, Dt, scheme, backend)
+        if dev and scheme in ('be', 'bdf2'):
+            fp = None
+            if not pprob.get('fzero'):
+                fp = {(k, p): pprob.f(*_centres(H, k, p), t1) for k in range(H.rootIdx, H.nlev + 1)
+                      for p in range(H.lev[k].np)}
+                fp = {kp: np.broadcast_to(v, _centres(H, *kp)[0].shape) for kp, v in fp.items()}
+            backend.parabolic_rhs(H, scheme, Dt, fp)
+        elif dev:
+            to_host(H)
+            H = ebpRhs(H, pprob, t1, Dt, scheme, backend)
+            to_device(H)
+        else:
+            H = ebpRhs(H, pprob, t1, Dt, scheme, backend)
         H = ebpSetTime(H, pprob, t1, _alpha(scheme) / Dt)
         H = ebSolveCycles(H, backend)
         st = H.stats['stages'][-1]
         cycles[n - 1] = st['vcycles']
         relres[n - 1] = st['finalRel']
-        H.par['Uoo'] = H.par['Uo']
-        H.par['Uo'] = _interiors(H)
+        if dev:
+            backend.history_push(H)
+            H.par['hasUoo'] = True
+        else:
+            H.par['Uoo'] = H.par['Uo']
+            H.par['Uo'] = _interiors(H)
         mass[n] = comp_mass(H)
         if opts.Callback is not None:
-            opts.Callback(H, t1, n)
+            if dev:
+                to_host(H)
+                opts.Callback(H, t1, n)
+                to_device(H)
+            else:
+                opts.Callback(H, t1, n)
         sv = int(opts.StepVerbose)
         if sv > 0 and (n % sv == 0 or n == nsteps):
             nc = sum(f.size for k in range(H.rootIdx, H.nlev + 1) for f in H.lev[k].FTrue)
             print(f'[ebsam-p] step {n:4d}/{nsteps}  t={t1:.4f}  V={cycles[n - 1]}  rel={relres[n - 1]:.1e}  '
                   f'levels={H.nlev - H.rootIdx + 1}  cells={nc}  mass={mass[n]:.6e}')
         if opts.RegridEvery > 0 and n % int(opts.RegridEvery) == 0 and n < nsteps and opts.eb.MaxLevels > 1:
+            if dev:
+                to_host(H)
             H = ebpRegrid(H, pprob, t1, _alpha(opts.Scheme) / Dt, opts, backend)
             nregrids += 1
+            if dev:
+                H.par['hasUoo'] = H.par['Uoo'] is not None
+                to_device(H)
+    if dev:
+        to_host(H)
     sol = {'H': H, 't': np.arange(nsteps + 1) * Dt, 'mass': mass, 'cycles': cycles, 'relres': relres,
            'nregrids': nregrids, 'stats': H.stats}
     if pprob.exact is not None:

@@ -135,6 +135,7 @@ struct bsam_hier_s {
   // the smoother's face coefficients: on levels whose h^2 is a power of two
   // pre-multiplied by the exact 1/h^2 (k_relax<T, true>), else as uploaded
   DBuf<double> DeWr, DnSr;
+  DBuf<double> Uo, Uoo, fsrc;      // parabolic history (cells) and f staging
   bool f32_dirty = true;
   DecompH all_cells;               // every cell of every level (batch force reset)
   std::vector<InstRes> hir;        // host copy of the per-instance reduction plan
@@ -1158,7 +1159,7 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
 void release(bsam_hier h) {
   drop_graph(h);
   for (DBuf<double> *b : {&h->Q, &h->F, &h->FTrue, &h->QC, &h->CC, &h->ID, &h->DeW, &h->DnS, &h->bcg, &h->cfd,
-                          &h->pcoef, &h->Ainv, &h->bcRhs, &h->slots, &h->partials, &h->hist, &h->saveQ, &h->saveQC, &h->DeWr, &h->DnSr,
+                          &h->pcoef, &h->Ainv, &h->bcRhs, &h->slots, &h->partials, &h->hist, &h->saveQ, &h->saveQC, &h->DeWr, &h->DnSr, &h->Uo, &h->Uoo, &h->fsrc,
                           &h->saveF})
     b->release();
   for (DBuf<float> *b : {&h->E, &h->F32, &h->QC32, &h->DeW32, &h->DnS32, &h->CC32, &h->ID32, &h->pcoef32, &h->cfd32,
@@ -1279,6 +1280,16 @@ int bsam_set_opts(bsam_hier h, const bsam_solve_opts *opts) {
   return apply_opts(h);
 }
 
+static int ensure_history(bsam_hier h) {
+  int rc;
+  if (!h->Uo.p) {
+    if ((rc = h->Uo.alloc(h->n_cells)) || (rc = h->Uoo.alloc(h->n_cells))) return rc;
+    CK(cudaMemsetAsync(h->Uo.p, 0, sizeof(double) * h->n_cells, h->stream));
+    CK(cudaMemsetAsync(h->Uoo.p, 0, sizeof(double) * h->n_cells, h->stream));
+  }
+  return BSAM_OK;
+}
+
 static DBuf<double> *field_buf(bsam_hier h, int which) {
   switch (which) {
     case BSAM_FIELD_Q: return &h->Q;
@@ -1287,30 +1298,63 @@ static DBuf<double> *field_buf(bsam_hier h, int which) {
     case BSAM_FIELD_QC: return &h->QC;
     case BSAM_FIELD_CC: return &h->CC;
     case BSAM_FIELD_INVDIAG: return &h->ID;
+    case BSAM_FIELD_DEW: return &h->DeW;
+    case BSAM_FIELD_DNS: return &h->DnS;
+    case BSAM_FIELD_PCOEF: return &h->pcoef;
+    case BSAM_FIELD_CFD: return &h->cfd;
+    case BSAM_FIELD_BCG: return &h->bcg;
+    case BSAM_FIELD_AINV: return &h->Ainv;
+    case BSAM_FIELD_BCRHS: return &h->bcRhs;
+    case BSAM_FIELD_UO: return ensure_history(h) ? nullptr : &h->Uo;
+    case BSAM_FIELD_UOO: return ensure_history(h) ? nullptr : &h->Uoo;
     default: return nullptr;
   }
 }
 
+// the smoother's scaled copy of a face-coefficient array after its update
+static int rescale_faces(bsam_hier h, int which, const double *host) {
+  const bool x = which == BSAM_FIELD_DEW;
+  std::vector<double> v(host, host + (x ? h->DeW.n : h->DnS.n));
+  for (int k = 1; k <= h->nlev; ++k) {
+    const LevelPlan &L = h->lev[k];
+    if (!L.pow2) continue;
+    const double s = x ? 1.0 / (L.hx * L.hx) : 1.0 / (L.hy * L.hy);
+    for (int p = L.p0; p < L.p1; ++p) {
+      const int32_t *r = h->hpatches.data() + (size_t)p * PDN;
+      const int64_t off = x ? r[PD_DEWOFF] : r[PD_DNSOFF];
+      const int64_t n = x ? (int64_t)(r[PD_MX] + 1) * r[PD_MY] : (int64_t)r[PD_MX] * (r[PD_MY] + 1);
+      for (int64_t i = 0; i < n; ++i) v[off + i] *= s;
+    }
+  }
+  DBuf<double> &dst = x ? h->DeWr : h->DnSr;
+  CK(cudaMemcpyAsync(dst.p, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
 int bsam_set_field(bsam_hier h, int which, const double *host, int64_t n) {
   if (!h || !host) return fail(BSAM_ERR_ARG, "null argument");
+  int rc = set_device(h);
+  if (rc) return rc;
   DBuf<double> *b = field_buf(h, which);
   if (!b) return fail(BSAM_ERR_ARG, "unknown field");
   if ((size_t)n != b->n) return fail(BSAM_ERR_ARG, "field length mismatch");
-  int rc = set_device(h);
-  if (rc) return rc;
-  if (n) CK(cudaMemcpyAsync(b->p, host, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    if (n) CK(cudaMemcpyAsync(b->p, host, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  if (which == BSAM_FIELD_CC || which == BSAM_FIELD_INVDIAG) h->f32_dirty = true;
+  if (which == BSAM_FIELD_DEW || which == BSAM_FIELD_DNS) {
+    if ((rc = rescale_faces(h, which, host))) return rc;
+  }
+  if (which >= BSAM_FIELD_CC && which <= BSAM_FIELD_BCRHS) h->f32_dirty = true;
   return BSAM_OK;
 }
 
 int bsam_get_field(bsam_hier h, int which, double *host, int64_t n) {
   if (!h || !host) return fail(BSAM_ERR_ARG, "null argument");
+  int rc = set_device(h);
+  if (rc) return rc;
   DBuf<double> *b = field_buf(h, which);
   if (!b) return fail(BSAM_ERR_ARG, "unknown field");
   if ((size_t)n != b->n) return fail(BSAM_ERR_ARG, "field length mismatch");
-  int rc = set_device(h);
-  if (rc) return rc;
   if (n) CK(cudaMemcpyAsync(host, b->p, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return BSAM_OK;
@@ -1376,6 +1420,38 @@ int bsam_setup_levels(bsam_hier h) {
     }
     launch_fill(h, k);
   }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
+int bsam_parabolic_rhs(bsam_hier h, int scheme, double dt, const double *f, int64_t n) {
+  if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
+  if ((scheme != 0 && scheme != 1) || !(dt > 0)) return fail(BSAM_ERR_ARG, "bad scheme or time step");
+  if (f && n != h->n_cells) return fail(BSAM_ERR_ARG, "source length mismatch");
+  int rc = set_device(h);
+  if (rc || (rc = ensure_history(h))) return rc;
+  if (f) {
+    if (!h->fsrc.p && (rc = h->fsrc.alloc(h->n_cells))) return rc;
+    CK(cudaMemcpyAsync(h->fsrc.p, f, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+  }
+  Decomp D = decomp(h, h->all_cells);
+  launch_k(h, k_prhs, D.nblocks, kBlock, D, (const PatchD *)h->patches.p, h->FTrue.p,
+           (const double *)(f ? h->fsrc.p : nullptr), (const double *)h->Uo.p, (const double *)h->Uoo.p, dt, scheme);
+  h->launch_count++;
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
+int bsam_history_push(bsam_hier h) {
+  if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
+  int rc = set_device(h);
+  if (rc || (rc = ensure_history(h))) return rc;
+  Decomp D = decomp(h, h->all_cells);
+  launch_k(h, k_history, D.nblocks, kBlock, D, (const PatchD *)h->patches.p, (const double *)h->Q.p, h->Uo.p,
+           h->Uoo.p);
+  h->launch_count++;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(h->stream));
   return BSAM_OK;

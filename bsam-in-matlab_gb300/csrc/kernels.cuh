@@ -920,6 +920,38 @@ __global__ void __launch_bounds__(kBlock) k_update(Decomp D, const PatchD *__res
   Q[qi] = Q[qi] + (double)E[qi];
 }
 
+// Parabolic driver on the device.  k_history: Uoo = Uo, Uo = interior of Q
+// (ebpSolve.m:52-56).  k_prhs: FTrue of the step on the cells of levels at
+// or above the root (ebpRhs.m:25-47): BE f + Uo/Dt, BDF2 f + (2 Uo - 0.5
+// Uoo)/Dt, in that operation order; f null is f = 0.
+__global__ void __launch_bounds__(kBlock) k_history(Decomp D, const PatchD *__restrict__ patches, const double *Q,
+                                                    double *Uo, double *Uoo) {
+  chain_in();
+  const int g = blockIdx.x * kBlock + threadIdx.x;
+  if (g >= D.n) return;
+  const int p = find_patch(D, blockIdx.x, g);
+  const PatchD &P = patches[p];
+  const int s = g - __ldg(D.beg + p);
+  const int lj = s / P.mx, lx = s - lj * P.mx;
+  const int cc = P.c_off + s;
+  Uoo[cc] = Uo[cc];
+  Uo[cc] = Q[P.q_off + (lx + 1) + (lj + 1) * (P.mx + 2)];
+}
+
+__global__ void __launch_bounds__(kBlock) k_prhs(Decomp D, const PatchD *__restrict__ patches, double *FTrue,
+                                                 const double *__restrict__ fsrc, const double *__restrict__ Uo,
+                                                 const double *__restrict__ Uoo, double dt, int bdf2) {
+  chain_in();
+  const int g = blockIdx.x * kBlock + threadIdx.x;
+  if (g >= D.n) return;
+  const int p = find_patch(D, blockIdx.x, g);
+  const PatchD &P = patches[p];
+  if (!(P.pflags & 1)) return;               // below the root
+  const int cc = P.c_off + (g - __ldg(D.beg + p));
+  const double f = fsrc ? fsrc[cc] : 0.0;
+  FTrue[cc] = bdf2 ? f + (2 * Uo[cc] - 0.5 * Uoo[cc]) / dt : f + Uo[cc] / dt;
+}
+
 // FP32 copy of an FP64 array (coefficient copies of the mixed form)
 __global__ void __launch_bounds__(kBlock) k_to_f32(const double *__restrict__ a, float *__restrict__ b, long long n) {
   chain_in();

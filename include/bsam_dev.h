@@ -44,6 +44,19 @@ extern "C" {
 #define BSAM_FIELD_QC 3     /* padded coarse shadows (levels >= 2)          */
 #define BSAM_FIELD_CC 4     /* reaction coefficient (cells)                 */
 #define BSAM_FIELD_INVDIAG 5 /* relaxation diagonal InvDiagS (cells)        */
+/* coefficient arrays (incremental upload: the execution plan depends on the
+ * hierarchy's structure only, so new coefficients of an unchanged hierarchy
+ * -- ebpSetTime.m:11-55 -- replace these arrays without a new upload)     */
+#define BSAM_FIELD_DEW 6     /* x-face D                                     */
+#define BSAM_FIELD_DNS 7     /* y-face D                                     */
+#define BSAM_FIELD_PCOEF 8   /* parent coefficients over each footprint      */
+#define BSAM_FIELD_CFD 9     /* coarse interface D                           */
+#define BSAM_FIELD_BCG 10    /* boundary data                                */
+#define BSAM_FIELD_AINV 11   /* coarsest inverse blocks                      */
+#define BSAM_FIELD_BCRHS 12  /* coarsest boundary right-hand side            */
+/* BDF2 history of the parabolic driver (cells), resident on the device     */
+#define BSAM_FIELD_UO 13     /* u at t_n                                     */
+#define BSAM_FIELD_UOO 14    /* u at t_{n-1}                                 */
 
 typedef struct bsam_ctx_s *bsam_ctx;
 typedef struct bsam_hier_s *bsam_hier;
@@ -156,6 +169,15 @@ int bsam_batch_result(bsam_hier h, int inst, double *res_hist, int hist_cap, int
 /* Stop test (MaxVCycles, RelTol) of one instance of a batch; bsam_set_opts
  * sets every instance's to the options' values. */
 int bsam_batch_set_stop(bsam_hier h, int inst, int max_vcycles, double rel_tol);
+
+/* Parabolic step on the device (ParabolicBSAM, kept resident across steps).
+ * bsam_parabolic_rhs: ebpRhs.m:25-47 for scheme 0 = BE, FTrue = f + Uo/Dt,
+ * or 1 = BDF2, FTrue = f + (2 Uo - 0.5 Uoo)/Dt, on every cell of the levels
+ * at or above the root; f (cells, host) may be NULL for f = 0.
+ * bsam_history_push: after a step's solve, Uoo = Uo, Uo = the interior of
+ * Q on every level (ebpSolve.m:52-56). */
+int bsam_parabolic_rhs(bsam_hier h, int scheme, double dt, const double *f, int64_t n);
+int bsam_history_push(bsam_hier h);
 
 /* One ebVcycle(H, nlev) + ebTransfer(H,0,'filldown') (ebVcycle.m:16-35,
  * ebTransfer.m:73-79), force reset included (ebSolveCycles.m:30-34). */
