@@ -99,6 +99,7 @@ def lib():
         L.bsam_setup_levels.argtypes = [P]
         L.bsam_parabolic_rhs.argtypes = [P, C.c_int, D, P, I64]
         L.bsam_history_push.argtypes = [P]
+        L.bsam_tag_level.argtypes = [P, C.c_int, C.c_int, D, C.c_int, C.c_int, C.c_int, P]
         _lib = L
     return _lib
 
@@ -228,6 +229,13 @@ class DevHier:
 
     def history_push(self):
         check(lib().bsam_history_push(self.h))
+
+    def tag_level(self, level, indicator, threshold, buffer, n0, n1):
+        """Buffered, cover-limited tag mask of a level, shape (n0, n1)."""
+        out = np.zeros(int(n0) * int(n1), dtype=np.uint8)
+        check(lib().bsam_tag_level(self.h, int(level), {'ulap': 0, 'rte': 1}[indicator], float(threshold),
+                                   int(buffer), int(n0), int(n1), _ptr(out)))
+        return out.reshape(int(n0), int(n1)).astype(bool)
 
     def setup_levels(self):
         """Run the deferred set-up steps (new-level prolongations, fills)."""
@@ -403,6 +411,12 @@ class DeviceBackend:
 
     def history_push(self, H):
         self.ensure(H).history_push()
+
+    def tag_mask(self, H, indicator, threshold, buffer):
+        """ebTagCluster's tag mask of the finest level computed on the device."""
+        dh = self.ensure(H)
+        n = H.lev[H.nlev].n
+        return dh.tag_level(H.nlev, indicator, threshold, buffer, n[0], n[1])
 
     def history_get(self, H):
         """(Uo, Uoo) as per-patch arrays {(k, p): (mx, my)}."""

@@ -86,7 +86,7 @@ def final_stage(prob, opts_dict, backend, tree=False):
         if (H.nlev - H.rootIdx + 1) >= opts.MaxLevels:
             return fl, H
         H = ebSolveCycles(H, backend)
-        boxes = tag_cluster(H)
+        boxes = tag_cluster(H, backend)
         if boxes.shape[0] == 0:
             return fl, H
         H = hier.add_level(H, boxes, backend)

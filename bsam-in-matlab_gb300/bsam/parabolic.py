@@ -137,7 +137,7 @@ def ebpInit(pprob, opts, aDt1, backend):
     _set_u0(H, pprob, range(1, H.nlev + 1))
     backend.run(H, [('fill', k) for k in range(1, H.nlev + 1)])
     while (H.nlev - H.rootIdx + 1) < opts.eb.MaxLevels:
-        boxes = tag_cluster(H)
+        boxes = tag_cluster(H, backend)
         if boxes.shape[0] == 0:
             break
         H = hier.add_level(H, boxes, backend)
@@ -323,7 +323,7 @@ def ebpRegrid(Hold, pprob, t, aDtNext, opts, backend):
     Hn.mark_dirty('Q')
     backend.run(Hn, [('fill', k) for k in range(1, r + 1)])
     while (Hn.nlev - Hn.rootIdx + 1) < opts.eb.MaxLevels:
-        boxes = tag_cluster(Hn)
+        boxes = tag_cluster(Hn, backend)
         if boxes.shape[0] == 0:
             break
         Hn = hier.add_level(Hn, boxes, backend)

@@ -68,7 +68,7 @@ def build_hierarchy(prob, opts, backend, tree=False):
     level until MaxLevels (``ebSolve.m:30-37``); no solve."""
     H = hier.setup(prob, opts, backend, tree=tree)
     while (H.nlev - H.rootIdx + 1) < opts.MaxLevels:
-        boxes = tag_cluster(H)
+        boxes = tag_cluster(H, backend)
         if boxes.shape[0] == 0:
             break
         H = hier.add_level(H, boxes, backend)
@@ -84,7 +84,7 @@ def _solve(prob, args, kwargs, tree, backend):
     H = hier.setup(prob, opts, backend, tree=tree)
     if str(opts.Indicator).lower() == 'fun':
         while (H.nlev - H.rootIdx + 1) < opts.MaxLevels:
-            boxes = tag_cluster(H)
+            boxes = tag_cluster(H, backend)
             if boxes.shape[0] == 0:
                 break
             H = hier.add_level(H, boxes, backend)
@@ -92,7 +92,7 @@ def _solve(prob, args, kwargs, tree, backend):
     else:
         H = ebSolveCycles(H, backend)
         while (H.nlev - H.rootIdx + 1) < opts.MaxLevels:
-            boxes = tag_cluster(H)
+            boxes = tag_cluster(H, backend)
             if boxes.shape[0] == 0:
                 if opts.Verbose >= 1:
                     print(f'[ebsam] no cells tagged; stopping at {H.nlev - H.rootIdx + 1} AMR level(s)')

@@ -292,9 +292,12 @@ def rte_indicator(H, k, p):
     return np.repeat(np.repeat(np.abs(tau), 2, axis=0), 2, axis=1)
 
 
-def tag_cluster(H):
+def tag_cluster(H, backend=None):
     """``ebTagCluster`` / ``ebtTagCluster``: boxes (nb x 4, or nb x 5 with the
-    1-based parent index first for the tree form) for a new finest level."""
+    1-based parent index first for the tree form) for a new finest level.
+    With a device backend the solution-driven indicators ('ulap', 'rte')
+    and the buffering run on the GPU, where the solution is, and only the
+    tag mask comes back."""
     opts = H.opts
     k = H.nlev
     lev = H.lev[k]
@@ -302,7 +305,14 @@ def tag_cluster(H):
     T = np.zeros((n[0], n[1]), dtype=bool)
     dom = H.prob.domain
     ind = str(opts.Indicator).lower()
-    for p in range(lev.np):
+    device = backend is not None and hasattr(backend, 'tag_mask') and ind in ('ulap', 'rte') and \
+        not (ind == 'rte' and k == 1)
+    if device:
+        thr = opts.TagThreshold
+        if callable(thr):
+            thr = thr(k - H.rootIdx + 1)
+        T = backend.tag_mask(H, ind, float(thr), int(opts.TagBuffer))
+    for p in range(0 if device else lev.np):
         b = [int(v) for v in lev.box[p]]
         if ind == 'fun':
             if opts.TagFunction is None:
@@ -333,13 +343,14 @@ def tag_cluster(H):
         else:
             raise ValueError(f'eb_tag_cluster:ind: unknown Indicator {opts.Indicator}')
         T[b[0] - 1:b[1], b[2] - 1:b[3]] |= tp
-    T = _dilate(T, int(opts.TagBuffer))
     cover = np.zeros((n[0], n[1]), dtype=bool)
     for p in range(lev.np):
         b = lev.box[p]
         cover[b[0] - 1:b[1], b[2] - 1:b[3]] = True
     allowed = _erode8(cover)
-    T &= allowed
+    if not device:
+        T = _dilate(T, int(opts.TagBuffer))
+        T &= allowed
     ncol = 5 if H.tree else 4
     if not T.any():
         return np.zeros((0, ncol), dtype=np.int64)

@@ -917,7 +917,8 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
     q.inst = pinst[p];
     const int root = h->inst_root[q.inst];
     q.pflags = (q.level >= root ? 1 : 0) | (q.level >= std::max(2, root + 1) ? 2 : 0);
-    q.pad0 = q.pad1 = 0;
+    q.ilo = r[PD_ILO];
+    q.jlo = r[PD_JLO];
   }
   // plan
   Builder B{h, d};
@@ -1454,6 +1455,46 @@ int bsam_history_push(bsam_hier h) {
   h->launch_count++;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
+int bsam_tag_level(bsam_hier h, int level, int indicator, double threshold, int buffer, int n0, int n1,
+                   uint8_t *mask) {
+  if (!h || !mask) return fail(BSAM_ERR_ARG, "null argument");
+  if (level < 1 || level > h->nlev || (level == 1 && indicator == 1)) return fail(BSAM_ERR_ARG, "level out of range");
+  if (indicator != 0 && indicator != 1) return fail(BSAM_ERR_ARG, "unknown indicator");
+  if (h->ninst > 1) return fail(BSAM_ERR_STATE, "tagging runs on a single hierarchy, not a batch");
+  if (n0 < 1 || n1 < 1 || buffer < 0) return fail(BSAM_ERR_ARG, "bad tag grid");
+  const LevelPlan &L = h->lev[level];
+  for (int p = L.p0; p < L.p1; ++p) {
+    const int32_t *r = h->hpatches.data() + (size_t)p * PDN;
+    if (r[PD_ILO] < 1 || r[PD_IHI] > n0 || r[PD_JLO] < 1 || r[PD_JHI] > n1)
+      return fail(BSAM_ERR_ARG, "patch box outside the tag grid");
+  }
+  int rc = set_device(h);
+  if (rc) return rc;
+  const size_t n = (size_t)n0 * n1;
+  uint8_t *buf = nullptr;
+  CK(cudaMalloc(&buf, 3 * n));
+  uint8_t *T = buf, *cover = buf + n, *out = buf + 2 * n;
+  cudaError_t e = cudaMemsetAsync(buf, 0, 2 * n, h->stream);
+  if (e == cudaSuccess) {
+    if (indicator == 0) {
+      Decomp D = decomp(h, L.cell);
+      k_tag_ulap<<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, level), D, (const double *)h->Q.p, threshold, T, cover,
+                                                      n1);
+    } else {
+      Decomp D = decomp(h, L.coarse);
+      k_tag_rte<<<D.nblocks, kBlock, 0, h->stream>>>(leveld(h, level), D, fields(h), threshold, T, cover, n1);
+    }
+    k_tag_buffer<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, h->stream>>>(T, cover, out, n0, n1, buffer);
+    h->launch_count += 2;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(mask, out, n, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_fail(e, "bsam_tag_level");
   return BSAM_OK;
 }
 

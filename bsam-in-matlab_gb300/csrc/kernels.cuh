@@ -44,7 +44,7 @@ struct PatchD {
   int inst;                    // instance of a batch (0 for a single hierarchy)
   int pflags;                  // bit0: level >= the instance's root (in the norms)
                                // bit1: QC refreshed by the residual (level >= root+1)
-  int pad0, pad1;
+  int ilo, jlo;                // 1-based origin of the patch box in the level's index space
 };
 
 // the arrays one V-cycle works on, in its value type T: the FP64 solve
@@ -950,6 +950,102 @@ __global__ void __launch_bounds__(kBlock) k_prhs(Decomp D, const PatchD *__restr
   const int cc = P.c_off + (g - __ldg(D.beg + p));
   const double f = fsrc ? fsrc[cc] : 0.0;
   FTrue[cc] = bdf2 ? f + (2 * Uo[cc] - 0.5 * Uoo[cc]) / dt : f + Uo[cc] / dt;
+}
+
+// ---------------------------------------------------------------------------
+// Tagging indicators on the device (ebTagCluster.m:50-59 'ulap',
+// ebRte.m:14-41 'rte'), on the finest level's index space (n0 x n1, stored
+// i-major: index i * n1 + j).  Only the final mask goes to the host, where
+// Berger-Rigoutsos clustering runs.  The arithmetic is the host
+// restatement's, in its order, so the masks are identical.
+__global__ void __launch_bounds__(kBlock) k_tag_ulap(LevelD L, Decomp D, const double *__restrict__ Q, double thr,
+                                                     uint8_t *T, uint8_t *cover, int n1) {
+  const int g = blockIdx.x * kBlock + threadIdx.x;
+  if (g >= D.n) return;
+  const int p = find_patch(D, blockIdx.x, g);
+  const PatchD &P = L.patches[p];
+  const int s = g - __ldg(D.beg + p);
+  const int lj = s / P.mx, li = s - lj * P.mx;
+  const int ldq = P.mx + 2;
+  const double *q = Q + P.q_off + (li + 1) + (lj + 1) * ldq;
+  const double sdx = (q[1] - 2 * q[0]) + q[-1];
+  const double sdy = (q[ldq] - 2 * q[0]) + q[-ldq];
+  const double v = sqrt(sdx * sdx + sdy * sdy);
+  const size_t o = (size_t)(P.ilo - 1 + li) * n1 + (P.jlo - 1 + lj);
+  cover[o] = 1;
+  if (v > thr) T[o] = 1;
+}
+
+// relative truncation error: |op_2h(R u) - R(op_h u)| per coarse cell,
+// spread to its four fine cells
+__global__ void __launch_bounds__(kBlock) k_tag_rte(LevelD L, Decomp D, Fields f, double thr, uint8_t *T,
+                                                    uint8_t *cover, int n1) {
+  const int g = blockIdx.x * kBlock + threadIdx.x;
+  if (g >= D.n) return;
+  const int p = find_patch(D, blockIdx.x, g);
+  const PatchD &P = L.patches[p];
+  const int mx = P.mx, my = P.my, cmx = mx >> 1, cmy = my >> 1, ldq = mx + 2;
+  const int s = g - __ldg(D.beg + p);
+  const int cj = s / cmx, ci = s - cj * cmx;
+  const double *Q = f.Q + P.q_off, *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off, *CC = f.CC + P.c_off;
+  double Lf[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int li = 2 * ci + (t & 1), lj = 2 * cj + (t >> 1);
+    Lf[t] = op_cell_r(Q, ldq, DeW, DnS, CC[li + lj * mx], mx, li, lj, L);
+  }
+  const double RL = 0.25 * (((Lf[0] + Lf[1]) + Lf[2]) + Lf[3]);
+  // the restricted solution and its ghost frame (pair averages of fine ghosts)
+  const double rc = restrict_cell(Q, ldq, ci, cj);
+  const double re = ci + 1 < cmx ? restrict_cell(Q, ldq, ci + 1, cj)
+                                 : 0.5 * (Q[(mx + 1) + (2 * cj + 1) * ldq] + Q[(mx + 1) + (2 * cj + 2) * ldq]);
+  const double rw = ci > 0 ? restrict_cell(Q, ldq, ci - 1, cj) : 0.5 * (Q[(2 * cj + 1) * ldq] + Q[(2 * cj + 2) * ldq]);
+  const double rn = cj + 1 < cmy ? restrict_cell(Q, ldq, ci, cj + 1)
+                                 : 0.5 * (Q[(2 * ci + 1) + (my + 1) * ldq] + Q[(2 * ci + 2) + (my + 1) * ldq]);
+  const double rs = cj > 0 ? restrict_cell(Q, ldq, ci, cj - 1) : 0.5 * (Q[2 * ci + 1] + Q[2 * ci + 2]);
+  // averaged coarse coefficients
+  const double cE = 0.5 * (DeW[(2 * ci + 2) + (2 * cj) * (mx + 1)] + DeW[(2 * ci + 2) + (2 * cj + 1) * (mx + 1)]);
+  const double cW = 0.5 * (DeW[(2 * ci) + (2 * cj) * (mx + 1)] + DeW[(2 * ci) + (2 * cj + 1) * (mx + 1)]);
+  const double cN = 0.5 * (DnS[(2 * ci) + (2 * cj + 2) * mx] + DnS[(2 * ci + 1) + (2 * cj + 2) * mx]);
+  const double cS = 0.5 * (DnS[(2 * ci) + (2 * cj) * mx] + DnS[(2 * ci + 1) + (2 * cj) * mx]);
+  const double cC = 0.25 * (((CC[2 * ci + 2 * cj * mx] + CC[2 * ci + 1 + 2 * cj * mx]) + CC[2 * ci + (2 * cj + 1) * mx]) +
+                            CC[2 * ci + 1 + (2 * cj + 1) * mx]);
+  const double H2x = (2 * L.hx) * (2 * L.hx), H2y = (2 * L.hy) * (2 * L.hy);
+  const double feE = cE * (re - rc), feW = cW * (rc - rw), fnN = cN * (rn - rc), fnS = cS * (rc - rs);
+  const double tau = ((-(feE - feW)) / H2x - (fnN - fnS) / H2y + cC * rc) - RL;
+  const bool tag = fabs(tau) > thr;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int li = 2 * ci + (t & 1), lj = 2 * cj + (t >> 1);
+    const size_t o = (size_t)(P.ilo - 1 + li) * n1 + (P.jlo - 1 + lj);
+    cover[o] = 1;
+    if (tag) T[o] = 1;
+  }
+}
+
+// dilate by b cells (outside the index space counts as untagged), then keep
+// what the 8-eroded patch cover allows (outside counts as covered)
+__global__ void __launch_bounds__(kBlock) k_tag_buffer(const uint8_t *__restrict__ T, const uint8_t *__restrict__ cover,
+                                                       uint8_t *out, int n0, int n1, int b) {
+  const long long g = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (g >= (long long)n0 * n1) return;
+  const int i = (int)(g / n1), j = (int)(g - (long long)i * n1);
+  bool t = false;
+  for (int dx = -b; dx <= b && !t; ++dx)
+    for (int dy = -b; dy <= b; ++dy) {
+      const int ii = i + dx, jj = j + dy;
+      if (ii >= 0 && ii < n0 && jj >= 0 && jj < n1 && T[(size_t)ii * n1 + jj]) {
+        t = true;
+        break;
+      }
+    }
+  bool a = true;
+  for (int dx = -1; dx <= 1; ++dx)
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int ii = i + dx, jj = j + dy;
+      if (ii >= 0 && ii < n0 && jj >= 0 && jj < n1 && !cover[(size_t)ii * n1 + jj]) a = false;
+    }
+  out[g] = (t && a) ? 1 : 0;
 }
 
 // FP32 copy of an FP64 array (coefficient copies of the mixed form)

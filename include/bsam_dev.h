@@ -179,6 +179,16 @@ int bsam_batch_set_stop(bsam_hier h, int inst, int max_vcycles, double rel_tol);
 int bsam_parabolic_rhs(bsam_hier h, int scheme, double dt, const double *f, int64_t n);
 int bsam_history_push(bsam_hier h);
 
+/* Tagging of the finest level on the device (ebTagCluster.m:50-59 'ulap',
+ * indicator 0; ebRte.m:14-41 'rte', indicator 1), on the current solution:
+ * tag where the indicator exceeds threshold, dilate by `buffer` cells
+ * (ebTagCluster.m:113-127) and keep the cells the 8-eroded patch cover
+ * allows (ebTagCluster.m:130-141).  mask receives the level's n0 x n1 index
+ * space, i-major (mask[i * n1 + j], 0-based), 1 = tagged; the host clusters
+ * it.  Single hierarchies only. */
+int bsam_tag_level(bsam_hier h, int level, int indicator, double threshold, int buffer, int n0, int n1,
+                   uint8_t *mask);
+
 /* One ebVcycle(H, nlev) + ebTransfer(H,0,'filldown') (ebVcycle.m:16-35,
  * ebTransfer.m:73-79), force reset included (ebSolveCycles.m:30-34). */
 int bsam_vcycle(bsam_hier h);

@@ -82,3 +82,26 @@ def test_config1_solution_driven_matches_oracle_pipeline():
     for k in range(1, a['H'].nlev + 1):
         for qa, qb in zip(a['H'].lev[k].Q, b['H'].lev[k].Q):
             np.testing.assert_array_equal(qa, qb)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('indicator', ['ulap', 'rte'])
+@pytest.mark.parametrize('tree', [False, True])
+def test_device_tag_mask_equals_host(indicator, tree):
+    """Tagging on the device (indicator, buffer, cover erosion) gives the
+    host restatement's mask bit for bit on a solved hierarchy."""
+    from bsam.tagcluster import tag_cluster
+    opts = ebOptions('BaseCells', 32, 'MaxLevels', 3, 'Indicator', indicator, 'TagThreshold', 1e-3, 'Verbose', 0,
+                     'TagBuffer', 2, 'RelTol', 1e-10)
+    be = dev()
+    from bsam.solve import ebSolveCycles
+    p = vardc_problem()
+    H = hier.setup(p, opts, be, tree=tree)
+    H = ebSolveCycles(H, be)
+    for _ in range(2):
+        host = tag_cluster(H)
+        devb = tag_cluster(H, be)
+        np.testing.assert_array_equal(host, devb)
+        assert host.shape[0] > 0
+        H = hier.add_level(H, host, be)
+        H = ebSolveCycles(H, be)
