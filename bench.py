@@ -293,6 +293,18 @@ def batched_form(backend, n, steps, warmup, flush, local):
         d = {'value': n * steps / (ms.sum() / 1e3), 'unit': 'solves/s', 'ms_per_batch': float(ms.mean()),
              'p50_ms': float(np.percentile(ms, 50)), 'p99_ms': float(np.percentile(ms, 99)),
              'vcycles_slowest': maxit, 'kernels_per_vcycle': bh.kernels_per_vcycle()}
+        # smoother roofline per merged level (levels larger than L2 here)
+        peak, peak_kind = load_peaks()
+        cells = [int(b.levels[k - 1, 5] - b.levels[k - 1, 4]) for k in range(1, b.nlev + 1)]
+        lv = []
+        for k in range(2, b.nlev + 1):
+            pr = bh.profile(2, level=k)['relax']
+            if pr['launches']:
+                ach = pr['bytes'] / (pr['ms'] / 1e3) / 1e9
+                lv.append({'level': k, 'cells': cells[k - 1], 'avg_launch_us': 1e3 * pr['ms'] / pr['launches'],
+                           'achieved_gbs': ach, 'frac': ach / peak})
+        d['smoother_levels'] = lv
+        d['smoother_peak'] = {'value': peak, 'kind': peak_kind, 'unit': 'GB/s'}
         if prec == 'fp64':
             d['equal_to_solo_bitwise'] = bool(equal)
         else:

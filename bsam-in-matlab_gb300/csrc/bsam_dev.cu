@@ -1017,6 +1017,7 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
     CK(cudaStreamSynchronize(s));
   }
   // residual plan: warp tasks, slots in instance order, level by level
+  constexpr int kTask = 32 * kResLane;
   // (main cells, then the level's correction targets), then the QC refresh
   // tasks of the levels above each instance's root
   std::vector<ResTask> tasks;
@@ -1034,7 +1035,7 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
         const int32_t *r = B.P(p);
         const int n = r[PD_MX] * r[PD_MY];
         for (int c = 0; c < n; ++c) h->inst_visible[i] += (d->covered[r[PD_COFF] + c] == 0);
-        for (int b0 = 0; b0 < n; b0 += 32) tasks.push_back(ResTask{0, k, p, b0, std::min(32, n - b0), ns++, i, 0});
+        for (int b0 = 0; b0 < n; b0 += kTask) tasks.push_back(ResTask{0, k, p, b0, std::min(kTask, n - b0), ns++, i, 0});
       }
       if (k < d->nlev) {
         const LevelPlan &Lf = h->lev[k + 1];
@@ -1045,7 +1046,8 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
             if (t0 < 0) t0 = t;
             t1 = t + 1;
           }
-        for (int t = t0; t0 >= 0 && t < t1; t += 32) tasks.push_back(ResTask{1, k, 0, t, std::min(32, t1 - t), ns++, i, 0});
+        for (int t = t0; t0 >= 0 && t < t1; t += kTask)
+          tasks.push_back(ResTask{1, k, 0, t, std::min(kTask, t1 - t), ns++, i, 0});
       }
       ranges.push_back(SlotRange{s0, ns, L.hx * L.hy});
     }
@@ -1061,10 +1063,10 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
       const int32_t *r = B.P(p);
       const int root = h->inst_root[pinst[p]];
       if (k < std::max(2, root + 1)) continue;
-      for (int t = r[PD_RING0]; t < r[PD_RING1]; t += 32)
-        tasks.push_back(ResTask{2, k, t, 0, std::min(32, r[PD_RING1] - t), 0, pinst[p], 0});
+      for (int t = r[PD_RING0]; t < r[PD_RING1]; t += kTask)
+        tasks.push_back(ResTask{2, k, t, 0, std::min(kTask, r[PD_RING1] - t), 0, pinst[p], 0});
       const int nc = (r[PD_MX] / 2) * (r[PD_MY] / 2);
-      for (int b0 = 0; b0 < nc; b0 += 32) tasks.push_back(ResTask{3, k, p, b0, std::min(32, nc - b0), 0, pinst[p], 0});
+      for (int b0 = 0; b0 < nc; b0 += kTask) tasks.push_back(ResTask{3, k, p, b0, std::min(kTask, nc - b0), 0, pinst[p], 0});
     }
   }
   h->nrtasks = (int)tasks.size();

@@ -643,8 +643,8 @@ __global__ void __launch_bounds__(kBlock) k_coarsest(const double *__restrict__ 
 // ---------------------------------------------------------------------------
 // Composite residual (ebCompResidual.m:15-85) of every level >= root, for one
 // hierarchy or every instance of a batch, in one launch.  The work is a list
-// of warp tasks, each covering up to 32 items of ONE patch (or of one
-// instance's correction targets), so every warp belongs to one instance:
+// of warp tasks, each covering up to 32 * kResLane items of ONE patch (or of
+// one instance's correction targets), so every warp belongs to one instance:
 //   kind 0  r = FTrue - op(Q) on visible cells of a patch in the norms,
 //           correction targets excluded while the corrections are on
 //   kind 1  r at correction targets of a level, corrections added in order,
@@ -668,6 +668,22 @@ struct LevelX {
   int ct_n, pad;
 };
 
+// max of non-negative doubles on the integer pipe (their bit patterns order
+// like the values; the FP64 pipe of GB300 is the scarce one).  A NaN loses,
+// as in fmax and the reference's max: its pattern ranks below zero here.
+__device__ __forceinline__ double pmax(double a, double b) {
+  constexpr long long kInf = 0x7FF0000000000000LL;
+  long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  x = x > kInf ? -1 : x;
+  y = y > kInf ? -1 : y;
+  const long long m = x > y ? x : y;
+  return __longlong_as_double(m < 0 ? 0 : m);
+}
+
+// items per lane of a residual warp task (a task covers up to 32 * kResLane
+// items of one patch or one instance's targets)
+constexpr int kResLane = 4;
+
 __global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ X, const PatchD *__restrict__ patches,
                                                      const ResTask *__restrict__ tasks, int ntask, Fields f,
                                                      const int *__restrict__ ring, double *slots, int nslots,
@@ -682,64 +698,56 @@ __global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ 
     return;
   }
   const ResTask T = tasks[w];
-  const bool have = lane < T.n;
+  chain_wait();
   if (T.kind >= 2) {
-    chain_wait();
-    if (!mass_corr || !have) return;
+    if (!mass_corr) return;
     if (T.kind == 2) {
-      const int i = T.a + lane;
-      f.QC[__ldg(ring + 2 * i + 1)] = f.Q[__ldg(ring + 2 * i)];
+      for (int e = lane; e < T.n; e += 32) {
+        const int i = T.a + e;
+        f.QC[__ldg(ring + 2 * i + 1)] = f.Q[__ldg(ring + 2 * i)];
+      }
       return;
     }
     const PatchD &P = patches[T.a];
     const int cmx = P.mx >> 1;
-    const int s = T.b + lane;
-    const int cj = s / cmx, ci = s - cj * cmx;
-    f.QC[P.qc_off + (ci + 1) + (cj + 1) * (cmx + 2)] = restrict_cell(f.Q + P.q_off, P.mx + 2, ci, cj);
+    for (int e = lane; e < T.n; e += 32) {
+      const int s = T.b + e;
+      const int cj = s / cmx, ci = s - cj * cmx;
+      f.QC[P.qc_off + (ci + 1) + (cj + 1) * (cmx + 2)] = restrict_cell(f.Q + P.q_off, P.mx + 2, ci, cj);
+    }
     return;
   }
   double li = 0, sq = 0, fn = 0;
   const LevelX &Xk = X[T.level];
   if (T.kind == 0) {
-    bool on = false;
-    int c = 0, ldq = 0, q_off = 0, cc_out = 0;
-    double ft = 0, dE = 0, dW = 0, dN = 0, dS = 0, cf = 0;
-    if (have) {
-      const PatchD &P = patches[T.a];
-      const int mx = P.mx;
-      const int s = T.b + lane;
+    const PatchD &P = patches[T.a];
+    const int mx = P.mx, ldq = mx + 2;
+    const double *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off, *Qp = f.Q + P.q_off;
+#pragma unroll
+    for (int u = 0; u < kResLane; ++u) {
+      const int e = lane + 32 * u;
+      if (e >= T.n) break;
+      const int s = T.b + e;
       const int lj = s / mx, lx = s - lj * mx;
       const int cc = P.c_off + s;
       const uint8_t fl = __ldg(f.flags + cc);
-      if (!(fl & 1) && !(mass_corr && (fl & 2))) {
-        on = true;
-        ft = __ldg(f.FTrue + cc);
-        const double *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off;
-        dE = __ldg(DeW + (lx + 1) + lj * (mx + 1));
-        dW = __ldg(DeW + lx + lj * (mx + 1));
-        dN = __ldg(DnS + lx + (lj + 1) * mx);
-        dS = __ldg(DnS + lx + lj * mx);
-        cf = __ldg(f.CC + cc);
-        ldq = mx + 2;
-        q_off = P.q_off;
-        c = (lx + 1) + (lj + 1) * ldq;
-        cc_out = cc;
-      }
+      if ((fl & 1) || (mass_corr && (fl & 2))) continue;
+      const double ft = __ldg(f.FTrue + cc);
+      const int c = (lx + 1) + (lj + 1) * ldq;
+      const double r = ft - op_pre(Qp[c], Qp[c + 1], Qp[c - 1], Qp[c + ldq], Qp[c - ldq],
+                                   __ldg(DeW + (lx + 1) + lj * (mx + 1)), __ldg(DeW + lx + lj * (mx + 1)),
+                                   __ldg(DnS + lx + (lj + 1) * mx), __ldg(DnS + lx + lj * mx), __ldg(f.CC + cc), Xk.L);
+      li = pmax(li, fabs(r));
+      sq = sq + r * r;
+      fn = pmax(fn, fabs(ft));
+      if (rout) rout[cc] = (float)r;
     }
-    chain_wait();
-    if (on) {
-      const double *Qp = f.Q + q_off;
-      const double r = ft - op_pre(Qp[c], Qp[c + 1], Qp[c - 1], Qp[c + ldq], Qp[c - ldq], dE, dW, dN, dS, cf, Xk.L);
-      li = fabs(r);
-      sq = r * r;
-      fn = fabs(ft);
-      if (rout) rout[cc_out] = (float)r;
-    }
-  } else {   // kind 1: targets of this level, corrections from the level above
-    chain_wait();
+  } else if (mass_corr) {   // kind 1: targets of this level, corrections from the level above
     const LevelX &Xf = X[T.level + 1];
-    if (mass_corr && have) {
-      const int g = T.b + lane;
+    for (int u = 0; u < kResLane; ++u) {
+      const int e = lane + 32 * u;
+      if (e >= T.n) break;
+      const int g = T.b + e;
       const int cell = Xf.C.cell[g];
       const PatchD &Pc = Xk.L.patches[Xf.C.patch[g]];
       const int s = cell - Pc.c_off;
@@ -750,16 +758,16 @@ __global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ 
       r = add_corrections(r, Xf.C, g, Xf.L, Xk.L, f, true);
       if (rout) rout[cell] = (float)r;
       if (!(f.flags[cell] & 1)) {
-        li = fabs(r);
-        sq = r * r;
-        fn = fabs(ft);
+        li = pmax(li, fabs(r));
+        sq = sq + r * r;
+        fn = pmax(fn, fabs(ft));
       }
     }
   }
 #pragma unroll
   for (int off = 16; off >= 1; off >>= 1) {
-    li = fmax(li, __shfl_down_sync(0xffffffffu, li, off));
-    fn = fmax(fn, __shfl_down_sync(0xffffffffu, fn, off));
+    li = pmax(li, __shfl_down_sync(0xffffffffu, li, off));
+    fn = pmax(fn, __shfl_down_sync(0xffffffffu, fn, off));
     sq = sq + __shfl_down_sync(0xffffffffu, sq, off);
   }
   if (lane == 0) {
@@ -807,12 +815,12 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__rest
       const double a0 = slots[i], a1 = slots[i + kFinal], a2 = slots[i + 2 * kFinal], a3 = slots[i + 3 * kFinal];
       const double b0 = slots[2 * nslots + i], b1 = slots[2 * nslots + i + kFinal];
       const double b2 = slots[2 * nslots + i + 2 * kFinal], b3 = slots[2 * nslots + i + 3 * kFinal];
-      li = fmax(li, fmax(fmax(a0, a1), fmax(a2, a3)));
-      fn = fmax(fn, fmax(fmax(b0, b1), fmax(b2, b3)));
+      li = pmax(li, pmax(pmax(a0, a1), pmax(a2, a3)));
+      fn = pmax(fn, pmax(pmax(b0, b1), pmax(b2, b3)));
     }
     for (; i < s1; i += kFinal) {
-      li = fmax(li, slots[i]);
-      fn = fmax(fn, slots[2 * nslots + i]);
+      li = pmax(li, slots[i]);
+      fn = pmax(fn, slots[2 * nslots + i]);
     }
   }
   s_a[t] = li;
@@ -820,8 +828,8 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__rest
   __syncthreads();
   for (int off = kFinal / 2; off >= 1; off >>= 1) {
     if (t < off) {
-      s_a[t] = fmax(s_a[t], s_a[t + off]);
-      s_b[t] = fmax(s_b[t], s_b[t + off]);
+      s_a[t] = pmax(s_a[t], s_a[t + off]);
+      s_b[t] = pmax(s_b[t], s_b[t + off]);
     }
     __syncthreads();
   }
