@@ -131,10 +131,13 @@ struct bsam_hier_s {
   DBuf<int> inst_nlev;             // per instance: its finest level
   // mixed form: FP32 correction, its right-hand side and coarse shadows,
   // FP32 coefficient copies (homogeneous boundary data)
-  DBuf<float> E, F32, QC32, DeW32, DnS32, CC32, ID32, pcoef32, cfd32, bcg32, DeWr32, DnSr32;
-  // the smoother's face coefficients: on levels whose h^2 is a power of two
-  // pre-multiplied by the exact 1/h^2 (k_relax<T, true>), else as uploaded
-  DBuf<double> DeWr, DnSr;
+  DBuf<float> E, F32, QC32, DeW32, DnS32, CC32, ID32, pcoef32, cfd32, bcg32, rpack32;
+  // the smoother's packed operands (k_relax): per chunk and colour the face
+  // coefficients -- on levels whose h^2 is a power of two pre-multiplied by
+  // the exact 1/h^2 -- and InvDiagS; built on the host from these copies
+  DBuf<double> rpack;
+  std::vector<double> hDeWr, hDnSr, hID;
+  std::vector<RelaxChunk> hchunks;
   DBuf<double> Uo, Uoo, fsrc;      // parabolic history (cells) and f staging
   bool f32_dirty = true;
   DecompH all_cells;               // every cell of every level (batch force reset)
@@ -268,19 +271,38 @@ template <> FieldsT<float> fields_t<float>(bsam_hier h) {
   return f;
 }
 
-// the smoother's arrays: face coefficients pre-scaled on power-of-two levels
-template <class T> FieldsT<T> relax_fields(bsam_hier h);
-template <> Fields relax_fields<double>(bsam_hier h) {
-  Fields f = fields(h);
-  f.DeW = h->DeWr.p;
-  f.DnS = h->DnSr.p;
-  return f;
-}
-template <> FieldsT<float> relax_fields<float>(bsam_hier h) {
-  FieldsT<float> f = fields_t<float>(h);
-  f.DeW = h->DeWr32.p;
-  f.DnS = h->DnSr32.p;
-  return f;
+// the smoother's packed operands in the cycle's value type
+template <class T> const T *relax_pack(bsam_hier h);
+template <> const double *relax_pack<double>(bsam_hier h) { return h->rpack.p; }
+template <> const float *relax_pack<float>(bsam_hier h) { return h->rpack32.p; }
+
+// pack the smoother's operands of every chunk and colour (see kPackRows)
+int build_relax_pack(bsam_hier h) {
+  const size_t row = kPackRows * kChunk;
+  std::vector<double> pk(std::max<size_t>(h->hchunks.size(), 1) * 2 * row, 0.0);
+  for (size_t ch = 0; ch < h->hchunks.size(); ++ch) {
+    const RelaxChunk &R = h->hchunks[ch];
+    const int half = R.mx >> 1;
+    for (int m = 0; m < 2; ++m) {
+      double *o = pk.data() + (ch * 2 + m) * row;
+      for (int t = 0; t < R.n; ++t) {
+        const int s = R.s0 + t;
+        const int lj = s / half;
+        const int li = 2 * (s - lj * half) + ((m + lj + R.par0) & 1);
+        o[t] = h->hDeWr[R.dew_off + (li + 1) + lj * (R.mx + 1)];
+        o[kChunk + t] = h->hDeWr[R.dew_off + li + lj * (R.mx + 1)];
+        o[2 * kChunk + t] = h->hDnSr[R.dns_off + li + (lj + 1) * R.mx];
+        o[3 * kChunk + t] = h->hDnSr[R.dns_off + li + lj * R.mx];
+        o[4 * kChunk + t] = h->hID[R.c_off + li + lj * R.mx];
+      }
+    }
+  }
+  int rc;
+  if (!h->rpack.p && (rc = h->rpack.alloc(pk.size()))) return rc;
+  CK(cudaMemcpyAsync(h->rpack.p, pk.data(), sizeof(double) * pk.size(), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->f32_dirty = true;
+  return BSAM_OK;
 }
 
 // algorithmic bytes scale with the value type (FP64 figures x size/8)
@@ -305,9 +327,10 @@ template <class T = double>
 void launch_relax(bsam_hier h, int k, int nsweeps) {
   if (nsweeps <= 0) return;
   const LevelPlan &L = h->lev[k];
-  FieldsT<T> f = relax_fields<T>(h);
+  FieldsT<T> f = fields_t<T>(h);
   LevelD ld = leveld(h, k);
   const RelaxChunk *ch = h->rchunks.p + L.rc_off;
+  const T *pk = relax_pack<T>(h) + (size_t)L.rc_off * 2 * kPackRows * kChunk;
   const int grid = (L.rc_n + kBlock / kChunk - 1) / (kBlock / kChunk);
   const int unit = h->opts.omega == 1.0 ? 1 : 0;
   for (int s = 0; s < nsweeps; ++s)
@@ -315,10 +338,10 @@ void launch_relax(bsam_hier h, int k, int nsweeps) {
       const int fresh = (s > 0 || m > 0) ? 1 : 0;
       Launch l(h, K_RELAX, 24.0 * tscale<T>() * (double)L.ncells, k);
       if (L.pow2)
-        launch_k(h, k_relax<T, true>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m,
+        launch_k(h, k_relax<T, true>, grid, kBlock, ld, ch, L.rc_n, f, pk, (const Rule *)h->perim.p, m,
                  (T)h->opts.omega, unit, fresh);
       else
-        launch_k(h, k_relax<T, false>, grid, kBlock, ld, ch, L.rc_n, f, (const Rule *)h->perim.p, m,
+        launch_k(h, k_relax<T, false>, grid, kBlock, ld, ch, L.rc_n, f, pk, (const Rule *)h->perim.p, m,
                  (T)h->opts.omega, unit, fresh);
     }
   launch_fill<T>(h, k);
@@ -474,7 +497,7 @@ int ensure_f32(bsam_hier h) {
         (rc = h->DeW32.alloc(h->DeW.n)) || (rc = h->DnS32.alloc(h->DnS.n)) || (rc = h->CC32.alloc(h->CC.n)) ||
         (rc = h->ID32.alloc(h->ID.n)) || (rc = h->pcoef32.alloc(std::max<size_t>(h->pcoef.n, 1))) ||
         (rc = h->cfd32.alloc(std::max<size_t>(h->cfd.n, 1))) || (rc = h->bcg32.alloc(std::max<size_t>(h->bcg.n, 1))) ||
-        (rc = h->DeWr32.alloc(h->DeW.n)) || (rc = h->DnSr32.alloc(h->DnS.n)))
+        (rc = h->rpack32.alloc(h->rpack.n)))
       return rc;
     CK(cudaMemsetAsync(h->F32.p, 0, sizeof(float) * h->F32.n, h->stream));
     CK(cudaMemsetAsync(h->QC32.p, 0, sizeof(float) * h->QC32.n, h->stream));
@@ -485,7 +508,7 @@ int ensure_f32(bsam_hier h) {
     const std::pair<DBuf<double> *, DBuf<float> *> cv[] = {{&h->DeW, &h->DeW32}, {&h->DnS, &h->DnS32},
                                                            {&h->CC, &h->CC32},   {&h->ID, &h->ID32},
                                                            {&h->pcoef, &h->pcoef32}, {&h->cfd, &h->cfd32},
-                                                           {&h->DeWr, &h->DeWr32}, {&h->DnSr, &h->DnSr32}};
+                                                           {&h->rpack, &h->rpack32}};
     for (const auto &c : cv)
       if (c.first->n) launch_k(h, k_to_f32, 4 * 152, kBlock, (const double *)c.first->p, c.second->p, (long long)c.first->n);
     CK(cudaGetLastError());
@@ -1013,8 +1036,11 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
         for (int64_t i = 0; i < mx * (my + 1); ++i) dns[r[PD_DNSOFF] + i] *= iy;
       }
     }
-    if ((rc = h->DeWr.upload(dew.data(), dew.size(), s)) || (rc = h->DnSr.upload(dns.data(), dns.size(), s))) return rc;
-    CK(cudaStreamSynchronize(s));
+    h->hDeWr.swap(dew);
+    h->hDnSr.swap(dns);
+    h->hID.assign(d->InvDiagS, d->InvDiagS + d->n_cells);
+    h->hchunks = B.chunks;
+    if ((rc = build_relax_pack(h))) return rc;
   }
   // residual plan: warp tasks, slots in instance order, level by level
   constexpr int kTask = 32 * kResLane;
@@ -1162,11 +1188,11 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
 void release(bsam_hier h) {
   drop_graph(h);
   for (DBuf<double> *b : {&h->Q, &h->F, &h->FTrue, &h->QC, &h->CC, &h->ID, &h->DeW, &h->DnS, &h->bcg, &h->cfd,
-                          &h->pcoef, &h->Ainv, &h->bcRhs, &h->slots, &h->partials, &h->hist, &h->saveQ, &h->saveQC, &h->DeWr, &h->DnSr, &h->Uo, &h->Uoo, &h->fsrc,
+                          &h->pcoef, &h->Ainv, &h->bcRhs, &h->slots, &h->partials, &h->hist, &h->saveQ, &h->saveQC, &h->rpack, &h->Uo, &h->Uoo, &h->fsrc,
                           &h->saveF})
     b->release();
   for (DBuf<float> *b : {&h->E, &h->F32, &h->QC32, &h->DeW32, &h->DnS32, &h->CC32, &h->ID32, &h->pcoef32, &h->cfd32,
-                         &h->bcg32, &h->DeWr32, &h->DnSr32})
+                         &h->bcg32, &h->rpack32})
     b->release();
   for (DBuf<int> *b : {&h->win, &h->fp, &h->ring, &h->ints, &h->ct_cell, &h->ct_patch, &h->ct_beg, &h->ct_item,
                        &h->ct_j, &h->active, &h->iters, &h->ones, &h->g_inst, &h->ring_inst, &h->inst_nlev, &h->g_dst, &h->g_a, &h->g_b, &h->g_c, &h->g_d, &h->g_e})
@@ -1314,25 +1340,27 @@ static DBuf<double> *field_buf(bsam_hier h, int which) {
   }
 }
 
-// the smoother's scaled copy of a face-coefficient array after its update
-static int rescale_faces(bsam_hier h, int which, const double *host) {
+// the smoother's packed operands after an update of DeW, DnS or InvDiagS
+static int repack(bsam_hier h, int which, const double *host) {
+  if (which == BSAM_FIELD_INVDIAG) {
+    h->hID.assign(host, host + h->ID.n);
+    return build_relax_pack(h);
+  }
   const bool x = which == BSAM_FIELD_DEW;
-  std::vector<double> v(host, host + (x ? h->DeW.n : h->DnS.n));
+  std::vector<double> &v = x ? h->hDeWr : h->hDnSr;
+  v.assign(host, host + (x ? h->DeW.n : h->DnS.n));
   for (int k = 1; k <= h->nlev; ++k) {
     const LevelPlan &L = h->lev[k];
     if (!L.pow2) continue;
-    const double s = x ? 1.0 / (L.hx * L.hx) : 1.0 / (L.hy * L.hy);
+    const double sc = x ? 1.0 / (L.hx * L.hx) : 1.0 / (L.hy * L.hy);
     for (int p = L.p0; p < L.p1; ++p) {
       const int32_t *r = h->hpatches.data() + (size_t)p * PDN;
       const int64_t off = x ? r[PD_DEWOFF] : r[PD_DNSOFF];
       const int64_t n = x ? (int64_t)(r[PD_MX] + 1) * r[PD_MY] : (int64_t)r[PD_MX] * (r[PD_MY] + 1);
-      for (int64_t i = 0; i < n; ++i) v[off + i] *= s;
+      for (int64_t i = 0; i < n; ++i) v[off + i] *= sc;
     }
   }
-  DBuf<double> &dst = x ? h->DeWr : h->DnSr;
-  CK(cudaMemcpyAsync(dst.p, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice, h->stream));
-  CK(cudaStreamSynchronize(h->stream));
-  return BSAM_OK;
+  return build_relax_pack(h);
 }
 
 int bsam_set_field(bsam_hier h, int which, const double *host, int64_t n) {
@@ -1344,8 +1372,8 @@ int bsam_set_field(bsam_hier h, int which, const double *host, int64_t n) {
   if ((size_t)n != b->n) return fail(BSAM_ERR_ARG, "field length mismatch");
     if (n) CK(cudaMemcpyAsync(b->p, host, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  if (which == BSAM_FIELD_DEW || which == BSAM_FIELD_DNS) {
-    if ((rc = rescale_faces(h, which, host))) return rc;
+  if (which == BSAM_FIELD_DEW || which == BSAM_FIELD_DNS || which == BSAM_FIELD_INVDIAG) {
+    if ((rc = repack(h, which, host))) return rc;
   }
   if (which >= BSAM_FIELD_CC && which <= BSAM_FIELD_BCRHS) h->f32_dirty = true;
   return BSAM_OK;

@@ -147,6 +147,23 @@ __device__ __forceinline__ T eval_rule(const GhostItems &G, int i, const T *Q, c
   }
 }
 
+// one ghost item: its final value (or the QC ring refresh)
+template <class T>
+__device__ __forceinline__ void ghost_item(const GhostItems &G, int i, int8_t ty, int dst, T *Q, T *QC, const T *bcg,
+                                           T hx, T hy) {
+  if (ty == G_RING) {
+    QC[dst] = Q[G.a[i]];
+  } else if (ty == G_PHYS_CORNER) {
+    // (face ghost 1 + face ghost 2) - interior, the face ghosts evaluated by
+    // their own final rules (ebFillGhosts.m:84-89 reads them after stage 3)
+    const T v1 = eval_rule<T>(G, G.a[i], Q, bcg, hx, hy);
+    const T v2 = eval_rule<T>(G, G.b[i], Q, bcg, hx, hy);
+    Q[dst] = (v1 + v2) - Q[G.c[i]];
+  } else {
+    Q[dst] = eval_rule<T>(G, i, Q, bcg, hx, hy);
+  }
+}
+
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, T *__restrict__ Q, T *__restrict__ QC,
                                                   const T *__restrict__ bcg, double hx_, double hy_,
@@ -164,18 +181,7 @@ __global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, 
   const int dst = skip ? 0 : G.dst[i];
   chain_wait();
   if (skip) return;
-  const T hx = T(hx_), hy = T(hy_);   // once per thread, outside the relaxation
-  if (ty == G_RING) {
-    QC[dst] = Q[G.a[i]];
-  } else if (ty == G_PHYS_CORNER) {
-    // (face ghost 1 + face ghost 2) - interior, the face ghosts evaluated by
-    // their own final rules (ebFillGhosts.m:84-89 reads them after stage 3)
-    const T v1 = eval_rule<T>(G, G.a[i], Q, bcg, hx, hy);
-    const T v2 = eval_rule<T>(G, G.b[i], Q, bcg, hx, hy);
-    Q[dst] = (v1 + v2) - Q[G.c[i]];
-  } else {
-    Q[dst] = eval_rule<T>(G, i, Q, bcg, hx, hy);
-  }
+  ghost_item<T>(G, i, ty, dst, Q, QC, bcg, T(hx_), T(hy_));
 }
 
 // ---------------------------------------------------------------------------
@@ -219,19 +225,28 @@ __device__ __forceinline__ T eval_inline(const Rule &R, const T *Q) {
   }
 }
 
-template <class T, bool kPow2>
-__global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__restrict__ chunks, int nchunks,
-                                                  FieldsT<T> f, const Rule *__restrict__ perim, int m, T omega,
-                                                  int unit_omega, int fresh) {
-  chain_trigger();
-  const int ch = blockIdx.x * (kBlock / kChunk) + threadIdx.x / kChunk;
+// The smoother's operands per chunk and colour, packed at upload: for chunk
+// ch and colour m, five rows of kChunk values -- dE, dW, dN, dS (pre-scaled
+// by 1/h^2 on power-of-two levels) and InvDiagS -- one per colour cell of
+// the chunk, so a warp reads each operand as one contiguous row instead of
+// every other value of the reference's arrays.
+constexpr int kPackRows = 5;
+
+// one colour-cell update of chunk ch (thread tc of the chunk); kChain: the
+// grid kernel's programmatic-launch wait sits between the static loads and
+// the first read of the solution
+template <class T, bool kPow2, bool kChain>
+__device__ __forceinline__ void relax_cell(const LevelD &L, const RelaxChunk *__restrict__ chunks, int nchunks,
+                                           const FieldsT<T> &f, const T *__restrict__ pack,
+                                           const Rule *__restrict__ perim, int m, T omega, int unit_omega, int fresh,
+                                           int ch, int tc) {
   bool ok = ch < nchunks;
   RelaxChunk R;
   if (ok) R = chunks[ch];
-  const int s = ok ? R.s0 + (threadIdx.x & (kChunk - 1)) : 0;
+  const int s = ok ? R.s0 + tc : 0;
   ok = ok && s < R.s0 + R.n && f.active[R.inst];
   if (!ok) {
-    chain_wait();
+    if (kChain) chain_wait();
     return;
   }
   const int mx = R.mx, my = R.my, half = mx >> 1;
@@ -240,12 +255,10 @@ __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__
   const int ldq = mx + 2;
   const int c = (li + 1) + (lj + 1) * ldq;
   const int cc = R.c_off + li + lj * mx;
-  // static operands: coefficients, diagonal, boundary data, ghost rules
-  const T *__restrict__ DeW = f.DeW + R.dew_off;
-  const T *__restrict__ DnS = f.DnS + R.dns_off;
-  const T dE = __ldg(DeW + (li + 1) + lj * (mx + 1)), dW = __ldg(DeW + li + lj * (mx + 1));
-  const T dN = __ldg(DnS + li + (lj + 1) * mx), dS = __ldg(DnS + li + lj * mx);
-  const T idg = __ldg(f.ID + cc);
+  // static operands: packed coefficients and diagonal, boundary data, rules
+  const T *__restrict__ pk = pack + (size_t)(ch * 2 + m) * (kPackRows * kChunk) + tc;
+  const T dE = __ldg(pk), dW = __ldg(pk + kChunk), dN = __ldg(pk + 2 * kChunk), dS = __ldg(pk + 3 * kChunk);
+  const T idg = __ldg(pk + 4 * kChunk);
   const T *__restrict__ g4 = f.bcg + R.bcg_off;
   // a cell touches at most one x side (W or E) and one y side (S or N):
   // kind 0 interior neighbour, 1 Dirichlet, 2 Neumann, 3 ghost rule
@@ -264,7 +277,7 @@ __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__
     if (bc) { ky = bc; gy = __ldg(g4 + 2 * my + sy * mx + li); }
     else if (fresh) { ky = 3; ry = perim[R.pe_off + 2 * my + sy * mx + li]; }
   }
-  chain_wait();
+  if (kChain) chain_wait();
   const T c83 = T(8.0 / 3.0), c13 = T(1.0 / 3.0);
   const LevelH<T> H = level_h(L, T(0));
   T *__restrict__ Q = f.Q + R.q_off;
@@ -302,6 +315,17 @@ __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__
   if (unit_omega) Q[c] = t;
   else Q[c] = omega * t + (1 - omega) * Q[c];
 }
+
+template <class T, bool kPow2>
+__global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__restrict__ chunks, int nchunks,
+                                                  FieldsT<T> f, const T *__restrict__ pack,
+                                                  const Rule *__restrict__ perim, int m, T omega, int unit_omega,
+                                                  int fresh) {
+  chain_trigger();
+  relax_cell<T, kPow2, true>(L, chunks, nchunks, f, pack, perim, m, omega, unit_omega, fresh,
+                             blockIdx.x * (kBlock / kChunk) + threadIdx.x / kChunk, threadIdx.x & (kChunk - 1));
+}
+
 
 // ---------------------------------------------------------------------------
 // restrict2 (ebKernels.m:98-102) of each patch interior into its QC interior
