@@ -330,7 +330,7 @@ def serving_form(rates, per_rate):
                        'mixed precision, RelTol 1e-10',
            'builders': srv.nbuild, 'wave_slots': len(srv.ctxs), 'server_start_s': start_s, 'rates': []}
     for rate in rates:
-        n = int(max(per_rate, round(rate * 3)))
+        n = int(max(per_rate, round(rate * 6)))
         specs = [star_request(int(rate * 1000) + i) for i in range(n)]
         w0 = len(srv.waves_run)
         res, wall = run_stream(srv, specs, rate=rate, seed=int(rate))
@@ -481,7 +481,7 @@ def main():
         forms['parabolic'] = parabolic_form(backend)
         rates = [float(r) for r in args.serve_rates.split(',') if r.strip()]
         if rates and rank == 0:
-            forms['serving'] = serving_form(rates, 20)
+            forms['serving'] = serving_form(rates, 30)
 
     if rank == 0:
         cpu = None
