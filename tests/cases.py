@@ -63,3 +63,61 @@ def printed_close(value, printed):
         dec = len(s.split('.')[1]) if '.' in s else 0
         ulp = 10.0 ** (-dec)
     return abs(value - float(s)) <= 0.5 * ulp * (1 + 1e-9) + 1e-300
+
+
+def gauss52_problem():
+    """mmsCases('gauss52') (EllipticBSAM/tests/mmsCases.m:34-39, makeGauss52
+    :62-82): three periodic Gaussians on [0,1]^2, u - lap u = f, Dirichlet."""
+    sg = 0.25
+    xi, yi, Ai = (0.4375, 0.4375, 0.5625), (0.5625, 0.4375, 0.4375), (1.0, -1.0, 1.0)
+
+    def uex(x, y):
+        v = 0
+        for i in range(3):
+            v = v + Ai[i] * np.exp(-(np.sin(x - xi[i]) ** 2 + np.sin(y - yi[i]) ** 2) / (2 * sg ** 2))
+        return v
+
+    def f(x, y):
+        v = 0
+        for i in range(3):
+            gi = np.exp(-(np.sin(x - xi[i]) ** 2 + np.sin(y - yi[i]) ** 2) / (2 * sg ** 2))
+            gpx = -np.sin(2 * (x - xi[i])) / (2 * sg ** 2)
+            gppx = -np.cos(2 * (x - xi[i])) / sg ** 2
+            gpy = -np.sin(2 * (y - yi[i])) / (2 * sg ** 2)
+            gppy = -np.cos(2 * (y - yi[i])) / sg ** 2
+            v = v + Ai[i] * gi * (1 - (gppx + gpx ** 2 + gppy + gpy ** 2))
+        return v
+    return ebProblem([0, 1, 0, 1], 1, 1, f, ('dirichlet', uex), uex)
+
+
+def threebumps_problem():
+    """mmsCases('threebumps') (EllipticBSAM/tests/mmsCases.m:41-53)."""
+    s = 0.02
+    xi, yi, Ai = (0.30, 0.66, 0.49), (0.34, 0.42, 0.72), (1.0, 0.8, -0.9)
+    g = lambda x, y, a, b: np.exp(-((x - a) ** 2 + (y - b) ** 2) / (2 * s ** 2))
+    lg = lambda x, y, a, b: g(x, y, a, b) * (((x - a) ** 2 + (y - b) ** 2) / s ** 4 - 2 / s ** 2)
+    uex = lambda x, y: (Ai[0] * g(x, y, xi[0], yi[0]) + Ai[1] * g(x, y, xi[1], yi[1])) + Ai[2] * g(x, y, xi[2], yi[2])
+    lap = lambda x, y: (Ai[0] * lg(x, y, xi[0], yi[0]) + Ai[1] * lg(x, y, xi[1], yi[1])) + Ai[2] * lg(x, y, xi[2], yi[2])
+    f = lambda x, y: uex(x, y) - lap(x, y)
+    return ebProblem([0, 1, 0, 1], 1, 1, f, ('dirichlet', uex), uex)
+
+
+def lshape_tag(X, Y, L):
+    """T4 tag (EllipticBSAM/tests/runAllTests.m:89-90)."""
+    return (((X >= 0.375) & (X <= 0.625) & (Y >= 0.375) & (Y <= 0.5)) |
+            ((X >= 0.375) & (X <= 0.5) & (Y >= 0.5) & (Y <= 0.625)))
+
+
+def scattered_tag():
+    """T8 tag (runAllTests.m:207-212): 24 disks of radius 0.02 at rand(24,2)
+    after rng(42) -- MATLAB's default generator is MT19937 seeded like
+    numpy's legacy RandomState, with the same 53-bit doubles; rand fills the
+    24x2 matrix column by column."""
+    r = np.random.RandomState(42).random_sample(48)
+    px, py = r[:24], r[24:]
+
+    def tag(X, Y, L):
+        Xv, Yv = np.asarray(X).reshape(-1, 1, order='F'), np.asarray(Y).reshape(-1, 1, order='F')
+        hit = np.any((Xv - px[None, :]) ** 2 + (Yv - py[None, :]) ** 2 < 0.0004, axis=1)
+        return hit.reshape(np.shape(X), order='F')
+    return tag

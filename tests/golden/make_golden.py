@@ -73,6 +73,55 @@ for line in suite:
                    'V': int(m[7])})
 out['suite_T3_box_in_box'] = t3[:24]        # EllipticBSAM/tests/runAllTests.m
 out['suite_T3_box_in_box_tree'] = t3[24:48]  # EllipticBSAMTree/tests/runAllTreeTests.m
+
+
+def section(name, which):
+    """Lines of suite section `name` (e.g. 'T2'), occurrence `which` (0: the
+    QC-ring suite, 1: the tree suite)."""
+    starts = [i for i, l in enumerate(suite) if l.startswith('=== ' + name + ':')]
+    i = starts[which] + 1
+    lines = []
+    while i < len(suite) and not suite[i].startswith('===') and suite[i].strip():
+        lines.append(suite[i])
+        i += 1
+    return lines
+
+
+for which, tag in ((0, ''), (1, '_tree')):
+    t2 = []
+    for line in section('T2', which):
+        m = re.match(r'\s+m=\s*(\d+)\s+err_inf=([0-9.e+-]+)\s+err_l2=([0-9.e+-]+)\s+factor=([0-9.]+)\s+V=(\d+)', line)
+        if m:
+            t2.append({'m': int(m[1]), 'err_inf': m[2], 'err_l2': m[3], 'factor': m[4], 'V': int(m[5])})
+    out['suite_T2_pure_neumann' + tag] = t2
+    t4 = []
+    for line in section('T4', which):
+        m = re.match(r'\s+m0=\s*(\d+)\s+err_inf=([0-9.e+-]+)\s+factor=([0-9.]+)\s+level-2 patches=(\d+)\s+mass=([0-9.e+-]+)',
+                     line)
+        if m:
+            t4.append({'m0': int(m[1]), 'err_inf': m[2], 'factor': m[3], 'np2': int(m[4]), 'mass': m[5]})
+    out['suite_T4_lshape' + tag] = t4
+    t5 = []
+    for line in section('T5', which):
+        m = re.match(r'\s+MaxLevels=(\d) \(got (\d)\): err_inf=([0-9.e+-]+)\s+err_l2=([0-9.e+-]+)\s+factor=([0-9.]+)'
+                     r'\s+dof=(\d+)', line)
+        if m:
+            t5.append({'MaxLevels': int(m[1]), 'got': int(m[2]), 'err_inf': m[3], 'err_l2': m[4], 'factor': m[5],
+                       'dof': int(m[6])})
+    out['suite_T5_adaptive' + tag] = t5
+    t7 = []
+    for line in section('T7', which):
+        m = re.match(r'\s+levels=(\d)\s+corrections=(\d) : mass defect \(rel\) = ([0-9.e+-]+)\s+err=([0-9.e+-]+)', line)
+        if m:
+            t7.append({'levels': int(m[1]), 'corrections': int(m[2]), 'mass': m[3], 'err': m[4]})
+    out['suite_T7_mass' + tag] = t7
+    t8 = []
+    for line in section('T8', which):
+        m = re.match(r'\s+patches=(\d+)\s+min width=(\d+) \(fine cells\)\s+factor=([0-9.]+)\s+err=([0-9.e+-]+)'
+                     r'\s+mass=([0-9.e+-]+)', line)
+        if m:
+            t8.append({'patches': int(m[1]), 'minw': int(m[2]), 'factor': m[3], 'err': m[4], 'mass': m[5]})
+    out['suite_T8_scattered' + tag] = t8
 out['source'] = {'repository': 'BSAM-in-MATLAB', 'files': ['verification/starfish-full-residual.csv',
                                                           'verification/starfish-full.json',
                                                           'verification/readme-examples.txt',
