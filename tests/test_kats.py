@@ -96,3 +96,76 @@ def test_operator_second_order():
         errs.append(np.max(np.abs(Lu - f(X[1:-1, 1:-1], Y[1:-1, 1:-1]))))
     rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
     assert np.all(rates >= 1.8)
+
+
+def _rand_points_1127():
+    """rng(1127); X = 4*rand(300,1)-2; Y = 4*rand(300,1)-2 (MATLAB's MT19937,
+    reproduced by numpy's legacy generator with the same seeding)."""
+    r = np.random.RandomState(1127).random_sample(600)
+    return 4 * r[:300] - 2, 4 * r[300:] - 2
+
+
+def _inpolygon(X, Y, v):
+    """Crossing-number point-in-polygon test (points on the boundary count
+    as inside, as in MATLAB's inpolygon)."""
+    x0, y0, x1, y1 = v[:-1, 0], v[:-1, 1], v[1:, 0], v[1:, 1]
+    inside = np.zeros(X.shape, dtype=bool)
+    for i in range(X.size):
+        cond = (y0 > Y[i]) != (y1 > Y[i])
+        xc = x0[cond] + (Y[i] - y0[cond]) * (x1[cond] - x0[cond]) / (y1[cond] - y0[cond])
+        inside[i] = np.count_nonzero(X[i] < xc) % 2 == 1
+    return inside
+
+
+def test_starfish_distance_brute_force():
+    """testStarfish.m:5-16: the tree-pruned signed distance against a brute
+    force over every segment, its sign against point-in-polygon, vertices on
+    the curve."""
+    from bsam.ddm import ddStarfishGeometry
+    g = ddStarfishGeometry()
+    X, Y = _rand_points_1127()
+    v = g.vertices
+    brute = np.full(X.shape, np.inf)
+    for k in range(v.shape[0] - 1):
+        a = v[k]
+        e = v[k + 1] - a
+        t = np.maximum(0, np.minimum(1, ((X - a[0]) * e[0] + (Y - a[1]) * e[1]) / np.sum(e ** 2)))
+        brute = np.minimum(brute, np.hypot(X - a[0] - t * e[0], Y - a[1] - t * e[1]))
+    d = g.signedDistance(X, Y)
+    assert np.max(np.abs(np.abs(d) - brute)) < 5e-14
+    assert np.all((d >= 0) == _inpolygon(X, Y, v))
+    assert g.signedDistance(np.array([0.0]), np.array([0.0]))[0] > 0
+    assert g.signedDistance(np.array([2.0]), np.array([2.0]))[0] < 0
+    assert np.max(np.abs(g.signedDistance(v[:, 0], v[:, 1]))) < 1e-13
+
+
+def _constant_solution(backend, device_geometry=None):
+    from bsam.ddm import StarGeometry, ddTransmissionProblem
+    from bsam import ebSolve
+    g = StarGeometry(3000, 0.9, 1.2, 0.7, 5.0, 0.0, device=device_geometry)
+    data = {'alpha': 3, 'beta': 2, 'gamma': 1, 'kappa': 0.01, 'q': 2, 'h': 4, 'g': -0.02,
+            'exact': lambda x, y: 2 + np.zeros(np.shape(x))}
+    p, aux = ddTransmissionProblem(g, 0.05, [-2, 2, -2, 2], data)
+    X, Y = _rand_points_1127()
+    assert np.max(np.abs(p.f(X, Y) - 2 * p.C(X, Y))) < 1e-13
+    return ebSolve(p, 'BaseCells', 32, 'MaxLevels', 3, 'Indicator', 'fun',
+                   'TagFunction', lambda x, y: np.abs(g.signedDistance(x, y)) < 0.2, 'RelTol', 1e-11,
+                   'Verbose', 0, backend=backend)
+
+
+def test_transmission_constant_solution():
+    """testStarfish.m:17-30: u = 2 with q = gamma u, h = beta u,
+    g = -kappa u is exact; the interface source sign makes or breaks it
+    (reference: Linf 4.263e-14, residual 3.183e-12)."""
+    s = _constant_solution(OracleBackend())
+    assert s['err']['linf'] < 1e-9 and s['stats']['stages'][-1]['finalRel'] < 1e-11
+
+
+@pytest.mark.gpu
+def test_transmission_constant_solution_device():
+    """The same known answer on the device path, with the geometry's segment
+    minimum on the device too."""
+    from bsam.device import DeviceBackend
+    be = DeviceBackend.get(0)
+    s = _constant_solution(be, be.ctx)
+    assert s['err']['linf'] < 1e-9 and s['stats']['stages'][-1]['finalRel'] < 1e-11
