@@ -323,8 +323,11 @@ void launch_fill(bsam_hier h, int k, int need = 0) {
 // ebRelaxLevel (ebRelaxLevel.m:28-38): 2*nsweeps colour passes; the ghost
 // refill after every colour is folded into the next pass (k_relax `fresh`),
 // and one fill after the last pass leaves the ghost frame as the reference's.
+// first_fresh: the first pass evaluates its neighbours' ghost rules too (the
+// ghosts were not refilled since the interior last changed everywhere, and
+// the rules give what a fill would)
 template <class T = double>
-void launch_relax(bsam_hier h, int k, int nsweeps) {
+void launch_relax(bsam_hier h, int k, int nsweeps, bool first_fresh = false) {
   if (nsweeps <= 0) return;
   const LevelPlan &L = h->lev[k];
   FieldsT<T> f = fields_t<T>(h);
@@ -335,7 +338,7 @@ void launch_relax(bsam_hier h, int k, int nsweeps) {
   const int unit = h->opts.omega == 1.0 ? 1 : 0;
   for (int s = 0; s < nsweeps; ++s)
     for (int m = 0; m < 2; ++m) {
-      const int fresh = (s > 0 || m > 0) ? 1 : 0;
+      const int fresh = (first_fresh || s > 0 || m > 0) ? 1 : 0;
       Launch l(h, K_RELAX, 24.0 * tscale<T>() * (double)L.ncells, k);
       if (L.pow2)
         launch_k(h, k_relax<T, true>, grid, kBlock, ld, ch, L.rc_n, f, pk, (const Rule *)h->perim.p, m,
@@ -412,8 +415,15 @@ void launch_vcycle(bsam_hier h, int k) {
   launch_coarse_load<T>(h, k);
   launch_vcycle<T>(h, k - 1);
   launch_prolong<T>(h, k, 1);
-  launch_fill<T>(h, k);
-  launch_relax<T>(h, k, h->opts.npost);
+  // the fill after the correction (ebVcycle.m:32) only feeds the first
+  // post-smoothing pass, whose ghost reads then evaluate the same rules on
+  // the same cells; the fill after the smoothing leaves the frame as the
+  // reference's
+  if (h->opts.npost > 0) {
+    launch_relax<T>(h, k, h->opts.npost, true);
+  } else {
+    launch_fill<T>(h, k);
+  }
 }
 
 void launch_filldown(bsam_hier h) {
