@@ -163,6 +163,10 @@ struct bsam_hier_s {
   // graph of one V-cycle + fill-down + residual
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
+  // the whole solve loop on the device: a WHILE node around that iteration
+  cudaGraph_t wgraph = nullptr;
+  cudaGraphExec_t wexec = nullptr;
+  bool while_tried = false;
   int64_t kernels_per_cycle = 0;
   // profiling
   bool profiling = false;
@@ -171,6 +175,7 @@ struct bsam_hier_s {
   std::vector<Rec> recs;
   int64_t launch_count = 0;
   int64_t graph_launches = 0;
+  int64_t while_bodies = 0;        // iterations run inside WHILE graphs
   DBuf<double> saveQ, saveQC, saveF;
 };
 
@@ -545,8 +550,61 @@ int build_graph(bsam_hier h) {
 void drop_graph(bsam_hier h) {
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
   if (h->graph) cudaGraphDestroy(h->graph);
+  if (h->wexec) cudaGraphExecDestroy(h->wexec);
+  if (h->wgraph) cudaGraphDestroy(h->wgraph);
   h->gexec = nullptr;
   h->graph = nullptr;
+  h->wexec = nullptr;
+  h->wgraph = nullptr;
+  h->while_tried = false;
+}
+
+// ebSolveCycles' loop as one graph: a conditional WHILE node whose body is
+// one iteration followed by k_any_active, which sets the condition from the
+// instances' stop tests.  A solve is then one graph launch and one read of
+// the results, with no host round trip per V-cycle.  Returns false (and the
+// per-iteration graph is used) when the runtime cannot build it.
+bool build_while_graph(bsam_hier h) {
+  if (h->wexec) return true;
+  if (h->while_tried) return false;
+  h->while_tried = true;
+  cudaGraph_t g = nullptr;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return false;
+  cudaGraphConditionalHandle cond;
+  cudaGraphNodeParams np = {};
+  cudaGraphNode_t node;
+  bool ok = cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  if (ok) {
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
+  }
+  if (ok) {
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    ok = cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+         cudaSuccess;
+    if (ok) {
+      const int64_t before = h->launch_count;
+      const int rc = launch_iteration(h, 1);
+      h->kernels_per_cycle = h->launch_count - before;
+      launch_k(h, k_any_active, 1, kBlock, (const int *)h->active.p, h->ninst, cond);
+      cudaGraph_t out = nullptr;
+      ok = cudaStreamEndCapture(h->stream, &out) == cudaSuccess && rc == BSAM_OK;
+      h->launch_count = before;
+    }
+  }
+  if (ok) ok = cudaGraphInstantiate(&h->wexec, g, 0) == cudaSuccess;
+  cudaGetLastError();   // a refused build leaves no sticky error behind
+  if (!ok) {
+    if (h->wexec) cudaGraphExecDestroy(h->wexec);
+    h->wexec = nullptr;
+    cudaGraphDestroy(g);
+    return false;
+  }
+  h->wgraph = g;
+  return true;
 }
 
 // per-instance residuals and active flags -> host (pinned); returns the
@@ -1568,10 +1626,17 @@ int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles,
     launch_consistent(h);
     launch_residual(h, 2);
   }
-  if (nactive && (rc = build_graph(h))) return rc;
   // every instance iterates until its own stop test fails; a converged
   // instance of a batch is frozen (its stores are predicated off) while the
-  // others continue
+  // others continue.  The loop runs on the device when the runtime can build
+  // its WHILE graph, else one graph launch per V-cycle with a host check.
+  bool on_device = false;
+  if (nactive && build_while_graph(h)) {
+    CK(cudaGraphLaunch(h->wexec, h->stream));
+    if ((rc = read_state(h, &nactive))) return rc;
+    on_device = true;
+  }
+  if (nactive && (rc = build_graph(h))) return rc;
   while (nactive) {
     CK(cudaGraphLaunch(h->gexec, h->stream));
     h->graph_launches++;
@@ -1586,6 +1651,7 @@ int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles,
   // eager operations after the solve act on every instance again
   CK(cudaMemcpyAsync(h->active.p, h->ones.p, sizeof(int) * h->ninst, cudaMemcpyDeviceToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  if (on_device) h->while_bodies += *std::max_element(h->res_iters.begin(), h->res_iters.end());
   return bsam_batch_result(h, 0, res_hist, hist_cap, vcycles, final_rel, visible_cells);
 }
 
@@ -1736,7 +1802,7 @@ int bsam_restore_state(bsam_hier h) {
 
 int bsam_launch_count(bsam_hier h, int64_t *count) {
   if (!h || !count) return fail(BSAM_ERR_ARG, "null argument");
-  *count = h->launch_count + h->graph_launches * h->kernels_per_cycle;
+  *count = h->launch_count + h->graph_launches * h->kernels_per_cycle + h->while_bodies * (h->kernels_per_cycle + 1);
   return BSAM_OK;
 }
 

@@ -906,6 +906,22 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__rest
 }
 
 // ---------------------------------------------------------------------------
+// Condition of the solve loop's device-side WHILE node: 1 while any instance
+// still iterates (ebSolveCycles.m:22, per instance).  One block; a single
+// thread sets the condition.
+__global__ void __launch_bounds__(kBlock) k_any_active(const int *__restrict__ active, int ninst,
+                                                       cudaGraphConditionalHandle cond) {
+  chain_in();
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < ninst; i += kBlock)
+    if (active[i]) any = 1;   // benign: every writer stores 1
+  __syncthreads();
+  if (threadIdx.x == 0) cudaGraphSetConditional(cond, any ? 1u : 0u);
+}
+
+// ---------------------------------------------------------------------------
 // Force reset F = FTrue (ebSolveCycles.m:30-34) of the active instances of a
 // batch, one thread per cell over every patch of every level (a single
 // hierarchy copies the whole array instead).
