@@ -340,6 +340,18 @@ def serving_form(rates, per_rate):
         d['waves'] = len(sizes)
         d['mean_wave_size'] = float(np.mean(sizes)) if sizes else 0.0
         out['rates'].append(d)
+    # a mixed stream: one request in four is a parabolic run (BDF2 heat,
+    # 10 steps with regrids) holding a wave slot for its whole run
+    from bsam.serve import heat_request
+    rate = 10.0
+    specs = [heat_request(50000 + i) if i % 4 == 3 else star_request(60000 + i) for i in range(40)]
+    res, wall = run_stream(srv, specs, rate=rate, seed=77)
+    d = summarize(res, wall)
+    d['offered_rate'] = rate
+    d['parabolic_share'] = 0.25
+    par = [r for r in res if r.spec.get('kind') == 'parabolic']
+    d['parabolic_p50_ms'] = float(np.percentile([r.latency_s * 1e3 for r in par], 50))
+    out['mixed_stream'] = d
     srv.close()
     return out
 

@@ -339,8 +339,13 @@ class DeviceBackend:
     # on the device between steps
     resident = True
 
-    def __init__(self, device=0):
-        self.ctx = Context(device)
+    def __init__(self, device=0, ctx=None):
+        self.ctx = ctx if ctx is not None else Context(device)
+
+    @classmethod
+    def on(cls, ctx):
+        """A backend issuing its work on an existing context (stream)."""
+        return cls(ctx.device, ctx)
 
     def ensure(self, H):
         """The resident copy of H: re-uploaded after a structural change,

@@ -19,6 +19,11 @@ builder spec) arrive at any time.  Each one goes through two stages:
          wave slot and memory are free, so its work overlaps the running
          waves on the device.
 
+A parabolic request (a time-stepping run, ebpSolve) is not merged: it holds
+one wave slot for its whole run, its hierarchy, coefficients and BDF2
+history resident on that slot's stream across steps and regrids, while
+other waves run beside it.
+
 Every instance of a wave keeps its own stop test and is frozen once it has
 converged, so a request's result is the same alone and in any mix.
 Latency is measured from submission to the solved result on the host.
@@ -56,6 +61,29 @@ def star_request(seed, precision='mixed'):
             break
     return {'kind': 'dd_star', 'seed': int(seed), 'k': k, 'b': b, 'a0': a0, 'th0': th0, 'eps': eps,
             'MaxLevels': ml, 'Precision': precision}
+
+
+def heat_request(seed, precision='fp64'):
+    """A served parabolic request: BDF2 heat diffusion on [0,1]^2 (D = 1,
+    C = 0, f = 0, homogeneous Neumann) from u0 = 1 + a cos(2 pi kx x)
+    cos(2 pi ky y), a ~ U[0.1, 0.3], kx, ky in {1, 2}, Dt 0.002, TFinal
+    0.02, RegridEvery 5, BaseCells 32, MaxLevels 3 -- the README heat
+    example's recipe, seeded."""
+    rng = np.random.Generator(np.random.PCG64(int(seed)))
+    return {'kind': 'parabolic', 'seed': int(seed), 'a': float(rng.uniform(0.1, 0.3)),
+            'kx': int(rng.integers(1, 3)), 'ky': int(rng.integers(1, 3)), 'Dt': 0.002, 'TFinal': 0.02,
+            'RegridEvery': 5, 'BaseCells': 32, 'MaxLevels': 3, 'Precision': precision}
+
+
+def run_parabolic(spec, backend):
+    """One parabolic request on a device backend (its own stream)."""
+    from .parabolic import ebpProblem, ebpSolve
+    a, kx, ky = spec['a'], spec['kx'], spec['ky']
+    u0 = lambda x, y: 1 + a * np.cos(2 * np.pi * kx * x) * np.cos(2 * np.pi * ky * y)
+    prob = ebpProblem([0, 1, 0, 1], 1, 0, 0, ('neumann', 0), u0)
+    return ebpSolve(prob, 'Scheme', 'bdf2', 'Dt', spec['Dt'], 'TFinal', spec['TFinal'], 'BaseCells',
+                    spec['BaseCells'], 'MaxLevels', spec['MaxLevels'], 'RegridEvery', spec['RegridEvery'],
+                    'StepVerbose', 0, 'Precision', spec.get('Precision', 'fp64'), backend=backend)
 
 
 def _worker_init():
@@ -200,6 +228,15 @@ class Server:
             fut = cf.Future()
             self.futures[rid] = fut
         times = {'submit': time.perf_counter()}
+        if spec.get('kind') == 'parabolic':
+            # no host set-up stage: the run sets up and steps on its slot
+            base = int(spec['BaseCells'])
+            built = {'flat': None, 'opts': {}, 'key': ('parabolic', rid), 'build_s': 0.0, 'solo': True,
+                     'footprint': int(400 * base * base * 4 ** (int(spec['MaxLevels']) - 1)) + (1 << 22)}
+            bf = cf.Future()
+            bf.set_result(built)
+            bf.add_done_callback(lambda f, rid=rid, spec=spec, times=times: self._built(rid, spec, f, times))
+            return fut
         if self.pool is not None:
             bf = self.pool.submit(self.build_fn, spec)
         else:
@@ -243,7 +280,7 @@ class Server:
         take, rest, used = [], deque(), 0
         for item in self.ready:
             b = item[2]
-            if (b['key'] == key and len(take) < self.wave_size and
+            if (b['key'] == key and len(take) < (1 if b.get('solo') else self.wave_size) and
                     self.inflight + used + b['footprint'] <= self.budget):
                 take.append(item)
                 used += b['footprint']
@@ -269,7 +306,17 @@ class Server:
 
     def _solve(self, slot, items):
         """One wave on the GPU: merged upload, ebSolveCycles of every
-        instance, per-instance solutions and histories."""
+        instance, per-instance solutions and histories (a parabolic request:
+        its whole run on the slot's stream)."""
+        if items[0][2].get('solo'):
+            from .device import DeviceBackend
+            from .flat import flatten
+            sol = run_parabolic(items[0][1], DeviceBackend.on(self.ctxs[slot]))
+            fl = flatten(sol['H'])
+            items[0][2]['flat'] = fl
+            items[0][2]['solution'] = sol
+            return [(fl.Q, int(np.sum(sol['cycles'])), np.asarray(sol['relres']), float(np.max(sol['relres'])),
+                     int(fl.F.size))]
         from .batch import merge_flats, split_field
         from .device import DevHier, BSAM_FIELD_Q
         from .flat import FIELD_Q
@@ -303,6 +350,7 @@ class Server:
                 times['done'] = time.perf_counter()
                 q, it, hist, rel, vis = res[i]
                 r = Result(rid, spec, q, built['flat'], it, hist, rel, vis, times)
+                r.solution = built.get('solution')
                 self.futures.pop(rid).set_result(r)
         except Exception as e:  # noqa: BLE001 -- every request of the wave learns of it
             self.errors.append(repr(e))

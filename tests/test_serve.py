@@ -166,3 +166,30 @@ def test_deferred_setup_equals_setup_on_device():
     Q = dh.get(BSAM_FIELD_Q, bb.Q.size)
     for i, fa in enumerate((a2, a3)):
         np.testing.assert_array_equal(split_field(bb, FIELD_Q, Q, i), fa.Q)
+
+
+@pytest.mark.gpu
+def test_parabolic_request_same_alone_and_beside_waves():
+    """A served parabolic run holds one wave slot with its state resident on
+    that stream; beside concurrent diffuse-domain waves it gives the same
+    steps and solution as alone, and the same as ebpSolve on the default
+    stream."""
+    from bsam.serve import build_spec, heat_request, run_parabolic
+    from bsam.device import DeviceBackend
+    spec = heat_request(7)
+    direct = run_parabolic(spec, DeviceBackend.get(0))
+    alone = Server(waves=1, wave_size=4, build_fn=build_spec)
+    ra = alone.submit(spec).result(timeout=600)
+    alone.close()
+    mix = Server(waves=3, wave_size=4, build_fn=build_spec)
+    with mix.lock:
+        futs = [mix.submit(spec)] + [mix.submit(dict(star_request(s), MaxLevels=3)) for s in (21, 22)]
+    rm = [f.result(timeout=600) for f in futs]
+    mix.close()
+    for r in (ra, rm[0]):
+        np.testing.assert_array_equal(r.solution['cycles'], direct['cycles'])
+        np.testing.assert_array_equal(r.solution['relres'], direct['relres'])
+        for k in range(1, direct['H'].nlev + 1):
+            for qa, qb in zip(direct['H'].lev[k].Q, r.solution['H'].lev[k].Q):
+                np.testing.assert_array_equal(qa[1:-1, 1:-1], qb[1:-1, 1:-1])
+    assert all(r.final_rel <= 1e-10 for r in rm[1:])
