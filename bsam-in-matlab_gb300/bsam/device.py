@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import time
 
 import numpy as np
 
@@ -102,6 +103,21 @@ def lib():
         L.bsam_tag_level.argtypes = [P, C.c_int, C.c_int, D, C.c_int, C.c_int, C.c_int, P]
         _lib = L
     return _lib
+
+
+_trace_path = os.environ.get('BSAM_TRACE')
+
+
+def trace(event, **fields):
+    """Append one JSON line per event to the file named by BSAM_TRACE (per
+    solve: V-cycles, residual history, final rel, wall ms)."""
+    if not _trace_path:
+        return
+    import json
+    rec = {'event': event, 'time': time.time()}
+    rec.update(fields)
+    with open(_trace_path, 'a') as f:
+        f.write(json.dumps(rec) + '\n')
 
 
 def check(rc):
@@ -204,8 +220,29 @@ class DevHier:
         it = C.c_int(0)
         rel = D(0)
         vis = I64(0)
+        t0 = time.perf_counter()
         check(lib().bsam_solve_cycles(self.h, _ptr(hist), hist.size, C.byref(it), C.byref(rel), C.byref(vis)))
-        return it.value, hist[:it.value + 1].copy(), rel.value, vis.value
+        out = it.value, hist[:it.value + 1].copy(), rel.value, vis.value
+        trace('solve_cycles', ms=1e3 * (time.perf_counter() - t0), vcycles=out[0], resHist=out[1].tolist(),
+              finalRel=out[2], visibleCells=out[3], ninst=int(getattr(self.fl, 'ninst', 1)))
+        return out
+
+    def checkpoint(self):
+        """Host snapshot of the solution state (Q, QC, F, FTrue and the
+        parabolic history when present), for a resume on a fresh upload."""
+        fl = self.fl
+        cp = {'Q': self.get(BSAM_FIELD_Q, fl.Q.size), 'QC': self.get(BSAM_FIELD_QC, fl.QC.size),
+              'F': self.get(BSAM_FIELD_F, fl.F.size), 'FTrue': self.get(BSAM_FIELD_FTRUE, fl.F.size)}
+        for name, which in (('Uo', BSAM_FIELD_UO), ('Uoo', BSAM_FIELD_UOO)):
+            cp[name] = self.get(which, fl.F.size)
+        return cp
+
+    def resume(self, cp):
+        """Load a checkpoint of the same hierarchy (same flat tables)."""
+        for name, which in (('Q', BSAM_FIELD_Q), ('QC', BSAM_FIELD_QC), ('F', BSAM_FIELD_F),
+                            ('FTrue', BSAM_FIELD_FTRUE), ('Uo', BSAM_FIELD_UO), ('Uoo', BSAM_FIELD_UOO)):
+            if name in cp:
+                self.set(which, cp[name])
 
     def batch_result(self, inst, hist_cap):
         """(vcycles, resHist, finalRel, visibleCells) of one instance of a
