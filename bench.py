@@ -229,6 +229,7 @@ def mixed_form(backend, fl, opts, ref_Q, steps, warmup, flush, local):
     return {'value': steps / (ms.sum() / 1e3), 'unit': 'solves/s', 'ms_per_solve': float(ms.mean()),
             'p50_ms': float(np.percentile(ms, 50)), 'p99_ms': float(np.percentile(ms, 99)),
             'vcycles': r[0], 'final_rel': r[2], 'rel_l2_vs_fp64': l2, 'rel_max_vs_fp64': mx,
+            'relax_cells_per_thread': dh.relax_tuning(1).tolist(),
             'dtype': 'f32 smoothing / f64 defect correction',
             'note': 'error against the FP64 path, which equals the C oracle bit for bit'}
 
@@ -292,7 +293,8 @@ def batched_form(backend, n, steps, warmup, flush, local):
                 worst_l2, worst_max = max(worst_l2, l2), max(worst_max, mx)
         d = {'value': n * steps / (ms.sum() / 1e3), 'unit': 'solves/s', 'ms_per_batch': float(ms.mean()),
              'p50_ms': float(np.percentile(ms, 50)), 'p99_ms': float(np.percentile(ms, 99)),
-             'vcycles_slowest': maxit, 'kernels_per_vcycle': bh.kernels_per_vcycle()}
+             'vcycles_slowest': maxit, 'kernels_per_vcycle': bh.kernels_per_vcycle(),
+             'relax_cells_per_thread': bh.relax_tuning(1 if prec == 'mixed' else 0).tolist()}
         # smoother roofline per merged level (levels larger than L2 here)
         peak, peak_kind = load_peaks()
         cells = [int(b.levels[k - 1, 5] - b.levels[k - 1, 4]) for k in range(1, b.nlev + 1)]
@@ -514,7 +516,8 @@ def main():
                        'l2': 'flushed between solves (256 MiB write)', 'vcycles_per_solve': it,
                        'final_rel': rel, 'visible_cells': vis, 'stored_cells': int(fl.F.size - 0),
                        'p50_ms': float(np.percentile(per, 50)), 'p99_ms': float(np.percentile(per, 99)),
-                       'kernels_per_vcycle': dh.kernels_per_vcycle(), 'per_kernel': per_kind},
+                       'kernels_per_vcycle': dh.kernels_per_vcycle(), 'per_kernel': per_kind,
+                       'relax_cells_per_thread': dh.relax_tuning(0).tolist()},
             'e2e': {'value': e2e_value, 'unit': 'solves/s',
                     'h2d_bytes_per_step': int(8 * (Q0.size + F0.size)),
                     'd2h_bytes_per_step': int(8 * Qout.size + hist_bytes),

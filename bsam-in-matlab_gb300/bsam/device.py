@@ -93,6 +93,7 @@ def lib():
         L.bsam_save_state.argtypes = [P]
         L.bsam_restore_state.argtypes = [P]
         L.bsam_launch_count.argtypes = [P, C.POINTER(I64)]
+        L.bsam_relax_tuning.argtypes = [P, C.c_int, P, C.c_int]
         L.bsam_batch_result.argtypes = [P, C.c_int, P, C.c_int, C.POINTER(C.c_int), C.POINTER(D), C.POINTER(I64)]
         L.bsam_batch_set_stop.argtypes = [P, C.c_int, C.c_int, D]
         L.bsam_polygon_dist2.argtypes = [P, P, C.c_int, P, P, P, I64]
@@ -321,6 +322,12 @@ class DevHier:
         n = I64(0)
         check(lib().bsam_launch_count(self.h, C.byref(n)))
         return n.value
+
+    def relax_tuning(self, precision=0):
+        """Colour cells per smoother thread, levels 1..nlev, as tuned."""
+        out = np.zeros(int(self.fl.nlev), np.int32)
+        check(lib().bsam_relax_tuning(self.h, int(precision), out.ctypes.data, out.size))
+        return out
 
     def kernels_per_vcycle(self):
         n = I64(0)

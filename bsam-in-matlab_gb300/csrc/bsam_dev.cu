@@ -176,6 +176,10 @@ struct bsam_hier_s {
   int64_t launch_count = 0;
   int64_t graph_launches = 0;
   int64_t while_bodies = 0;        // iterations run inside WHILE graphs
+  // per precision and level: colour cells per smoother thread (1, 2, 4),
+  // picked by the autotuner at the first solve (result-neutral)
+  std::vector<int> relax_n[2];
+  bool tuned[2] = {false, false};
   DBuf<double> saveQ, saveQC, saveF;
 };
 
@@ -341,10 +345,26 @@ void launch_relax(bsam_hier h, int k, int nsweeps, bool first_fresh = false) {
   const T *pk = relax_pack<T>(h) + (size_t)L.rc_off * 2 * kPackRows * kChunk;
   const int grid = (L.rc_n + kBlock / kChunk - 1) / (kBlock / kChunk);
   const int unit = h->opts.omega == 1.0 ? 1 : 0;
+  const std::vector<int> &rn = h->relax_n[sizeof(T) == sizeof(float) ? 1 : 0];
+  const int kn = rn.empty() ? 1 : rn[k];
   for (int s = 0; s < nsweeps; ++s)
     for (int m = 0; m < 2; ++m) {
       const int fresh = (first_fresh || s > 0 || m > 0) ? 1 : 0;
       Launch l(h, K_RELAX, 24.0 * tscale<T>() * (double)L.ncells, k);
+      if (kn > 1) {
+        const int cpb = kBlock * kn / kChunk;     // chunks per block
+        const int g = (L.rc_n + cpb - 1) / cpb;
+        const Rule *pr = (const Rule *)h->perim.p;
+        const T om = (T)h->opts.omega;
+        if (kn == 2) {
+          if (L.pow2) launch_k(h, k_relax_n<T, true, 2>, g, kBlock, ld, ch, L.rc_n, f, pk, pr, m, om, unit, fresh);
+          else launch_k(h, k_relax_n<T, false, 2>, g, kBlock, ld, ch, L.rc_n, f, pk, pr, m, om, unit, fresh);
+        } else {
+          if (L.pow2) launch_k(h, k_relax_n<T, true, 4>, g, kBlock, ld, ch, L.rc_n, f, pk, pr, m, om, unit, fresh);
+          else launch_k(h, k_relax_n<T, false, 4>, g, kBlock, ld, ch, L.rc_n, f, pk, pr, m, om, unit, fresh);
+        }
+        continue;
+      }
       if (L.pow2)
         launch_k(h, k_relax<T, true>, grid, kBlock, ld, ch, L.rc_n, f, pk, (const Rule *)h->perim.p, m,
                  (T)h->opts.omega, unit, fresh);
@@ -502,6 +522,56 @@ int launch_iteration(bsam_hier h, int mode) {
   return BSAM_OK;
 }
 
+// Autotuner of the smoother's thread coarsening: for each level large enough
+// to matter, time two sweeps with 1, 2 and 4 colour cells per thread (best of
+// three, CUDA events on the stream) in the precision the cycle runs in, and
+// keep the fastest.  The choice does not change a single bit of the result
+// (each update's arithmetic is the same), so it is tuned on the live state
+// and the FP64 state is restored afterwards.  BSAM_RELAX_N=1|2|4 forces one
+// value on every level.
+constexpr int64_t kTuneMinCells = 131072;
+
+template <class T>
+int tune_level(bsam_hier h, int k, int *best) {
+  std::vector<int> &rn = h->relax_n[sizeof(T) == sizeof(float) ? 1 : 0];
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  float bt = 1e30f;
+  *best = 1;
+  for (int kn : {1, 2, 4}) {
+    rn[k] = kn;
+    launch_relax<T>(h, k, 1);          // warm-up
+    float t = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(a, h->stream);
+      launch_relax<T>(h, k, 2);
+      cudaEventRecord(b, h->stream);
+      CK(cudaEventSynchronize(b));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      t = std::min(t, ms);
+    }
+    if (t < bt * 0.97f) {              // a change must win clearly
+      bt = t;
+      *best = kn;
+    }
+  }
+  rn[k] = *best;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  CK(cudaGetLastError());
+  return BSAM_OK;
+}
+
+int autotune(bsam_hier h);
+
+uint64_t tune_key(int precision, bool pow2, int chunks) {
+  int b = 0;
+  while ((chunks >> (b + 1)) > 0) ++b;
+  return ((uint64_t)precision << 40) | ((uint64_t)pow2 << 32) | (uint64_t)b;
+}
+
 // FP32 arrays of the mixed form: allocated on first use, coefficient copies
 // refreshed whenever the FP64 coefficients changed
 int ensure_f32(bsam_hier h) {
@@ -530,6 +600,60 @@ int ensure_f32(bsam_hier h) {
     h->f32_dirty = false;
   }
   return BSAM_OK;
+}
+
+int autotune(bsam_hier h) {
+  const int p = mixed(h) ? 1 : 0;
+  if (h->tuned[p]) return BSAM_OK;
+  h->tuned[p] = true;
+  std::vector<int> &rn = h->relax_n[p];
+  rn.assign(h->nlev + 1, 1);
+  if (const char *env = getenv("BSAM_RELAX_N")) {
+    const int kn = atoi(env);
+    rn.assign(h->nlev + 1, (kn == 2 || kn == 4) ? kn : 1);
+    return BSAM_OK;
+  }
+  // levels already measured on this context (same precision, same h^2 form,
+  // chunk count within a factor of two) take the cached choice
+  bsam_ctx_s *c = h->ctx;
+  std::vector<int> todo;
+  {
+    std::lock_guard<std::mutex> lk(c->tune_mu);
+    for (int k = 2; k <= h->nlev; ++k) {
+      if (h->lev[k].ncells < kTuneMinCells) continue;
+      auto it = c->relax_tune.find(tune_key(p, h->lev[k].pow2, h->lev[k].rc_n));
+      if (it != c->relax_tune.end()) rn[k] = it->second;
+      else todo.push_back(k);
+    }
+  }
+  if (todo.empty()) return BSAM_OK;
+  // the FP64 smoother runs on the solution itself: keep a copy to put back
+  // (the FP32 correction is zeroed at the start of every correction cycle)
+  DBuf<double> keep;
+  int rc = BSAM_OK;
+  if (!p) {
+    if ((rc = keep.alloc(h->Q.n))) return rc;
+    CK(cudaMemcpyAsync(keep.p, h->Q.p, sizeof(double) * h->Q.n, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  const bool prof = h->profiling;
+  const int64_t lc = h->launch_count;
+  h->profiling = false;
+  for (int k : todo) {
+    int best = 1;
+    rc = p ? tune_level<float>(h, k, &best) : tune_level<double>(h, k, &best);
+    if (rc) break;
+    std::lock_guard<std::mutex> lk(c->tune_mu);
+    c->relax_tune[tune_key(p, h->lev[k].pow2, h->lev[k].rc_n)] = best;
+  }
+  h->profiling = prof;
+  h->launch_count = lc;
+  if (!p) {
+    cudaError_t e = cudaMemcpyAsync(h->Q.p, keep.p, sizeof(double) * h->Q.n, cudaMemcpyDeviceToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    keep.release();
+    if (!rc && e != cudaSuccess) rc = cuda_fail(e, "autotune restore");
+  }
+  return rc;
 }
 
 int build_graph(bsam_hier h) {
@@ -1109,6 +1233,8 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
     h->hID.assign(d->InvDiagS, d->InvDiagS + d->n_cells);
     h->hchunks = B.chunks;
     if ((rc = build_relax_pack(h))) return rc;
+    h->relax_n[0].assign(d->nlev + 1, 1);
+    h->relax_n[1].assign(d->nlev + 1, 1);
   }
   // residual plan: warp tasks, slots in instance order, level by level
   constexpr int kTask = 32 * kResLane;
@@ -1631,6 +1757,7 @@ int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles,
   // others continue.  The loop runs on the device when the runtime can build
   // its WHILE graph, else one graph launch per V-cycle with a host check.
   bool on_device = false;
+  if (nactive && (rc = autotune(h))) return rc;
   if (nactive && build_while_graph(h)) {
     CK(cudaGraphLaunch(h->wexec, h->stream));
     if ((rc = read_state(h, &nactive))) return rc;
@@ -1806,6 +1933,15 @@ int bsam_launch_count(bsam_hier h, int64_t *count) {
   return BSAM_OK;
 }
 
+int bsam_relax_tuning(bsam_hier h, int precision, int32_t *cells_per_thread, int cap) {
+  if (!h || !cells_per_thread) return fail(BSAM_ERR_ARG, "null argument");
+  if (precision != 0 && precision != 1) return fail(BSAM_ERR_ARG, "precision must be 0 or 1");
+  const std::vector<int> &rn = h->relax_n[precision];
+  for (int k = 1; k <= h->nlev && k <= cap; ++k)
+    cells_per_thread[k - 1] = h->tuned[precision] && (int)rn.size() > k ? rn[k] : 0;
+  return BSAM_OK;
+}
+
 int bsam_stream(bsam_hier h, void **stream) {
   if (!h || !stream) return fail(BSAM_ERR_ARG, "null argument");
   *stream = (void *)h->stream;
@@ -1832,6 +1968,7 @@ int bsam_profile_vcycles(bsam_hier h, int ncycles, int level, double ms[BSAM_NKI
     launch_consistent(h);
     launch_residual(h, 2);
   }
+  if ((rc = autotune(h))) return rc;
   h->profiling = true;
   h->profile_level = level;
   h->recs.clear();

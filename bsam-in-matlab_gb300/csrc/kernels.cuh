@@ -316,6 +316,126 @@ __device__ __forceinline__ void relax_cell(const LevelD &L, const RelaxChunk *__
   else Q[c] = omega * t + (1 - omega) * Q[c];
 }
 
+// Coarsened smoother: each thread updates kN colour cells of its chunk
+// (cells t, t + kChunk/kN, ...), in three phases -- static loads of every
+// cell, then the solution loads of every cell, then every update -- so the
+// loads of a thread's cells are in flight together.  Within a colour pass no
+// cell reads another cell of its colour (a ghost rule reads cells of the
+// other colour, parent cells or the reading cell itself, before its update),
+// so loading all before storing any changes nothing: the arithmetic of each
+// update is relax_cell's.
+template <class T, bool kPow2, int kN>
+__global__ void __launch_bounds__(kBlock) k_relax_n(LevelD L, const RelaxChunk *__restrict__ chunks, int nchunks,
+                                                    FieldsT<T> f, const T *__restrict__ pack,
+                                                    const Rule *__restrict__ perim, int m, T omega, int unit_omega,
+                                                    int fresh) {
+  chain_trigger();
+  constexpr int tpc = kChunk / kN;                    // threads per chunk
+  const int ch = blockIdx.x * (kBlock / tpc) + threadIdx.x / tpc;
+  const int t0 = threadIdx.x % tpc;
+  bool okc = ch < nchunks;
+  RelaxChunk R;
+  if (okc) R = chunks[ch];
+  okc = okc && f.active[R.inst];
+  if (!okc) {
+    chain_wait();
+    return;
+  }
+  const int mx = R.mx, my = R.my, half = mx >> 1, ldq = mx + 2;
+  const T *__restrict__ g4 = f.bcg + R.bcg_off;
+  const T *__restrict__ pk0 = pack + (size_t)(ch * 2 + m) * (kPackRows * kChunk);
+  bool on[kN];
+  int c[kN], cc[kN], code[kN], rxi[kN], ryi[kN];    // code: kx | ky << 2 | sx << 4 | sy << 5
+  T dE[kN], dW[kN], dN[kN], dS[kN], idg[kN], gx[kN], gy[kN];
+#pragma unroll
+  for (int u = 0; u < kN; ++u) {
+    const int tc = t0 + u * tpc;
+    on[u] = tc < R.n;
+    const int s = R.s0 + (on[u] ? tc : 0);
+    const int lj = s / half;
+    const int li = 2 * (s - lj * half) + ((m + lj + R.par0) & 1);
+    c[u] = (li + 1) + (lj + 1) * ldq;
+    cc[u] = R.c_off + li + lj * mx;
+    const T *__restrict__ pk = pk0 + (on[u] ? tc : 0);
+    dE[u] = __ldg(pk);
+    dW[u] = __ldg(pk + kChunk);
+    dN[u] = __ldg(pk + 2 * kChunk);
+    dS[u] = __ldg(pk + 3 * kChunk);
+    idg[u] = __ldg(pk + 4 * kChunk);
+    int kx = 0, ky = 0, sx = 0, sy = 0;
+    gx[u] = 0;
+    gy[u] = 0;
+    rxi[u] = 0;
+    ryi[u] = 0;
+    if (li == 0 || li == mx - 1) {
+      sx = (li == 0) ? 0 : 1;
+      const int bc = sx ? R.bc[1] : R.bc[0];
+      if (bc) { kx = bc; gx[u] = __ldg(g4 + sx * my + lj); }
+      else if (fresh) { kx = 3; rxi[u] = R.pe_off + sx * my + lj; }
+    }
+    if (lj == 0 || lj == my - 1) {
+      sy = (lj == 0) ? 0 : 1;
+      const int bc = sy ? R.bc[3] : R.bc[2];
+      if (bc) { ky = bc; gy[u] = __ldg(g4 + 2 * my + sy * mx + li); }
+      else if (fresh) { ky = 3; ryi[u] = R.pe_off + 2 * my + sy * mx + li; }
+    }
+    code[u] = kx | (ky << 2) | (sx << 4) | (sy << 5);
+  }
+  chain_wait();
+  const T c83 = T(8.0 / 3.0), c13 = T(1.0 / 3.0);
+  const LevelH<T> H = level_h(L, T(0));
+  T *__restrict__ Q = f.Q + R.q_off;
+  T qe[kN], qw[kN], qn[kN], qs[kN], fv[kN], qc[kN];
+#pragma unroll
+  for (int u = 0; u < kN; ++u) {
+    const int cu = c[u];
+    qe[u] = Q[cu + 1];
+    qw[u] = Q[cu - 1];
+    qn[u] = Q[cu + ldq];
+    qs[u] = Q[cu - ldq];
+    qc[u] = unit_omega ? T(0) : Q[cu];
+    fv[u] = f.F[cc[u]];
+  }
+#pragma unroll
+  for (int u = 0; u < kN; ++u) {
+    const int kx = code[u] & 3, ky = (code[u] >> 2) & 3, sx = (code[u] >> 4) & 1, sy = (code[u] >> 5) & 1;
+    const int cu = c[u];
+    if (kx > 0) {
+      T v;
+      if (kx == 1) v = c83 * gx[u] + c13 * Q[sx ? cu - 1 : cu + 1];
+      else if (kx == 2) v = H.hx * gx[u];
+      else v = eval_inline<T>(perim[rxi[u]], f.Q);
+      if (sx) qe[u] = v; else qw[u] = v;
+    }
+    if (ky > 0) {
+      T v;
+      if (ky == 1) v = c83 * gy[u] + c13 * Q[sy ? cu - ldq : cu + ldq];
+      else if (ky == 2) v = H.hy * gy[u];
+      else v = eval_inline<T>(perim[ryi[u]], f.Q);
+      if (sy) qn[u] = v; else qs[u] = v;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kN; ++u) {
+    if (!on[u]) continue;
+    T t = fv[u];
+    if (kPow2) {
+      t = t + qe[u] * dE[u];
+      t = t + qw[u] * dW[u];
+      t = t + qn[u] * dN[u];
+      t = t + qs[u] * dS[u];
+    } else {
+      t = t + (qe[u] * dE[u]) / H.hx2;
+      t = t + (qw[u] * dW[u]) / H.hx2;
+      t = t + (qn[u] * dN[u]) / H.hy2;
+      t = t + (qs[u] * dS[u]) / H.hy2;
+    }
+    t = t * idg[u];
+    if (unit_omega) Q[c[u]] = t;
+    else Q[c[u]] = omega * t + (1 - omega) * qc[u];
+  }
+}
+
 template <class T, bool kPow2>
 __global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__restrict__ chunks, int nchunks,
                                                   FieldsT<T> f, const T *__restrict__ pack,

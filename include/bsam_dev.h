@@ -229,6 +229,15 @@ int bsam_restore_state(bsam_hier h);
 /* Kernels launched on this hierarchy so far (eager and graph-replayed). */
 int bsam_launch_count(bsam_hier h, int64_t *count);
 
+/* The smoother's thread coarsening per level as the autotuner chose it at
+ * the first solve: colour cells updated per thread (1, 2 or 4) of levels
+ * 1..nlev in cells_per_thread[0..nlev-1], for precision 0 (FP64 cycle) or
+ * 1 (FP32 correction cycle); 0 where that cycle has not run yet.  The
+ * choice never changes a result bit; BSAM_RELAX_N=1|2|4 in the environment
+ * forces one value.  No reference counterpart (ebRelaxLevel.m has one
+ * loop order).                                                            */
+int bsam_relax_tuning(bsam_hier h, int precision, int32_t *cells_per_thread, int cap);
+
 /* Number of kernels one V-cycle (+ fill-down + residual) launches. */
 int bsam_kernels_per_vcycle(bsam_hier h, int64_t *count);
 

@@ -1,0 +1,50 @@
+"""Smoother autotuner: the colour cells updated per thread (1, 2 or 4) are
+picked per level and precision at the first solve of a hierarchy, by timing
+the candidates on the live state.  The choice may differ run to run, so it
+must never change a result bit: each forced setting (BSAM_RELAX_N) and the
+tuned one give the same V-cycle count, residual history and solution, in the
+FP64 cycle (ebRelaxLevel.m:28-38 per sweep) and the FP32 correction cycle.
+"""
+import numpy as np
+import pytest
+
+from bsam import ebOptions
+from bsam.flat import flatten
+from bsam.solve import build_hierarchy
+from bsam_oracle import OracleBackend
+from cases import vardc_problem
+
+pytestmark = pytest.mark.gpu
+
+WIDE_BAND = lambda x, y: np.abs(x - y) < 0.4
+
+
+def _flat(precision):
+    o = ebOptions('BaseCells', 128, 'MaxLevels', 3, 'Indicator', 'fun', 'TagFunction', WIDE_BAND, 'Verbose', 0,
+                  'RelTol', 1e-10, 'Precision', precision)
+    return flatten(build_hierarchy(vardc_problem(), o, OracleBackend())), o
+
+
+def _solve(fl, o):
+    from bsam.device import DeviceBackend, DevHier, BSAM_FIELD_Q
+    dh = DevHier(DeviceBackend.get(0).ctx, fl, o)
+    it, hist, rel, _ = dh.solve_cycles(o.MaxVCycles + 2)
+    return dh, it, hist, dh.get(BSAM_FIELD_Q, fl.Q.size)
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+def test_every_coarsening_gives_the_same_bits(precision, monkeypatch):
+    fl, o = _flat(precision)
+    monkeypatch.delenv('BSAM_RELAX_N', raising=False)
+    dh, it, hist, Q = _solve(fl, o)
+    p = 1 if precision == 'mixed' else 0
+    tuned = dh.relax_tuning(p)
+    assert set(tuned.tolist()) <= {1, 2, 4} and tuned[0] == 1
+    assert np.all(dh.relax_tuning(1 - p) == 0)      # that cycle never ran
+    for kn in (1, 2, 4):
+        monkeypatch.setenv('BSAM_RELAX_N', str(kn))
+        dk, itk, histk, Qk = _solve(fl, o)
+        assert np.all(dk.relax_tuning(p) == kn)
+        assert itk == it
+        np.testing.assert_array_equal(histk, hist)
+        np.testing.assert_array_equal(Qk, Q)
