@@ -151,7 +151,10 @@ struct bsam_hier_s {
   DBuf<PatchD> patches;
   DBuf<ResAcc> acc;
   DBuf<Rule> perim;                // per-patch perimeter ghost rules (inline)
-  DBuf<RelaxChunk> rchunks;        // relax chunk records, all levels
+  DBuf<RelaxChunkD> rchunks;       // relax chunk records as the kernels read them, all levels
+  DBuf<uint8_t> cact;              // per chunk: its instance still iterates (batches, kActChunk)
+  DBuf<int> crange;                // per instance and level: its chunk range [begin, end)
+  int act_mode = 0;                // kActNone / kActChunk / kActInst
   DBuf<LevelX> levelx;             // per-level descriptors for the residual
   DBuf<ResTask> rtasks;            // residual warp tasks
   DBuf<InstRes> instres;           // per-instance residual reduction plan
@@ -341,10 +344,12 @@ void launch_relax(bsam_hier h, int k, int nsweeps, bool first_fresh = false) {
   const LevelPlan &L = h->lev[k];
   FieldsT<T> f = fields_t<T>(h);
   LevelD ld = leveld(h, k);
-  const RelaxChunk *ch = h->rchunks.p + L.rc_off;
+  const RelaxChunkD *ch = h->rchunks.p + L.rc_off;
   const T *pk = relax_pack<T>(h) + (size_t)L.rc_off * 2 * kPackRows * kChunk;
   const int grid = (L.rc_n + kBlock / kChunk - 1) / (kBlock / kChunk);
   const int unit = h->opts.omega == 1.0 ? 1 : 0;
+  const uint8_t *ca = h->act_mode == kActChunk ? h->cact.p + L.rc_off : nullptr;
+  const int am = h->act_mode;
   const std::vector<int> &rn = h->relax_n[sizeof(T) == sizeof(float) ? 1 : 0];
   const int kn = rn.empty() ? 1 : rn[k];
   for (int s = 0; s < nsweeps; ++s)
@@ -357,20 +362,20 @@ void launch_relax(bsam_hier h, int k, int nsweeps, bool first_fresh = false) {
         const Rule *pr = (const Rule *)h->perim.p;
         const T om = (T)h->opts.omega;
         if (kn == 2) {
-          if (L.pow2) launch_k(h, k_relax_n<T, true, 2>, g, kBlock, ld, ch, L.rc_n, f, pk, pr, m, om, unit, fresh);
-          else launch_k(h, k_relax_n<T, false, 2>, g, kBlock, ld, ch, L.rc_n, f, pk, pr, m, om, unit, fresh);
+          if (L.pow2) launch_k(h, k_relax_n<T, true, 2>, g, kBlock, ld, ch, L.rc_n, f, pk, pr, m, om, unit, fresh, ca, am);
+          else launch_k(h, k_relax_n<T, false, 2>, g, kBlock, ld, ch, L.rc_n, f, pk, pr, m, om, unit, fresh, ca, am);
         } else {
-          if (L.pow2) launch_k(h, k_relax_n<T, true, 4>, g, kBlock, ld, ch, L.rc_n, f, pk, pr, m, om, unit, fresh);
-          else launch_k(h, k_relax_n<T, false, 4>, g, kBlock, ld, ch, L.rc_n, f, pk, pr, m, om, unit, fresh);
+          if (L.pow2) launch_k(h, k_relax_n<T, true, 4>, g, kBlock, ld, ch, L.rc_n, f, pk, pr, m, om, unit, fresh, ca, am);
+          else launch_k(h, k_relax_n<T, false, 4>, g, kBlock, ld, ch, L.rc_n, f, pk, pr, m, om, unit, fresh, ca, am);
         }
         continue;
       }
       if (L.pow2)
         launch_k(h, k_relax<T, true>, grid, kBlock, ld, ch, L.rc_n, f, pk, (const Rule *)h->perim.p, m,
-                 (T)h->opts.omega, unit, fresh);
+                 (T)h->opts.omega, unit, fresh, ca, am);
       else
         launch_k(h, k_relax<T, false>, grid, kBlock, ld, ch, L.rc_n, f, pk, (const Rule *)h->perim.p, m,
-                 (T)h->opts.omega, unit, fresh);
+                 (T)h->opts.omega, unit, fresh, ca, am);
     }
   launch_fill<T>(h, k);
 }
@@ -475,7 +480,8 @@ void launch_residual(bsam_hier h, int mode) {
   }
   Launch l(h, K_RESID, 0);
   launch_k(h, k_residual_final, h->ninst, kFinal, (const InstRes *)h->instres.p, (const SlotRange *)h->sranges.p,
-           (const double *)h->slots.p, h->nslots, h->acc.p, h->active.p, h->iters.p, h->hist.p, h->hist_stride, mode);
+           (const double *)h->slots.p, h->nslots, h->acc.p, h->active.p, h->iters.p, h->hist.p, h->hist_stride, mode,
+           (const int *)h->crange.p, h->nlev, h->act_mode == kActChunk ? h->cact.p : nullptr);
 }
 
 // Mixed form: after Q changed on every level at once (or before the first
@@ -1211,9 +1217,40 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
   for (int p = 0; p < d->npatch; ++p) pd[p].pe_off = B.pe_off[p];
   if ((rc = h->patches.upload(pd.data(), pd.size(), s))) return rc;
   if (B.perim.empty()) B.perim.push_back(Rule{-1, 0, 0, 0, 0, 0});
+  std::vector<RelaxChunkD> dchunks(B.chunks.size());
+  for (size_t i = 0; i < B.chunks.size(); ++i) {
+    const RelaxChunk &c = B.chunks[i];
+    int fl = (c.par0 & 1) << 8;
+    for (int sd = 0; sd < 4; ++sd) fl |= c.bc[sd] << (2 * sd);   // codes 0..2, checked above
+    dchunks[i] = RelaxChunkD{c.q_off, c.c_off, c.bcg_off, c.pe_off, c.mx, c.my, c.s0, c.n, c.inst, fl, 0, 0};
+  }
   if ((rc = h->perim.upload(B.perim.data(), B.perim.size(), s)) ||
-      (rc = h->rchunks.upload(B.chunks.data(), B.chunks.size(), s)))
+      (rc = h->rchunks.upload(dchunks.data(), dchunks.size(), s)))
     return rc;
+  // frozen-chunk flags of a batch: each instance's chunks must form one
+  // range per level (instances stored one after another within a level),
+  // else the smoother reads the instance flag through the chunk record
+  h->act_mode = h->ninst > 1 ? kActChunk : kActNone;
+  if (h->ninst > 1) {
+    const int nl = d->nlev;
+    std::vector<int> cr((size_t)h->ninst * nl * 2, 0), cnt((size_t)h->ninst * nl, 0);
+    for (int k = 1; k <= nl; ++k) {
+      const LevelPlan &L = h->lev[k];
+      for (int c = L.rc_off; c < L.rc_off + L.rc_n; ++c) {
+        const size_t e = (size_t)B.chunks[c].inst * nl + (k - 1);
+        if (!cnt[e]) cr[2 * e] = c;
+        cr[2 * e + 1] = c + 1;
+        ++cnt[e];
+      }
+    }
+    for (size_t e = 0; e < cnt.size(); ++e)
+      if (cnt[e] && cnt[e] != cr[2 * e + 1] - cr[2 * e]) h->act_mode = kActInst;
+    if (h->act_mode == kActChunk) {
+      if ((rc = h->crange.upload(cr.data(), cr.size(), s)) || (rc = h->cact.alloc(std::max<size_t>(B.chunks.size(), 1))))
+        return rc;
+      CK(cudaMemsetAsync(h->cact.p, 1, h->cact.n, s));
+    }
+  }
   // smoother coefficients, exactly scaled by 1/h^2 on power-of-two levels
   {
     std::vector<double> dew(d->DeW, d->DeW + d->n_dew), dns(d->DnS, d->DnS + d->n_dns);
@@ -1392,7 +1429,7 @@ void release(bsam_hier h) {
                        &h->ct_j, &h->active, &h->iters, &h->ones, &h->g_inst, &h->ring_inst, &h->inst_nlev, &h->g_dst, &h->g_a, &h->g_b, &h->g_c, &h->g_d, &h->g_e})
     b->release();
   h->flags.release(); h->g_type.release(); h->patches.release(); h->acc.release(); h->perim.release();
-  h->rchunks.release(); h->levelx.release(); h->rtasks.release(); h->instres.release(); h->sranges.release();
+  h->rchunks.release(); h->cact.release(); h->crange.release(); h->levelx.release(); h->rtasks.release(); h->instres.release(); h->sranges.release();
   h->coarsest.release();
   if (h->acc_host) cudaFreeHost(h->acc_host);
   if (h->active_host) cudaFreeHost(h->active_host);
@@ -1777,6 +1814,7 @@ int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles,
   CK(cudaMemcpyAsync(h->res_iters.data(), h->iters.p, sizeof(int) * h->ninst, cudaMemcpyDeviceToHost, h->stream));
   // eager operations after the solve act on every instance again
   CK(cudaMemcpyAsync(h->active.p, h->ones.p, sizeof(int) * h->ninst, cudaMemcpyDeviceToDevice, h->stream));
+  if (h->act_mode == kActChunk) CK(cudaMemsetAsync(h->cact.p, 1, h->cact.n, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   if (on_device) h->while_bodies += *std::max_element(h->res_iters.begin(), h->res_iters.end());
   return bsam_batch_result(h, 0, res_hist, hist_cap, vcycles, final_rel, visible_cells);

@@ -201,12 +201,30 @@ __global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, 
 // ghosts as the last fill left them, as the reference does.
 constexpr int kChunk = 64;
 
-struct RelaxChunk {
+struct RelaxChunk {           // host record (packing of the operands)
   int q_off, c_off, dew_off, dns_off;
   int bcg_off, pe_off, mx, my;
   int par0, s0, n, inst;     // first colour-cell index in the patch, cells in the chunk, instance
   int bc[4];
 };
+
+// the chunk as the smoother kernels read it: three 16-byte words (three
+// vector loads, ten registers); flags holds the W, E, S, N boundary codes in
+// 2-bit fields and par0 in bit 8
+struct __align__(16) RelaxChunkD {
+  int q_off, c_off, bcg_off, pe_off;
+  int mx, my, s0, n;
+  int inst, flags, pad0, pad1;
+};
+
+// how a smoother chunk learns that its instance is frozen: kActNone, one
+// instance (always live while a V-cycle runs); kActChunk, the per-chunk flag
+// array k_residual_final keeps (instances' chunks contiguous per level);
+// kActInst, the instance's flag through the chunk record
+enum { kActNone = 0, kActChunk = 1, kActInst = 2 };
+
+__device__ __forceinline__ int chunk_bc(int flags, int side) { return (flags >> (2 * side)) & 3; }
+__device__ __forceinline__ int chunk_par0(int flags) { return (flags >> 8) & 1; }
 
 struct Rule {                // one ghost rule, inline (perimeter table)
   int type, a, b, c, d, e;
@@ -232,74 +250,97 @@ __device__ __forceinline__ T eval_inline(const Rule &R, const T *Q) {
 // every other value of the reference's arrays.
 constexpr int kPackRows = 5;
 
+// a static table row (never written while kernels run) brought into L1
+// before the programmatic-launch wait; the read after the wait then hits L1
+// without holding the row in registers across the wait
+template <class R>
+__device__ __forceinline__ void prefetch_l1(const R *p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+  asm volatile("prefetch.global.L1 [%0];" ::"l"((const char *)(p + 1) - 1));
+}
+
 // one colour-cell update of chunk ch (thread tc of the chunk); kChain: the
 // grid kernel's programmatic-launch wait sits between the static loads and
 // the first read of the solution
 template <class T, bool kPow2, bool kChain>
-__device__ __forceinline__ void relax_cell(const LevelD &L, const RelaxChunk *__restrict__ chunks, int nchunks,
+__device__ __forceinline__ void relax_cell(const LevelD &L, const RelaxChunkD *__restrict__ chunks, int nchunks,
                                            const FieldsT<T> &f, const T *__restrict__ pack,
                                            const Rule *__restrict__ perim, int m, T omega, int unit_omega, int fresh,
-                                           int ch, int tc) {
-  bool ok = ch < nchunks;
-  RelaxChunk R;
-  if (ok) R = chunks[ch];
-  const int s = ok ? R.s0 + tc : 0;
-  ok = ok && s < R.s0 + R.n && f.active[R.inst];
-  if (!ok) {
+                                           const uint8_t *__restrict__ cact, int amode, int ch, int tc) {
+  // the chunk record, its frozen flag and the packed operands are indexed
+  // by the chunk alone: record and flag are requested together, the
+  // operands (a chunk's pack rows hold kChunk entries whatever its cell
+  // count) as soon as the small, cached flag says the chunk is live, so
+  // they are in flight with the record and a frozen chunk reads nothing else
+  const bool okc = ch < nchunks;
+  RelaxChunkD R;
+  bool live = okc;
+  T dE = 0, dW = 0, dN = 0, dS = 0, idg = 0;
+  if (okc) {
+    R = chunks[ch];
+    if (amode == kActChunk) live = cact[ch] != 0;
+  }
+  if (live) {
+    const T *__restrict__ pk = pack + (size_t)(ch * 2 + m) * (kPackRows * kChunk) + tc;
+    dE = __ldg(pk);
+    dW = __ldg(pk + kChunk);
+    dN = __ldg(pk + 2 * kChunk);
+    dS = __ldg(pk + 3 * kChunk);
+    idg = __ldg(pk + 4 * kChunk);
+  }
+  if (!live || tc >= R.n || (amode == kActInst && !f.active[R.inst])) {
     if (kChain) chain_wait();
     return;
   }
+  const int s = R.s0 + tc;
   const int mx = R.mx, my = R.my, half = mx >> 1;
   const int lj = s / half;
-  const int li = 2 * (s - lj * half) + ((m + lj + R.par0) & 1);
+  const int li = 2 * (s - lj * half) + ((m + lj + chunk_par0(R.flags)) & 1);
   const int ldq = mx + 2;
   const int c = (li + 1) + (lj + 1) * ldq;
   const int cc = R.c_off + li + lj * mx;
-  // static operands: packed coefficients and diagonal, boundary data, rules
-  const T *__restrict__ pk = pack + (size_t)(ch * 2 + m) * (kPackRows * kChunk) + tc;
-  const T dE = __ldg(pk), dW = __ldg(pk + kChunk), dN = __ldg(pk + 2 * kChunk), dS = __ldg(pk + 3 * kChunk);
-  const T idg = __ldg(pk + 4 * kChunk);
+  // static boundary data and ghost rules
   const T *__restrict__ g4 = f.bcg + R.bcg_off;
   // a cell touches at most one x side (W or E) and one y side (S or N):
   // kind 0 interior neighbour, 1 Dirichlet, 2 Neumann, 3 ghost rule
   int kx = 0, ky = 0, sx = 0, sy = 0;       // sx: 0 west 1 east; sy: 0 south 1 north
   T gx = 0, gy = 0;
-  Rule rx, ry;
+  int rx = 0, ry = 0;                       // ghost rule indices (perimeter table)
   if (li == 0 || li == mx - 1) {
     sx = (li == 0) ? 0 : 1;
-    const int bc = sx ? R.bc[1] : R.bc[0];   // selects, not an indexed (local-memory) array
+    const int bc = chunk_bc(R.flags, sx);   // a shift, not an indexed (local-memory) array
     if (bc) { kx = bc; gx = __ldg(g4 + sx * my + lj); }
-    else if (fresh) { kx = 3; rx = perim[R.pe_off + sx * my + lj]; }
+    else if (fresh) { kx = 3; rx = R.pe_off + sx * my + lj; prefetch_l1(perim + rx); }
   }
   if (lj == 0 || lj == my - 1) {
     sy = (lj == 0) ? 0 : 1;
-    const int bc = sy ? R.bc[3] : R.bc[2];
+    const int bc = chunk_bc(R.flags, 2 + sy);
     if (bc) { ky = bc; gy = __ldg(g4 + 2 * my + sy * mx + li); }
-    else if (fresh) { ky = 3; ry = perim[R.pe_off + 2 * my + sy * mx + li]; }
+    else if (fresh) { ky = 3; ry = R.pe_off + 2 * my + sy * mx + li; prefetch_l1(perim + ry); }
   }
   if (kChain) chain_wait();
   const T c83 = T(8.0 / 3.0), c13 = T(1.0 / 3.0);
   const LevelH<T> H = level_h(L, T(0));
   T *__restrict__ Q = f.Q + R.q_off;
   T qe = Q[c + 1], qw = Q[c - 1], qn = Q[c + ldq], qs = Q[c - ldq];
+  T t = f.F[cc];
   if (kx > 0) {
     T v;
     if (kx == 1) v = c83 * gx + c13 * Q[sx ? c - 1 : c + 1];
     else if (kx == 2) v = H.hx * gx;
-    else v = eval_inline<T>(rx, f.Q);
+    else v = eval_inline<T>(perim[rx], f.Q);
     if (sx) qe = v; else qw = v;
   }
   if (ky > 0) {
     T v;
     if (ky == 1) v = c83 * gy + c13 * Q[sy ? c - ldq : c + ldq];
     else if (ky == 2) v = H.hy * gy;
-    else v = eval_inline<T>(ry, f.Q);
+    else v = eval_inline<T>(perim[ry], f.Q);
     if (sy) qn = v; else qs = v;
   }
   // kPow2: the coefficients arrive pre-scaled by the exact 1/h^2 (a power of
   // two), and (q D) 2^-k == q (D 2^-k) in floating point, so one product
   // per neighbour gives the reference's (q D)/h^2 bit for bit
-  T t = f.F[cc];
   if (kPow2) {
     t = t + qe * dE;
     t = t + qw * dW;
@@ -325,43 +366,52 @@ __device__ __forceinline__ void relax_cell(const LevelD &L, const RelaxChunk *__
 // so loading all before storing any changes nothing: the arithmetic of each
 // update is relax_cell's.
 template <class T, bool kPow2, int kN>
-__global__ void __launch_bounds__(kBlock) k_relax_n(LevelD L, const RelaxChunk *__restrict__ chunks, int nchunks,
+__global__ void __launch_bounds__(kBlock) k_relax_n(LevelD L, const RelaxChunkD *__restrict__ chunks, int nchunks,
                                                     FieldsT<T> f, const T *__restrict__ pack,
                                                     const Rule *__restrict__ perim, int m, T omega, int unit_omega,
-                                                    int fresh) {
+                                                    int fresh, const uint8_t *__restrict__ cact, int amode) {
   chain_trigger();
   constexpr int tpc = kChunk / kN;                    // threads per chunk
   const int ch = blockIdx.x * (kBlock / tpc) + threadIdx.x / tpc;
   const int t0 = threadIdx.x % tpc;
-  bool okc = ch < nchunks;
-  RelaxChunk R;
-  if (okc) R = chunks[ch];
-  okc = okc && f.active[R.inst];
-  if (!okc) {
+  // chunk record and packed operands requested together (as relax_cell)
+  const bool okc = ch < nchunks;
+  RelaxChunkD R;
+  bool live = okc;
+  T dE[kN], dW[kN], dN[kN], dS[kN], idg[kN], gx[kN], gy[kN];
+  if (okc) {
+    R = chunks[ch];
+    if (amode == kActChunk) live = cact[ch] != 0;
+  }
+  if (live) {
+    const T *__restrict__ pk0 = pack + (size_t)(ch * 2 + m) * (kPackRows * kChunk) + t0;
+#pragma unroll
+    for (int u = 0; u < kN; ++u) {
+      const T *__restrict__ pk = pk0 + u * tpc;
+      dE[u] = __ldg(pk);
+      dW[u] = __ldg(pk + kChunk);
+      dN[u] = __ldg(pk + 2 * kChunk);
+      dS[u] = __ldg(pk + 3 * kChunk);
+      idg[u] = __ldg(pk + 4 * kChunk);
+    }
+  }
+  if (!live || t0 >= R.n || (amode == kActInst && !f.active[R.inst])) {
     chain_wait();
     return;
   }
   const int mx = R.mx, my = R.my, half = mx >> 1, ldq = mx + 2;
   const T *__restrict__ g4 = f.bcg + R.bcg_off;
-  const T *__restrict__ pk0 = pack + (size_t)(ch * 2 + m) * (kPackRows * kChunk);
   bool on[kN];
   int c[kN], cc[kN], code[kN], rxi[kN], ryi[kN];    // code: kx | ky << 2 | sx << 4 | sy << 5
-  T dE[kN], dW[kN], dN[kN], dS[kN], idg[kN], gx[kN], gy[kN];
 #pragma unroll
   for (int u = 0; u < kN; ++u) {
     const int tc = t0 + u * tpc;
     on[u] = tc < R.n;
     const int s = R.s0 + (on[u] ? tc : 0);
     const int lj = s / half;
-    const int li = 2 * (s - lj * half) + ((m + lj + R.par0) & 1);
+    const int li = 2 * (s - lj * half) + ((m + lj + chunk_par0(R.flags)) & 1);
     c[u] = (li + 1) + (lj + 1) * ldq;
     cc[u] = R.c_off + li + lj * mx;
-    const T *__restrict__ pk = pk0 + (on[u] ? tc : 0);
-    dE[u] = __ldg(pk);
-    dW[u] = __ldg(pk + kChunk);
-    dN[u] = __ldg(pk + 2 * kChunk);
-    dS[u] = __ldg(pk + 3 * kChunk);
-    idg[u] = __ldg(pk + 4 * kChunk);
     int kx = 0, ky = 0, sx = 0, sy = 0;
     gx[u] = 0;
     gy[u] = 0;
@@ -369,15 +419,15 @@ __global__ void __launch_bounds__(kBlock) k_relax_n(LevelD L, const RelaxChunk *
     ryi[u] = 0;
     if (li == 0 || li == mx - 1) {
       sx = (li == 0) ? 0 : 1;
-      const int bc = sx ? R.bc[1] : R.bc[0];
+      const int bc = chunk_bc(R.flags, sx);
       if (bc) { kx = bc; gx[u] = __ldg(g4 + sx * my + lj); }
-      else if (fresh) { kx = 3; rxi[u] = R.pe_off + sx * my + lj; }
+      else if (fresh) { kx = 3; rxi[u] = R.pe_off + sx * my + lj; prefetch_l1(perim + rxi[u]); }
     }
     if (lj == 0 || lj == my - 1) {
       sy = (lj == 0) ? 0 : 1;
-      const int bc = sy ? R.bc[3] : R.bc[2];
+      const int bc = chunk_bc(R.flags, 2 + sy);
       if (bc) { ky = bc; gy[u] = __ldg(g4 + 2 * my + sy * mx + li); }
-      else if (fresh) { ky = 3; ryi[u] = R.pe_off + 2 * my + sy * mx + li; }
+      else if (fresh) { ky = 3; ryi[u] = R.pe_off + 2 * my + sy * mx + li; prefetch_l1(perim + ryi[u]); }
     }
     code[u] = kx | (ky << 2) | (sx << 4) | (sy << 5);
   }
@@ -437,12 +487,12 @@ __global__ void __launch_bounds__(kBlock) k_relax_n(LevelD L, const RelaxChunk *
 }
 
 template <class T, bool kPow2>
-__global__ void __launch_bounds__(kBlock) k_relax(LevelD L, const RelaxChunk *__restrict__ chunks, int nchunks,
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 8 : 5) k_relax(LevelD L, const RelaxChunkD *__restrict__ chunks, int nchunks,
                                                   FieldsT<T> f, const T *__restrict__ pack,
                                                   const Rule *__restrict__ perim, int m, T omega, int unit_omega,
-                                                  int fresh) {
+                                                  int fresh, const uint8_t *__restrict__ cact, int amode) {
   chain_trigger();
-  relax_cell<T, kPow2, true>(L, chunks, nchunks, f, pack, perim, m, omega, unit_omega, fresh,
+  relax_cell<T, kPow2, true>(L, chunks, nchunks, f, pack, perim, m, omega, unit_omega, fresh, cact, amode,
                              blockIdx.x * (kBlock / kChunk) + threadIdx.x / kChunk, threadIdx.x & (kChunk - 1));
 }
 
@@ -944,11 +994,13 @@ constexpr int kFinal = 512;
 __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__restrict__ ir,
                                                           const SlotRange *__restrict__ ranges, const double *slots,
                                                           int nslots, ResAcc *acc, int *active, int *iters,
-                                                          double *hist, int hist_stride, int mode) {
+                                                          double *hist, int hist_stride, int mode,
+                                                          const int *__restrict__ crange, int nlev, uint8_t *cact) {
   chain_in();
   const int inst = blockIdx.x;
   const InstRes R = ir[inst];
   __shared__ double s_a[kFinal], s_b[kFinal];
+  __shared__ int s_write;
   const int t = threadIdx.x;
   // four independent loads in flight per thread (max is order-free)
   double li = 0, fn = 0;
@@ -1004,6 +1056,7 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__rest
     __syncthreads();
   }
   if (t == 0) {
+    int wr = -1;
     fnorm = fnorm > 2.2250738585072014e-308 ? fnorm : 2.2250738585072014e-308;
     const double rel = linf / fnorm;
     ResAcc &A = acc[inst];
@@ -1020,8 +1073,22 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__rest
       else it = it + 1;
       iters[inst] = it;
       if (it < hist_stride) hist[(size_t)inst * hist_stride + it] = linf;
-      active[inst] = (it < R.max_vcycles && rel > R.rel_tol) ? 1 : 0;
+      const int a = (it < R.max_vcycles && rel > R.rel_tol) ? 1 : 0;
+      active[inst] = a;
+      if (mode == 0 || !a) wr = a;     // every instance at the start; later only when it freezes
     }
+    s_write = wr;
+  }
+  // the smoother's per-chunk copy of the flag, over the instance's chunk
+  // range of every level (crange: [inst][level] begin, end)
+  if (cact) {
+    __syncthreads();
+    const int wr = s_write;
+    if (wr >= 0)
+      for (int k = 0; k < nlev; ++k) {
+        const int b = crange[2 * (inst * nlev + k)], e = crange[2 * (inst * nlev + k) + 1];
+        for (int c = b + t; c < e; c += kFinal) cact[c] = (uint8_t)wr;
+      }
   }
 }
 
