@@ -297,14 +297,19 @@ def batched_form(backend, n, steps, warmup, flush, local):
              'relax_cells_per_thread': bh.relax_tuning(1 if prec == 'mixed' else 0).tolist()}
         # smoother roofline per merged level (levels larger than L2 here)
         peak, peak_kind = load_peaks()
+        from bsam.device import fp64_rate
+        fp64_peak = fp64_rate(backend.ctx)
         cells = [int(b.levels[k - 1, 5] - b.levels[k - 1, 4]) for k in range(1, b.nlev + 1)]
         lv = []
         for k in range(2, b.nlev + 1):
             pr = bh.profile(2, level=k)['relax']
             if pr['launches']:
                 ach = pr['bytes'] / (pr['ms'] / 1e3) / 1e9
-                lv.append({'level': k, 'cells': cells[k - 1], 'avg_launch_us': 1e3 * pr['ms'] / pr['launches'],
+                us = 1e3 * pr['ms'] / pr['launches']
+                lv.append({'level': k, 'cells': cells[k - 1], 'avg_launch_us': us,
                            'achieved_gbs': ach, 'frac': ach / peak})
+                if prec == 'fp64':   # 9 FP64 operations per 48 algorithmic bytes
+                    lv[-1]['fp64_pipe_frac'] = pr['bytes'] * 9 / 48 / (pr['ms'] / 1e3) / 1e9 / fp64_peak
         d['smoother_levels'] = lv
         d['smoother_peak'] = {'value': peak, 'kind': peak_kind, 'unit': 'GB/s'}
         if prec == 'fp64':
@@ -480,6 +485,12 @@ def main():
     achieved = rl['bytes'] / (rl['ms'] / 1e3) / 1e9
     ra = prof['relax']
     achieved_all = ra['bytes'] / (ra['ms'] / 1e3) / 1e9
+    # the FP64 smoother's other bound: 9 separate FP64 operations per colour
+    # update (4 products, 4 sums, the diagonal product; no contraction), i.e.
+    # 9 per 48 algorithmic bytes (a pass moves 24 B per cell, updates half)
+    from bsam.device import fp64_rate
+    fp64_peak = fp64_rate(backend.ctx)
+    fp64_ach = rl['bytes'] * 9 / 48 / (rl['ms'] / 1e3) / 1e9
     per_kind = {k: {'ms_per_cycle': v['ms'] / 3, 'launches_per_cycle': v['launches'] / 3} for k, v in prof.items()}
 
     # ---- forms beside the plain FP64 path -----------------------------------
@@ -529,7 +540,9 @@ def main():
                          'bytes_per_launch': rl['bytes'] / max(rl['launches'], 1),
                          'avg_launch_us': 1e3 * rl['ms'] / max(rl['launches'], 1),
                          'all_levels': {'achieved': achieved_all, 'frac': achieved_all / peak,
-                                        'avg_launch_us': 1e3 * ra['ms'] / max(ra['launches'], 1)}},
+                                        'avg_launch_us': 1e3 * ra['ms'] / max(ra['launches'], 1)},
+                         'fp64_pipe': {'ops_per_update': 9, 'achieved_gops': fp64_ach, 'peak_gops': fp64_peak,
+                                       'peak_kind': 'measured (bsam_fp64_rate)', 'frac': fp64_ach / fp64_peak}},
             'cpu_baseline': cpu,
             'forms': forms,
             'gpu_launches': int(launches),

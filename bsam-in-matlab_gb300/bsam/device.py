@@ -98,6 +98,7 @@ def lib():
         L.bsam_batch_set_stop.argtypes = [P, C.c_int, C.c_int, D]
         L.bsam_polygon_dist2.argtypes = [P, P, C.c_int, P, P, P, I64]
         L.bsam_device_memory.argtypes = [C.c_int, C.POINTER(I64), C.POINTER(I64)]
+        L.bsam_fp64_rate.argtypes = [P, C.POINTER(D)]
         L.bsam_setup_levels.argtypes = [P]
         L.bsam_parabolic_rhs.argtypes = [P, C.c_int, D, P, I64]
         L.bsam_history_push.argtypes = [P]
@@ -324,7 +325,8 @@ class DevHier:
         return n.value
 
     def relax_tuning(self, precision=0):
-        """Colour cells per smoother thread, levels 1..nlev, as tuned."""
+        """Smoother launch form per level 1..nlev as tuned: colour cells per
+        thread (1, 2, 4), 0 for the single-cluster launch, -1 not yet run."""
         out = np.zeros(int(self.fl.nlev), np.int32)
         check(lib().bsam_relax_tuning(self.h, int(precision), out.ctypes.data, out.size))
         return out
@@ -340,6 +342,13 @@ def memory_info(device=0):
     f, t = I64(0), I64(0)
     check(lib().bsam_device_memory(int(device), C.byref(f), C.byref(t)))
     return f.value, t.value
+
+
+def fp64_rate(ctx):
+    """Measured FP64 multiply/add issue rate of the device, 1e9 ops/s."""
+    g = D(0)
+    check(lib().bsam_fp64_rate(ctx.h, C.byref(g)))
+    return g.value
 
 
 def polygon_dist2(ctx, verts, x, y, best):

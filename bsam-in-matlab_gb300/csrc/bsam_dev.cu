@@ -332,6 +332,60 @@ void launch_fill(bsam_hier h, int k, int need = 0) {
            (const int *)h->active.p, (const int *)h->inst_nlev.p, need);
 }
 
+// can the device co-schedule one cluster of `ctas` CTAs of kClusterBlock
+// threads of this smoother variant (sizes above 8 are non-portable)
+template <class T, bool kPow2>
+bool cluster_fits(int ctas) {
+  cudaFuncSetAttribute(k_relax_cluster<T, kPow2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)ctas);
+  cfg.blockDim = dim3(kClusterBlock);
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)ctas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveClusters(&n, k_relax_cluster<T, kPow2>, &cfg);
+  cudaGetLastError();
+  return e == cudaSuccess && n >= 1;
+}
+
+// CTAs of the smoother's single-cluster launch: 16 where every variant fits,
+// else 8, else 0 (the variant is then never chosen)
+int cluster_ctas() {
+  static int cached = -1;
+  if (cached >= 0) return cached;
+  cached = 0;
+  for (int c : {16, 8})
+    if (cluster_fits<double, true>(c) && cluster_fits<double, false>(c) && cluster_fits<float, true>(c) &&
+        cluster_fits<float, false>(c)) {
+      cached = c;
+      break;
+    }
+  return cached;
+}
+
+template <class T, bool kPow2, class... Args>
+void launch_cluster(bsam_hier h, int ctas, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)ctas);
+  cfg.blockDim = dim3(kClusterBlock);
+  cfg.stream = h->stream;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  at[1].id = cudaLaunchAttributeClusterDimension;
+  at[1].val.clusterDim.x = (unsigned)ctas;
+  at[1].val.clusterDim.y = 1;
+  at[1].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 2;
+  cudaLaunchKernelEx(&cfg, k_relax_cluster<T, kPow2>, args...);
+}
+
 // ebRelaxLevel (ebRelaxLevel.m:28-38): 2*nsweeps colour passes; the ghost
 // refill after every colour is folded into the next pass (k_relax `fresh`),
 // and one fill after the last pass leaves the ghost frame as the reference's.
@@ -352,6 +406,20 @@ void launch_relax(bsam_hier h, int k, int nsweeps, bool first_fresh = false) {
   const int am = h->act_mode;
   const std::vector<int> &rn = h->relax_n[sizeof(T) == sizeof(float) ? 1 : 0];
   const int kn = rn.empty() ? 1 : rn[k];
+  if (kn == 0) {   // the whole relaxation and its fill in one cluster launch
+    Launch l(h, K_RELAX, 24.0 * tscale<T>() * (double)L.ncells * 2 * nsweeps, k);
+    const int C = cluster_ctas();
+    const Rule *pr = (const Rule *)h->perim.p;
+    const T om = (T)h->opts.omega;
+    const int ff = first_fresh ? 1 : 0;
+    if (L.pow2)
+      launch_cluster<T, true>(h, C, ld, ch, L.rc_n, f, pk, pr, om, unit, nsweeps, ff, ca, am, ghost_items(h), L.g1_off,
+                              L.g1_n, L.hx, L.hy);
+    else
+      launch_cluster<T, false>(h, C, ld, ch, L.rc_n, f, pk, pr, om, unit, nsweeps, ff, ca, am, ghost_items(h),
+                               L.g1_off, L.g1_n, L.hx, L.hy);
+    return;
+  }
   for (int s = 0; s < nsweeps; ++s)
     for (int m = 0; m < 2; ++m) {
       const int fresh = (first_fresh || s > 0 || m > 0) ? 1 : 0;
@@ -528,30 +596,46 @@ int launch_iteration(bsam_hier h, int mode) {
   return BSAM_OK;
 }
 
-// Autotuner of the smoother's thread coarsening: for each level large enough
-// to matter, time two sweeps with 1, 2 and 4 colour cells per thread (best of
-// three, CUDA events on the stream) in the precision the cycle runs in, and
-// keep the fastest.  The choice does not change a single bit of the result
-// (each update's arithmetic is the same), so it is tuned on the live state
-// and the FP64 state is restored afterwards.  BSAM_RELAX_N=1|2|4 forces one
-// value on every level.
+// Autotuner of the smoother's launch form, per level and precision: on a
+// level large enough to matter, 1, 2 or 4 colour cells per thread; on a
+// level that one thread-block cluster covers with at most 4 cells per
+// thread, separate launches per colour pass or the single cluster launch
+// (kn 0).  Each candidate's relaxation (npre sweeps and the closing fill) is
+// timed best of three with CUDA events on the stream, in the precision the
+// cycle runs in; the fastest is kept.  The choice does not change a single
+// bit of the result (each update's arithmetic is the same), so it is tuned
+// on the live state and the FP64 state is restored afterwards.
+// BSAM_RELAX_N=0|1|2|4 forces one form on every level.
 constexpr int64_t kTuneMinCells = 131072;
+constexpr int kClusterMaxPerThread = 4;
+
+// candidate set of a level: 0 none, 1 coarsening {1,2,4}, 2 {1, cluster}
+int tune_set(bsam_hier h, int k) {
+  const LevelPlan &L = h->lev[k];
+  if (L.ncells >= kTuneMinCells) return 1;
+  const int C = cluster_ctas();
+  if (C > 0 && (int64_t)L.rc_n * kChunk <= (int64_t)kClusterMaxPerThread * C * kClusterBlock) return 2;
+  return 0;
+}
 
 template <class T>
-int tune_level(bsam_hier h, int k, int *best) {
+int tune_level(bsam_hier h, int k, int set, int *best) {
   std::vector<int> &rn = h->relax_n[sizeof(T) == sizeof(float) ? 1 : 0];
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
   float bt = 1e30f;
   *best = 1;
-  for (int kn : {1, 2, 4}) {
+  const int ns = std::max(h->opts.npre, 1);
+  const std::vector<int> cand = set == 1 ? std::vector<int>{1, 2, 4} : std::vector<int>{1, 0};
+  for (int kn : cand) {
     rn[k] = kn;
-    launch_relax<T>(h, k, 1);          // warm-up
+    launch_relax<T>(h, k, ns);         // warm-up
+    if (kn == 0 && cudaGetLastError() != cudaSuccess) continue;   // cluster launch refused: not a candidate
     float t = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
       cudaEventRecord(a, h->stream);
-      launch_relax<T>(h, k, 2);
+      launch_relax<T>(h, k, ns);
       cudaEventRecord(b, h->stream);
       CK(cudaEventSynchronize(b));
       float ms = 0;
@@ -572,10 +656,10 @@ int tune_level(bsam_hier h, int k, int *best) {
 
 int autotune(bsam_hier h);
 
-uint64_t tune_key(int precision, bool pow2, int chunks) {
+uint64_t tune_key(int precision, bool pow2, int chunks, int set) {
   int b = 0;
   while ((chunks >> (b + 1)) > 0) ++b;
-  return ((uint64_t)precision << 40) | ((uint64_t)pow2 << 32) | (uint64_t)b;
+  return ((uint64_t)set << 48) | ((uint64_t)precision << 40) | ((uint64_t)pow2 << 32) | (uint64_t)b;
 }
 
 // FP32 arrays of the mixed form: allocated on first use, coefficient copies
@@ -615,8 +699,10 @@ int autotune(bsam_hier h) {
   std::vector<int> &rn = h->relax_n[p];
   rn.assign(h->nlev + 1, 1);
   if (const char *env = getenv("BSAM_RELAX_N")) {
-    const int kn = atoi(env);
-    rn.assign(h->nlev + 1, (kn == 2 || kn == 4) ? kn : 1);
+    int kn = atoi(env);
+    if (kn == 0 && cluster_ctas() == 0) kn = 1;
+    rn.assign(h->nlev + 1, (kn == 0 || kn == 2 || kn == 4) ? kn : 1);
+    rn[1] = 1;
     return BSAM_OK;
   }
   // levels already measured on this context (same precision, same h^2 form,
@@ -626,8 +712,9 @@ int autotune(bsam_hier h) {
   {
     std::lock_guard<std::mutex> lk(c->tune_mu);
     for (int k = 2; k <= h->nlev; ++k) {
-      if (h->lev[k].ncells < kTuneMinCells) continue;
-      auto it = c->relax_tune.find(tune_key(p, h->lev[k].pow2, h->lev[k].rc_n));
+      const int set = tune_set(h, k);
+      if (!set) continue;
+      auto it = c->relax_tune.find(tune_key(p, h->lev[k].pow2, h->lev[k].rc_n, set));
       if (it != c->relax_tune.end()) rn[k] = it->second;
       else todo.push_back(k);
     }
@@ -646,10 +733,11 @@ int autotune(bsam_hier h) {
   h->profiling = false;
   for (int k : todo) {
     int best = 1;
-    rc = p ? tune_level<float>(h, k, &best) : tune_level<double>(h, k, &best);
+    const int set = tune_set(h, k);
+    rc = p ? tune_level<float>(h, k, set, &best) : tune_level<double>(h, k, set, &best);
     if (rc) break;
     std::lock_guard<std::mutex> lk(c->tune_mu);
-    c->relax_tune[tune_key(p, h->lev[k].pow2, h->lev[k].rc_n)] = best;
+    c->relax_tune[tune_key(p, h->lev[k].pow2, h->lev[k].rc_n, set)] = best;
   }
   h->profiling = prof;
   h->launch_count = lc;
@@ -1491,6 +1579,36 @@ int bsam_device_memory(int device, int64_t *free_bytes, int64_t *total_bytes) {
   return BSAM_OK;
 }
 
+int bsam_fp64_rate(bsam_ctx ctx, double *gops) {
+  if (!ctx || !gops) return fail(BSAM_ERR_ARG, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  const int blocks = sms * 8, iters = 4096;
+  double *out = nullptr;
+  CK(cudaMalloc(&out, sizeof(double) * blocks * kBlock));
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  for (int r = 0; r < 4; ++r) {
+    cudaEventRecord(a, ctx->stream);
+    k_fp64_rate<<<blocks, kBlock, 0, ctx->stream>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(b, ctx->stream);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    if (r > 0) best = std::min(best, ms);     // the first is a warm-up
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  const cudaError_t e = cudaGetLastError();
+  cudaFree(out);
+  if (e != cudaSuccess) return cuda_fail(e, "bsam_fp64_rate");
+  *gops = (double)kFp64RateOps * iters * blocks * kBlock / (best * 1e-3) / 1e9;
+  return BSAM_OK;
+}
+
 int bsam_ctx_destroy(bsam_ctx ctx) {
   if (!ctx) return BSAM_OK;
   cudaSetDevice(ctx->device);
@@ -1976,7 +2094,7 @@ int bsam_relax_tuning(bsam_hier h, int precision, int32_t *cells_per_thread, int
   if (precision != 0 && precision != 1) return fail(BSAM_ERR_ARG, "precision must be 0 or 1");
   const std::vector<int> &rn = h->relax_n[precision];
   for (int k = 1; k <= h->nlev && k <= cap; ++k)
-    cells_per_thread[k - 1] = h->tuned[precision] && (int)rn.size() > k ? rn[k] : 0;
+    cells_per_thread[k - 1] = h->tuned[precision] && (int)rn.size() > k ? rn[k] : -1;
   return BSAM_OK;
 }
 

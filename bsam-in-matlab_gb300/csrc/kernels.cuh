@@ -20,6 +20,7 @@
 // solution state.  Every thread executes the wait before it exits, so no
 // kernel completes before its predecessor.
 #pragma once
+#include <cooperative_groups.h>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -32,6 +33,15 @@ __device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait
 __device__ __forceinline__ void chain_in() {
   chain_trigger();
   chain_wait();
+}
+
+// a solution load; kCG: from L2 (ld.global.cg), for kernels whose blocks
+// read values other blocks of the same launch wrote after a cluster barrier
+// (another SM's L1 may hold an older copy of the line)
+template <bool kCG, class T>
+__device__ __forceinline__ T ld_sol(const T *p) {
+  if constexpr (kCG) return __ldcg(p);
+  else return *p;
 }
 
 // per-patch metadata on the device
@@ -129,38 +139,39 @@ struct GhostItems {
   const int *inst;             // instance per item (batches only, else null)
 };
 
-template <class T>
+template <class T, bool kCG = false>
 __device__ __forceinline__ T eval_rule(const GhostItems &G, int i, const T *Q, const T *bcg, T hx, T hy) {
   const T A1 = T(-1.0 / 5.0), A2 = T(2.0 / 3.0), A3 = T(8.0 / 15.0);
   const T B1 = T(5.0 / 32.0), B2 = T(15.0 / 16.0), B3 = T(-3.0 / 32.0);
   const T c23 = T(2.0 / 3.0), c13 = T(1.0 / 3.0), c83 = T(8.0 / 3.0);
   const int a = G.a[i];
+  auto q = [&](int j) { return ld_sol<kCG>(Q + j); };
   switch (G.type[i]) {
-    case G_COPY: return Q[a];
-    case G_QIF: return (A1 * Q[a] + A2 * Q[G.b[i]]) + A3 * Q[G.c[i]];
+    case G_COPY: return q(a);
+    case G_QIF: return (A1 * q(a) + A2 * q(G.b[i])) + A3 * q(G.c[i]);
     case G_QIF_END:
-      return (A1 * Q[a] + A2 * Q[G.b[i]]) + A3 * ((B1 * Q[G.c[i]] + B2 * Q[G.d[i]]) + B3 * Q[G.e[i]]);
-    case G_LIF: return (c23 * Q[G.c[i]] + c23 * Q[a]) - c13 * Q[G.b[i]];
-    case G_LIF_CORNER: return c23 * Q[G.c[i]] + c13 * Q[a];
-    case G_DIRICHLET: return (c83 * bcg[G.e[i]] - 2 * Q[a]) + c13 * Q[G.b[i]];
-    default: return Q[a] + (G.b[i] ? hy : hx) * bcg[G.e[i]];   // G_NEUMANN
+      return (A1 * q(a) + A2 * q(G.b[i])) + A3 * ((B1 * q(G.c[i]) + B2 * q(G.d[i])) + B3 * q(G.e[i]));
+    case G_LIF: return (c23 * q(G.c[i]) + c23 * q(a)) - c13 * q(G.b[i]);
+    case G_LIF_CORNER: return c23 * q(G.c[i]) + c13 * q(a);
+    case G_DIRICHLET: return (c83 * bcg[G.e[i]] - 2 * q(a)) + c13 * q(G.b[i]);
+    default: return q(a) + (G.b[i] ? hy : hx) * bcg[G.e[i]];   // G_NEUMANN
   }
 }
 
 // one ghost item: its final value (or the QC ring refresh)
-template <class T>
+template <class T, bool kCG = false>
 __device__ __forceinline__ void ghost_item(const GhostItems &G, int i, int8_t ty, int dst, T *Q, T *QC, const T *bcg,
                                            T hx, T hy) {
   if (ty == G_RING) {
-    QC[dst] = Q[G.a[i]];
+    QC[dst] = ld_sol<kCG>(Q + G.a[i]);
   } else if (ty == G_PHYS_CORNER) {
     // (face ghost 1 + face ghost 2) - interior, the face ghosts evaluated by
     // their own final rules (ebFillGhosts.m:84-89 reads them after stage 3)
-    const T v1 = eval_rule<T>(G, G.a[i], Q, bcg, hx, hy);
-    const T v2 = eval_rule<T>(G, G.b[i], Q, bcg, hx, hy);
-    Q[dst] = (v1 + v2) - Q[G.c[i]];
+    const T v1 = eval_rule<T, kCG>(G, G.a[i], Q, bcg, hx, hy);
+    const T v2 = eval_rule<T, kCG>(G, G.b[i], Q, bcg, hx, hy);
+    Q[dst] = (v1 + v2) - ld_sol<kCG>(Q + G.c[i]);
   } else {
-    Q[dst] = eval_rule<T>(G, i, Q, bcg, hx, hy);
+    Q[dst] = eval_rule<T, kCG>(G, i, Q, bcg, hx, hy);
   }
 }
 
@@ -230,16 +241,17 @@ struct Rule {                // one ghost rule, inline (perimeter table)
   int type, a, b, c, d, e;
 };
 
-template <class T>
+template <class T, bool kCG = false>
 __device__ __forceinline__ T eval_inline(const Rule &R, const T *Q) {
   const T A1 = T(-1.0 / 5.0), A2 = T(2.0 / 3.0), A3 = T(8.0 / 15.0);
   const T B1 = T(5.0 / 32.0), B2 = T(15.0 / 16.0), B3 = T(-3.0 / 32.0);
   const T c23 = T(2.0 / 3.0), c13 = T(1.0 / 3.0);
+  auto q = [&](int j) { return ld_sol<kCG>(Q + j); };
   switch (R.type) {
-    case G_COPY: return Q[R.a];
-    case G_QIF: return (A1 * Q[R.a] + A2 * Q[R.b]) + A3 * Q[R.c];
-    case G_QIF_END: return (A1 * Q[R.a] + A2 * Q[R.b]) + A3 * ((B1 * Q[R.c] + B2 * Q[R.d]) + B3 * Q[R.e]);
-    default: return (c23 * Q[R.c] + c23 * Q[R.a]) - c13 * Q[R.b];   // G_LIF
+    case G_COPY: return q(R.a);
+    case G_QIF: return (A1 * q(R.a) + A2 * q(R.b)) + A3 * q(R.c);
+    case G_QIF_END: return (A1 * q(R.a) + A2 * q(R.b)) + A3 * ((B1 * q(R.c) + B2 * q(R.d)) + B3 * q(R.e));
+    default: return (c23 * q(R.c) + c23 * q(R.a)) - c13 * q(R.b);   // G_LIF
   }
 }
 
@@ -262,7 +274,7 @@ __device__ __forceinline__ void prefetch_l1(const R *p) {
 // one colour-cell update of chunk ch (thread tc of the chunk); kChain: the
 // grid kernel's programmatic-launch wait sits between the static loads and
 // the first read of the solution
-template <class T, bool kPow2, bool kChain>
+template <class T, bool kPow2, bool kChain, bool kCG = false>
 __device__ __forceinline__ void relax_cell(const LevelD &L, const RelaxChunkD *__restrict__ chunks, int nchunks,
                                            const FieldsT<T> &f, const T *__restrict__ pack,
                                            const Rule *__restrict__ perim, int m, T omega, int unit_omega, int fresh,
@@ -322,20 +334,20 @@ __device__ __forceinline__ void relax_cell(const LevelD &L, const RelaxChunkD *_
   const T c83 = T(8.0 / 3.0), c13 = T(1.0 / 3.0);
   const LevelH<T> H = level_h(L, T(0));
   T *__restrict__ Q = f.Q + R.q_off;
-  T qe = Q[c + 1], qw = Q[c - 1], qn = Q[c + ldq], qs = Q[c - ldq];
+  T qe = ld_sol<kCG>(Q + c + 1), qw = ld_sol<kCG>(Q + c - 1), qn = ld_sol<kCG>(Q + c + ldq), qs = ld_sol<kCG>(Q + c - ldq);
   T t = f.F[cc];
   if (kx > 0) {
     T v;
-    if (kx == 1) v = c83 * gx + c13 * Q[sx ? c - 1 : c + 1];
+    if (kx == 1) v = c83 * gx + c13 * ld_sol<kCG>(Q + (sx ? c - 1 : c + 1));
     else if (kx == 2) v = H.hx * gx;
-    else v = eval_inline<T>(perim[rx], f.Q);
+    else v = eval_inline<T, kCG>(perim[rx], f.Q);
     if (sx) qe = v; else qw = v;
   }
   if (ky > 0) {
     T v;
-    if (ky == 1) v = c83 * gy + c13 * Q[sy ? c - ldq : c + ldq];
+    if (ky == 1) v = c83 * gy + c13 * ld_sol<kCG>(Q + (sy ? c - ldq : c + ldq));
     else if (ky == 2) v = H.hy * gy;
-    else v = eval_inline<T>(perim[ry], f.Q);
+    else v = eval_inline<T, kCG>(perim[ry], f.Q);
     if (sy) qn = v; else qs = v;
   }
   // kPow2: the coefficients arrive pre-scaled by the exact 1/h^2 (a power of
@@ -354,7 +366,7 @@ __device__ __forceinline__ void relax_cell(const LevelD &L, const RelaxChunkD *_
   }
   t = t * idg;
   if (unit_omega) Q[c] = t;
-  else Q[c] = omega * t + (1 - omega) * Q[c];
+  else Q[c] = omega * t + (1 - omega) * ld_sol<kCG>(Q + c);
 }
 
 // Coarsened smoother: each thread updates kN colour cells of its chunk
@@ -494,6 +506,45 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 8 : 5) k_relax(LevelD
   chain_trigger();
   relax_cell<T, kPow2, true>(L, chunks, nchunks, f, pack, perim, m, omega, unit_omega, fresh, cact, amode,
                              blockIdx.x * (kBlock / kChunk) + threadIdx.x / kChunk, threadIdx.x & (kChunk - 1));
+}
+
+// A small level's whole relaxation in one launch: one thread-block cluster
+// runs every colour pass of the `nsweeps` sweeps over all the level's chunks
+// (cluster-strided), with a cluster barrier (release / acquire) between
+// passes, then the level's ghost fill (launch_fill's items).  Each pass and
+// the fill compute exactly what the separate launches compute -- the same
+// relax_cell and ghost_item code -- with the solution read from L2.  One
+// cluster holds every block, so the barrier orders the whole level; no
+// thread leaves the loop early, so every barrier is reached by all.
+constexpr int kClusterBlock = 1024;
+
+template <class T, bool kPow2>
+__global__ void __launch_bounds__(kClusterBlock, 1)
+    k_relax_cluster(LevelD L, const RelaxChunkD *__restrict__ chunks, int nchunks, FieldsT<T> f,
+                    const T *__restrict__ pack, const Rule *__restrict__ perim, T omega, int unit_omega, int nsweeps,
+                    int first_fresh, const uint8_t *__restrict__ cact, int amode, GhostItems G, int g_off, int g_n,
+                    double hx_, double hy_) {
+  namespace cg = cooperative_groups;
+  chain_trigger();
+  cg::cluster_group cl = cg::this_cluster();
+  const int nth = (int)cl.num_blocks() * kClusterBlock;
+  const int tid = (int)cl.block_rank() * kClusterBlock + threadIdx.x;
+  chain_wait();
+  const int nitems = nchunks * kChunk;
+  for (int s = 0; s < nsweeps; ++s)
+    for (int m = 0; m < 2; ++m) {
+      const int fresh = (first_fresh || s > 0 || m > 0) ? 1 : 0;
+      for (int w = tid; w < nitems; w += nth)
+        relax_cell<T, kPow2, false, true>(L, chunks, nchunks, f, pack, perim, m, omega, unit_omega, fresh, cact,
+                                          amode, w / kChunk, w % kChunk);
+      cl.sync();
+    }
+  for (int t = tid; t < g_n; t += nth) {
+    const int i = g_off + t;
+    const int inst = G.inst ? G.inst[i] : -1;
+    if (inst >= 0 && !f.active[inst]) continue;
+    ghost_item<T, true>(G, i, G.type[i], G.dst[i], f.Q, f.QC, f.bcg, T(hx_), T(hy_));
+  }
 }
 
 
@@ -1090,6 +1141,25 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__rest
         for (int c = b + t; c < e; c += kFinal) cact[c] = (uint8_t)wr;
       }
   }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 issue-rate probe (bsam_fp64_rate): eight independent x = x*a + b
+// chains per thread, each a separate multiply and add (the library is built
+// without contraction), so 16 FP64 operations per iteration.
+constexpr int kFp64RateOps = 16;
+__global__ void __launch_bounds__(kBlock) k_fp64_rate(double *out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) x[u] = 1.0 + 1e-3 * u + 1e-9 * threadIdx.x;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) x[u] = x[u] * a + b;
+  }
+  double s = 0;
+#pragma unroll
+  for (int u = 0; u < 8; ++u) s = s + x[u];
+  out[blockIdx.x * kBlock + threadIdx.x] = s;
 }
 
 // ---------------------------------------------------------------------------

@@ -118,6 +118,13 @@ int bsam_ctx_destroy(bsam_ctx ctx);
  * loop; no reference counterpart). */
 int bsam_device_memory(int device, int64_t *free_bytes, int64_t *total_bytes);
 
+/* Measured issue rate of separate FP64 multiplies and adds on the context's
+ * device (the form every kernel of the library uses: no contraction), in
+ * 1e9 operations per second: independent chains on every SM, best of three
+ * CUDA-event timings.  The denominator of the FP64-bound kernels' roofline
+ * (no reference counterpart).                                            */
+int bsam_fp64_rate(bsam_ctx ctx, double *gops);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char *bsam_last_error(void);
 
@@ -229,13 +236,15 @@ int bsam_restore_state(bsam_hier h);
 /* Kernels launched on this hierarchy so far (eager and graph-replayed). */
 int bsam_launch_count(bsam_hier h, int64_t *count);
 
-/* The smoother's thread coarsening per level as the autotuner chose it at
- * the first solve: colour cells updated per thread (1, 2 or 4) of levels
- * 1..nlev in cells_per_thread[0..nlev-1], for precision 0 (FP64 cycle) or
- * 1 (FP32 correction cycle); 0 where that cycle has not run yet.  The
- * choice never changes a result bit; BSAM_RELAX_N=1|2|4 in the environment
- * forces one value.  No reference counterpart (ebRelaxLevel.m has one
- * loop order).                                                            */
+/* The smoother's launch form per level as the autotuner chose it at the
+ * first solve, levels 1..nlev in cells_per_thread[0..nlev-1], for
+ * precision 0 (FP64 cycle) or 1 (FP32 correction cycle): 1, 2 or 4 colour
+ * cells updated per thread, one launch per colour pass; 0 for the whole
+ * relaxation (every pass and the closing ghost fill) in one launch of a
+ * single thread-block cluster; -1 where that cycle has not run yet.  The
+ * choice never changes a result bit; BSAM_RELAX_N=0|1|2|4 in the
+ * environment forces one form.  No reference counterpart (ebRelaxLevel.m
+ * has one loop order).                                                    */
 int bsam_relax_tuning(bsam_hier h, int precision, int32_t *cells_per_thread, int cap);
 
 /* Number of kernels one V-cycle (+ fill-down + residual) launches. */

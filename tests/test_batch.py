@@ -108,7 +108,11 @@ def test_merge_rejects_different_spacing(parts):
 
 
 @pytest.mark.gpu
-def test_batch_equals_solo_bitwise(parts):
+@pytest.mark.parametrize('form', [None, '0', '2'])
+def test_batch_equals_solo_bitwise(parts, form, monkeypatch):
+    """form: the smoother's launch form forced on the batch (None: tuned; '0'
+    one cluster launch per relaxation; '2' two colour cells per thread), so
+    frozen instances are skipped through the per-chunk flags in every form."""
     from bsam.device import DeviceBackend, DevHier, BSAM_FIELD_Q, BSAM_FIELD_QC, BSAM_FIELD_F
     ctx = DeviceBackend.get(0).ctx
     Hs = _instances()
@@ -125,6 +129,8 @@ def test_batch_equals_solo_bitwise(parts):
         solo.append((it, hist, rel, vis, dh.get(BSAM_FIELD_Q, p.Q.size), dh.get(BSAM_FIELD_QC, p.QC.size),
                      dh.get(BSAM_FIELD_F, p.F.size)))
     b = merge_flats(parts)
+    if form is not None:
+        monkeypatch.setenv('BSAM_RELAX_N', form)
     bh = DevHier(ctx, b, opts)
     for i, s in enumerate(stops):
         bh.set_stop(i, *s)

@@ -1,9 +1,12 @@
-"""Smoother autotuner: the colour cells updated per thread (1, 2 or 4) are
-picked per level and precision at the first solve of a hierarchy, by timing
-the candidates on the live state.  The choice may differ run to run, so it
-must never change a result bit: each forced setting (BSAM_RELAX_N) and the
-tuned one give the same V-cycle count, residual history and solution, in the
-FP64 cycle (ebRelaxLevel.m:28-38 per sweep) and the FP32 correction cycle.
+"""Smoother autotuner: the launch form of each level's relaxation -- 1, 2 or
+4 colour cells updated per thread with one launch per colour pass, or every
+pass and the closing fill in one launch of a single thread-block cluster
+(form 0) -- is picked per level and precision at the first solve of a
+hierarchy, by timing the candidates on the live state.  The choice may
+differ run to run, so it must never change a result bit: each forced form
+(BSAM_RELAX_N, on every level) and the tuned one give the same V-cycle
+count, residual history and solution, in the FP64 cycle
+(ebRelaxLevel.m:28-38 per sweep) and the FP32 correction cycle.
 """
 import numpy as np
 import pytest
@@ -39,12 +42,20 @@ def test_every_coarsening_gives_the_same_bits(precision, monkeypatch):
     dh, it, hist, Q = _solve(fl, o)
     p = 1 if precision == 'mixed' else 0
     tuned = dh.relax_tuning(p)
-    assert set(tuned.tolist()) <= {1, 2, 4} and tuned[0] == 1
-    assert np.all(dh.relax_tuning(1 - p) == 0)      # that cycle never ran
-    for kn in (1, 2, 4):
+    assert set(tuned.tolist()) <= {0, 1, 2, 4} and tuned[0] == 1
+    assert np.all(dh.relax_tuning(1 - p) == -1)     # that cycle never ran
+    for kn in (0, 1, 2, 4):
         monkeypatch.setenv('BSAM_RELAX_N', str(kn))
         dk, itk, histk, Qk = _solve(fl, o)
-        assert np.all(dk.relax_tuning(p) == kn)
+        assert np.all(dk.relax_tuning(p)[1:] == kn)
         assert itk == it
         np.testing.assert_array_equal(histk, hist)
         np.testing.assert_array_equal(Qk, Q)
+
+
+def test_fp64_rate_is_measured():
+    """The FP64 issue-rate probe (the FP64 roofline's denominator) returns a
+    plausible figure: above 50 Gop/s, below the FP32 rate of any GPU."""
+    from bsam.device import DeviceBackend, fp64_rate
+    g = fp64_rate(DeviceBackend.get(0).ctx)
+    assert 50 < g < 1e5, g
