@@ -126,6 +126,17 @@ def rect_isect(a, b):
     return r
 
 
+def near_boxes(boxes, r, pad=1):
+    """Indices (ascending) of the boxes [i0, i1, j0, j1] that intersect the
+    rectangle r grown by `pad` cells on every side: a superset of the boxes
+    that any face- or cell-rectangle test against r can hit, so a loop over
+    these in order does what the reference's loop over every patch does
+    (the others intersect nothing and are skipped)."""
+    b = np.asarray(boxes).reshape(-1, 4)
+    m = (b[:, 0] <= r[1] + pad) & (b[:, 1] >= r[0] - pad) & (b[:, 2] <= r[3] + pad) & (b[:, 3] >= r[2] - pad)
+    return np.nonzero(m)[0].tolist()
+
+
 def sub2ind(m, i, j):
     """0-based linear index of 1-based (i, j) in an m-row column-major array."""
     return (np.asarray(i) - 1) + (np.asarray(j) - 1) * m
@@ -333,7 +344,7 @@ def coeff_filldown(H):
                     _push_face_y(levC, OC, range(qb[0] + Il - 1, qb[0] + Ih), qb[3] + 1, qb[3] + 1, cDnS[:, -1])
                 continue
             Il, Ih, Jl, Jh = (b[0] + 1) // 2, b[1] // 2, (b[2] + 1) // 2, b[3] // 2
-            for q in range(levC.np):
+            for q in near_boxes(levC.box, [Il, Ih, Jl, Jh]):
                 qb = [int(v) for v in levC.box[q]]
                 r = rect_isect([Il, Ih, Jl, Jh], qb)
                 if r is not None:
@@ -546,7 +557,7 @@ def build_ops(H, k):
         ops['ring'] = _resolve_cells(levC, OC, ringGi, ringGj, Il, Jl, cmx, cmy)
         ops['winrect'] = []
         ncov = sum(len(t[2]) for t in ops['ring'])
-        for q in range(levC.np):
+        for q in near_boxes(levC.box, [Il, Ih, Jl, Jh]):
             qb = [int(v) for v in levC.box[q]]
             r = rect_isect([Il, Ih, Jl, Jh], qb)
             if r is None:
@@ -558,7 +569,7 @@ def build_ops(H, k):
             raise ValueError(f'eb_build_ops:nesting: patch {p+1} at level {k}: parent window not fully covered '
                              f'({ncov} of {(cmx+2)*(cmy+2)}) - proper nesting violated.')
         ops['usc'], ops['fsc'] = [], []
-        for q in range(levC.np):
+        for q in near_boxes(levC.box, [Il, Ih, Jl, Jh]):
             qb = [int(v) for v in levC.box[q]]
             r = rect_isect([Il, Ih, Jl, Jh], qb)
             if r is None:
@@ -585,13 +596,14 @@ def build_ops(H, k):
             levC.children[q - 1].append(p + 1)
             levC.covered[q - 1][mb[0] - 1:mb[1], mb[2] - 1:mb[3]] = True
         return
+    fboxes = np.asarray(levF.box).reshape(-1, 4).astype(np.int64)
+    fps = np.stack([(fboxes[:, 0] + 1) // 2, fboxes[:, 1] // 2, (fboxes[:, 2] + 1) // 2, fboxes[:, 3] // 2], axis=1)
     for q in range(levC.np):
         levC.children[q] = []
         qb = [int(v) for v in levC.box[q]]
         cov = np.zeros((qb[1] - qb[0] + 1, qb[3] - qb[2] + 1), dtype=bool, order=F)
-        for p in range(levF.np):
-            b = levF.box[p]
-            fp = [(int(b[0]) + 1) // 2, int(b[1]) // 2, (int(b[2]) + 1) // 2, int(b[3]) // 2]
+        for p in near_boxes(fps, qb, pad=0):
+            fp = [int(v) for v in fps[p]]
             r = rect_isect(fp, qb)
             if r is not None:
                 levC.children[q].append(p + 1)
@@ -600,7 +612,8 @@ def build_ops(H, k):
     for p in range(levF.np):
         b = levF.box[p]
         fp = [(int(b[0]) + 1) // 2, int(b[1]) // 2, (int(b[2]) + 1) // 2, int(b[3]) // 2]
-        levF.parents[p] = [q + 1 for q in range(levC.np) if rect_isect(fp, list(levC.box[q])) is not None]
+        levF.parents[p] = [q + 1 for q in near_boxes(levC.box, fp, pad=0)
+                           if rect_isect(fp, list(levC.box[q])) is not None]
 
 
 # ---------------------------------------------------------------------------
@@ -621,7 +634,7 @@ def parent_coeffs(H, k, p):
     PDeW = np.full((cmx + 1, cmy), np.nan, order=F)
     PDnS = np.full((cmx, cmy + 1), np.nan, order=F)
     PCC = np.full((cmx, cmy), np.nan, order=F)
-    for q in range(levC.np):
+    for q in near_boxes(levC.box, [Il, Ih, Jl, Jh]):
         qb = [int(v) for v in levC.box[q]]
         r = rect_isect([Il, Ih, Jl, Jh], qb)
         if r is not None:

@@ -124,15 +124,30 @@ void bsam_starfish_vertices(void *p, double *out) {
   for (int i = 0; i < 2 * (g->ns + 1); ++i) out[i] = g->v[i];
 }
 
-static void visit(const Starfish *g, int id, double x, double y, double *best) {
-  const Node *nd = &g->nodes[id - 1];
+static double box_lb(const Node *nd, double x, double y) {
   const double *bb = nd->box;
   const double dx = fmax(fmax(bb[0] - x, 0.0), x - bb[2]);
   const double dy = fmax(fmax(bb[1] - y, 0.0), y - bb[3]);
-  if (!(dx * dx + dy * dy <= *best + 64 * DBL_EPSILON)) return;
+  return dx * dx + dy * dy;
+}
+
+/* The tree search of ddStarfishGeometry.m: a node is entered when its box's
+   squared distance is within best + 64 eps.  The result is the minimum over
+   every segment whose leaf is entered, and the leaf of the nearest segment
+   is always entered, so the order in which children are tried changes only
+   how much is pruned: the nearer child goes first. */
+static void visit(const Starfish *g, int id, double lb, double x, double y, double *best) {
+  if (!(lb <= *best + 64 * DBL_EPSILON)) return;
+  const Node *nd = &g->nodes[id - 1];
   if (nd->left != 0) {
-    visit(g, nd->right, x, y, best);
-    visit(g, nd->left, x, y, best);
+    const double ll = box_lb(&g->nodes[nd->left - 1], x, y), lr = box_lb(&g->nodes[nd->right - 1], x, y);
+    if (ll < lr) {
+      visit(g, nd->left, ll, x, y, best);
+      visit(g, nd->right, lr, x, y, best);
+    } else {
+      visit(g, nd->right, lr, x, y, best);
+      visit(g, nd->left, ll, x, y, best);
+    }
     return;
   }
   double local = *best;
@@ -161,7 +176,7 @@ void bsam_starfish_distance(void *p, const double *X, const double *Y, double *d
     if (seg > ns) seg = ns;
     const double ax = g->a[2 * (seg - 1)], ay = g->a[2 * (seg - 1) + 1];
     double best = (x - ax) * (x - ax) + (y - ay) * (y - ay);
-    visit(g, 1, x, y, &best);
+    visit(g, 1, box_lb(&g->nodes[0], x, y), x, y, &best);
     const double ux = cos(ang), uy = sin(ang);
     const double ex = g->e[2 * (seg - 1)], ey = g->e[2 * (seg - 1) + 1];
     const double radius = (ax * ey - ay * ex) / (ux * ey - uy * ex);
