@@ -308,6 +308,21 @@ def _gather_window(H, k, p):
     return W
 
 
+def regrid_keeps(H, pprob, aDtNext, backend):
+    """True when ``ebpRegrid`` would rebuild H itself, so the rebuild can be
+    skipped with every bit of the state unchanged: H is its root level alone,
+    the problem's D, C and boundary data do not depend on time, alpha/Dt is
+    the one H's coefficients carry, and tagging H's root marks nothing.  The
+    rebuild would then copy H's root solution, restrict it below the root as
+    the last fill-down did, sample the same coefficients with the same alpha/Dt
+    and add no level (``ebpRegrid.m:16-59``)."""
+    if pprob.tdD or pprob.tdC or pprob.tdBC:
+        return False
+    if H.nlev != H.rootIdx or H.par.get('aDt') != aDtNext:
+        return False
+    return tag_cluster(H, backend).shape[0] == 0
+
+
 def ebpRegrid(Hold, pprob, t, aDtNext, opts, backend):
     """``ebpRegrid.m:16-59``: new hierarchy on the current solution, with a
     conservative transfer of u and the BDF2 history."""
@@ -450,7 +465,9 @@ def ebpSolve(pprob, *args, backend=None, **kwargs):
         if opts.RegridEvery > 0 and n % int(opts.RegridEvery) == 0 and n < nsteps and opts.eb.MaxLevels > 1:
             if dev:
                 to_host(H)
-            H = ebpRegrid(H, pprob, t1, _alpha(opts.Scheme) / Dt, opts, backend)
+            aNext = _alpha(opts.Scheme) / Dt
+            if not regrid_keeps(H, pprob, aNext, backend):
+                H = ebpRegrid(H, pprob, t1, aNext, opts, backend)
             nregrids += 1
             if dev:
                 H.par['hasUoo'] = H.par['Uoo'] is not None

@@ -90,3 +90,44 @@ def test_time_dependent_device_matches_oracle_pipeline():
     for kp in Ha.par['Uo']:
         np.testing.assert_array_equal(Ha.par['Uo'][kp], Hb.par['Uo'][kp])
         np.testing.assert_array_equal(Ha.par['Uoo'][kp], Hb.par['Uoo'][kp])
+
+
+def _same_runs(a, b):
+    np.testing.assert_array_equal(a['cycles'], b['cycles'])
+    np.testing.assert_array_equal(a['relres'], b['relres'])
+    np.testing.assert_array_equal(a['mass'], b['mass'])
+    Ha, Hb = a['H'], b['H']
+    assert Ha.nlev == Hb.nlev and a['nregrids'] == b['nregrids']
+    for k in range(1, Ha.nlev + 1):
+        for qa, qb in zip(Ha.lev[k].Q, Hb.lev[k].Q):
+            np.testing.assert_array_equal(qa, qb)
+    for kp in Ha.par['Uo']:
+        np.testing.assert_array_equal(Ha.par['Uo'][kp], Hb.par['Uo'][kp])
+
+
+def _skip_vs_rebuild(backend, base, ml, monkeypatch):
+    import bsam.parabolic as par
+    kw = dict(Scheme='bdf2', Dt=0.002, TFinal=0.1, BaseCells=base, MaxLevels=ml, RegridEvery=5, StepVerbose=0)
+    hits = []
+    keeps = par.regrid_keeps
+    monkeypatch.setattr(par, 'regrid_keeps', lambda *x: hits.append(keeps(*x)) or hits[-1])
+    a = ebpSolve(heat_problem(), *sum(kw.items(), ()), backend=backend)
+    monkeypatch.setattr(par, 'regrid_keeps', lambda *x: False)
+    b = ebpSolve(heat_problem(), *sum(kw.items(), ()), backend=backend)
+    _same_runs(a, b)
+    return hits
+
+
+def test_regrid_skip_equals_rebuild(monkeypatch):
+    """A regrid that would rebuild the same root-only hierarchy is skipped;
+    the run equals the one that rebuilds at every regrid, bit for bit (the
+    early regrids of this run still change the hierarchy and rebuild)."""
+    hits = _skip_vs_rebuild(OracleBackend(), 32, 3, monkeypatch)
+    assert any(hits) and not all(hits)
+
+
+@pytest.mark.gpu
+def test_regrid_skip_equals_rebuild_on_device(monkeypatch):
+    from bsam.device import DeviceBackend
+    hits = _skip_vs_rebuild(DeviceBackend.get(0), 128, 4, monkeypatch)
+    assert all(hits)
