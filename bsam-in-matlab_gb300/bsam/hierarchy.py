@@ -20,6 +20,10 @@ Both hierarchy forms are built here:
 """
 from __future__ import annotations
 
+import hashlib
+import threading
+from collections import OrderedDict
+
 import numpy as np
 
 F = 'F'  # array order used for every patch array
@@ -726,10 +730,35 @@ def coarsest_assemble(H):
     if singular:
         e = np.ones((N, 1))
         K = np.block([[A, e], [e.T, np.zeros((1, 1))]])
-        Ainv = np.linalg.inv(K)[:N, :N]
+        Ainv = dense_inverse(K)[:N, :N]
     else:
-        Ainv = np.linalg.inv(A)
+        Ainv = dense_inverse(A)
     H.coarsest = {'singular': bool(singular), 'bcRhs': bcRhs, 'Ainv': np.ascontiguousarray(Ainv), 'A': A}
+
+
+_INV_LOCK = threading.Lock()
+_INV_CACHE = OrderedDict()
+
+
+def dense_inverse(A):
+    """np.linalg.inv of the coarsest operator, memoised by the matrix's
+    bytes (a rebuilt hierarchy with the same coarsest coefficients -- every
+    regrid of a time-independent problem, every served request of one recipe
+    -- gets the very same inverse without recomputing it) and serialised: the
+    threaded BLAS behind it stalled for about a second whenever two host
+    threads entered it at once."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    key = (A.shape, hashlib.sha1(A.tobytes()).digest())
+    with _INV_LOCK:
+        hit = _INV_CACHE.get(key)
+        if hit is not None and np.array_equal(hit[0], A):
+            _INV_CACHE.move_to_end(key)
+            return hit[1].copy()
+        inv = np.linalg.inv(A)
+        _INV_CACHE[key] = (A.copy(), inv.copy())
+        while len(_INV_CACHE) > 16:
+            _INV_CACHE.popitem(last=False)
+    return inv
 
 
 def compat_project(H):

@@ -217,6 +217,8 @@ class Server:
         self.closed = False
         self.waves_run = []
         self.errors = []
+        # one long-lived worker thread per wave slot
+        self.workers = cf.ThreadPoolExecutor(max_workers=waves, thread_name_prefix='bsam-wave')
         self.dispatcher = threading.Thread(target=self._dispatch, daemon=True)
         self.dispatcher.start()
 
@@ -253,6 +255,7 @@ class Server:
             self.closed = True
             self.lock.notify_all()
         self.dispatcher.join()
+        self.workers.shutdown()
         if self.pool is not None:
             self.pool.shutdown()
 
@@ -302,7 +305,7 @@ class Server:
                     self.lock.wait(0.05)
                 if w is None:
                     return
-            threading.Thread(target=self._run_wave, args=w, daemon=True).start()
+            self.workers.submit(self._run_wave, *w)
 
     def _solve(self, slot, items):
         """One wave on the GPU: merged upload, ebSolveCycles of every

@@ -57,14 +57,23 @@ enum {
   PD_SAME0, PD_SAME1, PD_RING0, PD_RING1, PD_WIN0, PD_FP0, PD_CORR0, PD_PARENT, PDN
 };
 
+// the stream of the hierarchy the calling thread is working on (set by
+// set_device): device buffers are allocated and freed in its order from the
+// device's memory pool, so setting up or tearing down one hierarchy never
+// waits for the work other hierarchies have in flight on other streams (a
+// plain cudaFree synchronises the whole device)
+thread_local cudaStream_t g_stream = nullptr;
+
 template <class T>
 struct DBuf {
   T *p = nullptr;
   size_t n = 0;
+  cudaStream_t s = nullptr;
   int alloc(size_t count) {
     n = count;
     if (count == 0) return BSAM_OK;
-    CK(cudaMalloc(&p, sizeof(T) * count));
+    s = g_stream;
+    CK(cudaMallocAsync((void **)&p, sizeof(T) * count, s));
     return BSAM_OK;
   }
   int upload(const T *h, size_t count, cudaStream_t s) {
@@ -74,7 +83,7 @@ struct DBuf {
     return BSAM_OK;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, s);
     p = nullptr;
     n = 0;
   }
@@ -161,8 +170,8 @@ struct bsam_hier_s {
   DBuf<SlotRange> sranges;
   DBuf<CoarsestD> coarsest;        // one coarsest operator per instance
   int nrtasks = 0, nslots = 0, npartials = 0, hist_stride = 0;
-  ResAcc *acc_host = nullptr;      // pinned, ninst entries
-  int *active_host = nullptr;      // pinned, ninst entries
+  ResAcc *acc_host = nullptr;      // ninst entries (pageable: freeing pinned memory synchronises the device)
+  int *active_host = nullptr;      // ninst entries
   // graph of one V-cycle + fill-down + residual
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -1498,8 +1507,8 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
   for (int k = 1; k <= d->nlev; ++k) np += h->lev[k].cell.nblocks;
   h->npartials = np;
   if ((rc = h->partials.alloc((size_t)4 * std::max(np, 1)))) return rc;
-  CK(cudaMallocHost(&h->acc_host, sizeof(ResAcc) * h->ninst));
-  CK(cudaMallocHost(&h->active_host, sizeof(int) * h->ninst));
+  h->acc_host = new ResAcc[h->ninst]();
+  h->active_host = new int[h->ninst]();
   CK(cudaStreamSynchronize(s));
   return BSAM_OK;
 }
@@ -1519,8 +1528,8 @@ void release(bsam_hier h) {
   h->flags.release(); h->g_type.release(); h->patches.release(); h->acc.release(); h->perim.release();
   h->rchunks.release(); h->cact.release(); h->crange.release(); h->levelx.release(); h->rtasks.release(); h->instres.release(); h->sranges.release();
   h->coarsest.release();
-  if (h->acc_host) cudaFreeHost(h->acc_host);
-  if (h->active_host) cudaFreeHost(h->active_host);
+  delete[] h->acc_host;
+  delete[] h->active_host;
   h->acc_host = nullptr;
   h->active_host = nullptr;
 }
@@ -1534,6 +1543,7 @@ int check_opts(const bsam_solve_opts *o) {
 
 int set_device(bsam_hier h) {
   CK(cudaSetDevice(h->ctx->device));
+  g_stream = h->stream;
   return BSAM_OK;
 }
 
@@ -1562,6 +1572,15 @@ int bsam_ctx_create(int device, bsam_ctx *out) {
     delete c;
     return cuda_fail(se, "cudaStreamCreate");
   }
+  // this process's device buffers come from the device's default memory
+  // pool in stream order; freed blocks stay in the pool for the next
+  // hierarchy instead of going back to the driver at every synchronisation
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  cudaGetLastError();
   *out = c;
   return BSAM_OK;
 }
@@ -1586,7 +1605,7 @@ int bsam_fp64_rate(bsam_ctx ctx, double *gops) {
   CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   const int blocks = sms * 8, iters = 4096;
   double *out = nullptr;
-  CK(cudaMalloc(&out, sizeof(double) * blocks * kBlock));
+  CK(cudaMallocAsync((void **)&out, sizeof(double) * blocks * kBlock, ctx->stream));
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
@@ -1603,7 +1622,7 @@ int bsam_fp64_rate(bsam_ctx ctx, double *gops) {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   const cudaError_t e = cudaGetLastError();
-  cudaFree(out);
+  cudaFreeAsync(out, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(e, "bsam_fp64_rate");
   *gops = (double)kFp64RateOps * iters * blocks * kBlock / (best * 1e-3) / 1e9;
   return BSAM_OK;
@@ -1612,8 +1631,8 @@ int bsam_fp64_rate(bsam_ctx ctx, double *gops) {
 int bsam_ctx_destroy(bsam_ctx ctx) {
   if (!ctx) return BSAM_OK;
   cudaSetDevice(ctx->device);
+  if (ctx->scratch) cudaFreeAsync(ctx->scratch, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
-  if (ctx->scratch) cudaFree(ctx->scratch);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return BSAM_OK;
@@ -1854,7 +1873,7 @@ int bsam_tag_level(bsam_hier h, int level, int indicator, double threshold, int 
   if (rc) return rc;
   const size_t n = (size_t)n0 * n1;
   uint8_t *buf = nullptr;
-  CK(cudaMalloc(&buf, 3 * n));
+  CK(cudaMallocAsync((void **)&buf, 3 * n, h->stream));
   uint8_t *T = buf, *cover = buf + n, *out = buf + 2 * n;
   cudaError_t e = cudaMemsetAsync(buf, 0, 2 * n, h->stream);
   if (e == cudaSuccess) {
@@ -1872,7 +1891,7 @@ int bsam_tag_level(bsam_hier h, int level, int indicator, double threshold, int 
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(mask, out, n, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-  cudaFree(buf);
+  cudaFreeAsync(buf, h->stream);
   if (e != cudaSuccess) return cuda_fail(e, "bsam_tag_level");
   return BSAM_OK;
 }

@@ -108,11 +108,11 @@ extern "C" int bsam_polygon_dist2(bsam_ctx ctx, const double *verts, int nverts,
   GCK(cudaSetDevice(ctx->device));
   const size_t nv = 2 * (size_t)nverts;
   const size_t need = sizeof(double) * (nv + 3 * (size_t)n);
-  if (need > ctx->scratch_bytes) {
-    if (ctx->scratch) cudaFree(ctx->scratch);
+  if (need > ctx->scratch_bytes) {   // stream-ordered: no device-wide synchronisation
+    if (ctx->scratch) cudaFreeAsync(ctx->scratch, ctx->stream);
     ctx->scratch = nullptr;
     ctx->scratch_bytes = 0;
-    GCK(cudaMalloc(&ctx->scratch, need));
+    GCK(cudaMallocAsync(&ctx->scratch, need, ctx->stream));
     ctx->scratch_bytes = need;
   }
   double *dv = (double *)ctx->scratch, *dx = dv + nv, *dy = dx + n, *db = dy + n;
