@@ -145,8 +145,7 @@ struct bsam_hier_s {
   // coefficients -- on levels whose h^2 is a power of two pre-multiplied by
   // the exact 1/h^2 -- and InvDiagS; built on the host from these copies
   DBuf<double> rpack;
-  std::vector<double> hDeWr, hDnSr, hID;
-  std::vector<RelaxChunk> hchunks;
+  DBuf<RelaxChunk> pchunks;        // chunk records with coefficient offsets (operand packing)
   DBuf<double> Uo, Uoo, fsrc;      // parabolic history (cells) and f staging
   bool f32_dirty = true;
   DecompH all_cells;               // every cell of every level (batch force reset)
@@ -297,30 +296,22 @@ template <class T> const T *relax_pack(bsam_hier h);
 template <> const double *relax_pack<double>(bsam_hier h) { return h->rpack.p; }
 template <> const float *relax_pack<float>(bsam_hier h) { return h->rpack32.p; }
 
-// pack the smoother's operands of every chunk and colour (see kPackRows)
+// pack the smoother's operands of every chunk and colour (see kPackRows) on
+// the device, from the resident DeW, DnS and InvDiagS: at upload and after
+// any of the three changes
 int build_relax_pack(bsam_hier h) {
-  const size_t row = kPackRows * kChunk;
-  std::vector<double> pk(std::max<size_t>(h->hchunks.size(), 1) * 2 * row, 0.0);
-  for (size_t ch = 0; ch < h->hchunks.size(); ++ch) {
-    const RelaxChunk &R = h->hchunks[ch];
-    const int half = R.mx >> 1;
-    for (int m = 0; m < 2; ++m) {
-      double *o = pk.data() + (ch * 2 + m) * row;
-      for (int t = 0; t < R.n; ++t) {
-        const int s = R.s0 + t;
-        const int lj = s / half;
-        const int li = 2 * (s - lj * half) + ((m + lj + R.par0) & 1);
-        o[t] = h->hDeWr[R.dew_off + (li + 1) + lj * (R.mx + 1)];
-        o[kChunk + t] = h->hDeWr[R.dew_off + li + lj * (R.mx + 1)];
-        o[2 * kChunk + t] = h->hDnSr[R.dns_off + li + (lj + 1) * R.mx];
-        o[3 * kChunk + t] = h->hDnSr[R.dns_off + li + lj * R.mx];
-        o[4 * kChunk + t] = h->hID[R.c_off + li + lj * R.mx];
-      }
-    }
-  }
+  const size_t nch = h->pchunks.n;
   int rc;
-  if (!h->rpack.p && (rc = h->rpack.alloc(pk.size()))) return rc;
-  CK(cudaMemcpyAsync(h->rpack.p, pk.data(), sizeof(double) * pk.size(), cudaMemcpyHostToDevice, h->stream));
+  if (!h->rpack.p && (rc = h->rpack.alloc(std::max<size_t>(nch, 1) * 2 * kPackRows * kChunk))) return rc;
+  for (int k = 1; k <= h->nlev; ++k) {
+    const LevelPlan &L = h->lev[k];
+    if (!L.rc_n) continue;
+    const int64_t items = (int64_t)L.rc_n * 2 * kChunk;
+    k_pack<<<(unsigned)((items + kBlock - 1) / kBlock), kBlock, 0, h->stream>>>(
+        h->pchunks.p + L.rc_off, L.rc_n, h->DeW.p, h->DnS.p, h->ID.p, 1.0 / (L.hx * L.hx), 1.0 / (L.hy * L.hy),
+        L.pow2 ? 1 : 0, h->rpack.p + (size_t)L.rc_off * 2 * kPackRows * kChunk);
+  }
+  CK(cudaGetLastError());
   CK(cudaStreamSynchronize(h->stream));
   h->f32_dirty = true;
   return BSAM_OK;
@@ -923,18 +914,33 @@ struct Builder {
   // ebFillGhosts.m in order, later stages overriding), ring refresh items,
   // physical corners last
   int ghosts(int k, LevelPlan &L) {
-    std::map<int, size_t> rule;   // dst -> index into tmp
+    // dst -> index into tmp, over the Q range of this level's patches (a flat
+    // index: a level has one rule slot per ghost cell)
+    int64_t qlo = INT64_MAX, qhi = 0;
+    for (int p = L.p0; p < L.p1; ++p) {
+      const int32_t *r = P(p);
+      qlo = std::min<int64_t>(qlo, r[PD_QOFF]);
+      qhi = std::max<int64_t>(qhi, (int64_t)r[PD_QOFF] + (int64_t)(r[PD_MX] + 2) * (r[PD_MY] + 2));
+    }
+    if (qlo < 0 || qhi > d->n_q || qhi <= qlo) return fail(BSAM_ERR_ARG, "patch Q range outside Q");
+    std::vector<int> slot((size_t)(qhi - qlo), -1);
+    bool outside = false;
+    auto rule_at = [&](int dst) -> int {
+      if (dst < qlo || dst >= qhi) { outside = true; return -1; }
+      return slot[(size_t)(dst - qlo)];
+    };
     struct G { int8_t t; int dst, a, b, c, dd, e; int inst = 0; };
     std::vector<G> tmp, ringi, corners;
     int cur = 0;                  // instance of the patch being planned
     auto put = [&](G g) {
       g.inst = cur;
-      auto it = rule.find(g.dst);
-      if (it == rule.end()) {
-        rule[g.dst] = tmp.size();
+      if (g.dst < qlo || g.dst >= qhi) { outside = true; return; }
+      int &sl = slot[(size_t)(g.dst - qlo)];
+      if (sl < 0) {
+        sl = (int)tmp.size();
         tmp.push_back(g);
       } else {
-        tmp[it->second] = g;
+        tmp[sl] = g;
       }
     };
     const bool qif = h->opts.ghost_interp == 0;
@@ -1039,13 +1045,14 @@ struct Builder {
       if (r[PD_CCNW] == 1) corners.push_back({G_PHYS_CORNER, Q(1, my + 2), Q(2, my + 2), Q(1, my + 1), Q(2, my + 1), 0, 0, cur});
       if (r[PD_CCNE] == 1) corners.push_back({G_PHYS_CORNER, Q(mx + 2, my + 2), Q(mx + 1, my + 2), Q(mx + 2, my + 1), Q(mx + 1, my + 1), 0, 0, cur});
     }
+    if (outside) return fail(BSAM_ERR_ARG, "ghost destination outside its level's patches");
     L.g1_off = (int)gt.size();
     for (G &g : corners) {
-      if (rule.count(g.dst)) return fail(BSAM_ERR_ARG, "physical corner also written by another ghost stage");
-      auto i1 = rule.find(g.a), i2 = rule.find(g.b);
-      if (i1 == rule.end() || i2 == rule.end()) return fail(BSAM_ERR_ARG, "physical corner next to a ghost without a rule");
-      g.a = L.g1_off + (int)i1->second;
-      g.b = L.g1_off + (int)i2->second;
+      if (rule_at(g.dst) >= 0) return fail(BSAM_ERR_ARG, "physical corner also written by another ghost stage");
+      const int i1 = rule_at(g.a), i2 = rule_at(g.b);
+      if (i1 < 0 || i2 < 0) return fail(BSAM_ERR_ARG, "physical corner next to a ghost without a rule");
+      g.a = L.g1_off + i1;
+      g.b = L.g1_off + i2;
     }
     auto emit = [&](const std::vector<G> &v) {
       for (const G &g : v) {
@@ -1066,9 +1073,9 @@ struct Builder {
       pe_off[p] = (int)perim.size();
       auto add = [&](int side, int dst) -> bool {
         if (r[PD_BCW + side] != 0) { perim.push_back(Rule{-1, 0, 0, 0, 0, 0}); return true; }
-        auto it = rule.find(dst);
-        if (it == rule.end()) return false;
-        const G &g = tmp[it->second];
+        const int ri = rule_at(dst);
+        if (ri < 0) return false;
+        const G &g = tmp[ri];
         if (g.t != G_COPY && g.t != G_QIF && g.t != G_QIF_END && g.t != G_LIF) return false;
         perim.push_back(Rule{g.t, g.a, g.b, g.c, g.dd, g.e});
         return true;
@@ -1348,25 +1355,10 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
       CK(cudaMemsetAsync(h->cact.p, 1, h->cact.n, s));
     }
   }
-  // smoother coefficients, exactly scaled by 1/h^2 on power-of-two levels
+  // smoother operands, the face coefficients exactly scaled by 1/h^2 on
+  // power-of-two levels, packed on the device
   {
-    std::vector<double> dew(d->DeW, d->DeW + d->n_dew), dns(d->DnS, d->DnS + d->n_dns);
-    for (int k = 1; k <= d->nlev; ++k) {
-      const LevelPlan &L = h->lev[k];
-      if (!L.pow2) continue;
-      const double ix = 1.0 / (L.hx * L.hx), iy = 1.0 / (L.hy * L.hy);
-      for (int p = L.p0; p < L.p1; ++p) {
-        const int32_t *r = B.P(p);
-        const int64_t mx = r[PD_MX], my = r[PD_MY];
-        for (int64_t i = 0; i < (mx + 1) * my; ++i) dew[r[PD_DEWOFF] + i] *= ix;
-        for (int64_t i = 0; i < mx * (my + 1); ++i) dns[r[PD_DNSOFF] + i] *= iy;
-      }
-    }
-    h->hDeWr.swap(dew);
-    h->hDnSr.swap(dns);
-    h->hID.assign(d->InvDiagS, d->InvDiagS + d->n_cells);
-    h->hchunks = B.chunks;
-    if ((rc = build_relax_pack(h))) return rc;
+    if ((rc = h->pchunks.upload(B.chunks.data(), B.chunks.size(), s)) || (rc = build_relax_pack(h))) return rc;
     h->relax_n[0].assign(d->nlev + 1, 1);
     h->relax_n[1].assign(d->nlev + 1, 1);
   }
@@ -1526,7 +1518,7 @@ void release(bsam_hier h) {
                        &h->ct_j, &h->active, &h->iters, &h->ones, &h->g_inst, &h->ring_inst, &h->inst_nlev, &h->g_dst, &h->g_a, &h->g_b, &h->g_c, &h->g_d, &h->g_e})
     b->release();
   h->flags.release(); h->g_type.release(); h->patches.release(); h->acc.release(); h->perim.release();
-  h->rchunks.release(); h->cact.release(); h->crange.release(); h->levelx.release(); h->rtasks.release(); h->instres.release(); h->sranges.release();
+  h->rchunks.release(); h->pchunks.release(); h->cact.release(); h->crange.release(); h->levelx.release(); h->rtasks.release(); h->instres.release(); h->sranges.release();
   h->coarsest.release();
   delete[] h->acc_host;
   delete[] h->active_host;
@@ -1709,27 +1701,6 @@ static DBuf<double> *field_buf(bsam_hier h, int which) {
 }
 
 // the smoother's packed operands after an update of DeW, DnS or InvDiagS
-static int repack(bsam_hier h, int which, const double *host) {
-  if (which == BSAM_FIELD_INVDIAG) {
-    h->hID.assign(host, host + h->ID.n);
-    return build_relax_pack(h);
-  }
-  const bool x = which == BSAM_FIELD_DEW;
-  std::vector<double> &v = x ? h->hDeWr : h->hDnSr;
-  v.assign(host, host + (x ? h->DeW.n : h->DnS.n));
-  for (int k = 1; k <= h->nlev; ++k) {
-    const LevelPlan &L = h->lev[k];
-    if (!L.pow2) continue;
-    const double sc = x ? 1.0 / (L.hx * L.hx) : 1.0 / (L.hy * L.hy);
-    for (int p = L.p0; p < L.p1; ++p) {
-      const int32_t *r = h->hpatches.data() + (size_t)p * PDN;
-      const int64_t off = x ? r[PD_DEWOFF] : r[PD_DNSOFF];
-      const int64_t n = x ? (int64_t)(r[PD_MX] + 1) * r[PD_MY] : (int64_t)r[PD_MX] * (r[PD_MY] + 1);
-      for (int64_t i = 0; i < n; ++i) v[off + i] *= sc;
-    }
-  }
-  return build_relax_pack(h);
-}
 
 int bsam_set_field(bsam_hier h, int which, const double *host, int64_t n) {
   if (!h || !host) return fail(BSAM_ERR_ARG, "null argument");
@@ -1741,7 +1712,7 @@ int bsam_set_field(bsam_hier h, int which, const double *host, int64_t n) {
     if (n) CK(cudaMemcpyAsync(b->p, host, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   if (which == BSAM_FIELD_DEW || which == BSAM_FIELD_DNS || which == BSAM_FIELD_INVDIAG) {
-    if ((rc = repack(h, which, host))) return rc;
+    if ((rc = build_relax_pack(h))) return rc;
   }
   if (which >= BSAM_FIELD_CC && which <= BSAM_FIELD_BCRHS) h->f32_dirty = true;
   return BSAM_OK;

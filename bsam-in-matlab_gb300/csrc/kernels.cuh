@@ -271,6 +271,43 @@ __device__ __forceinline__ void prefetch_l1(const R *p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"((const char *)(p + 1) - 1));
 }
 
+// Builds the packed operands of one level's chunks on the device from the
+// reference-layout DeW, DnS and InvDiagS (one thread per chunk, colour and
+// slot; slots past a chunk's cell count are zero).  `scale` multiplies the
+// face coefficients by the exact 1/h^2 of a power-of-two level (ix, iy), the
+// same product the relaxation's pre-scaled form relies on.
+__global__ void __launch_bounds__(kBlock) k_pack(const RelaxChunk *__restrict__ ch, int nch,
+                                                 const double *__restrict__ DeW, const double *__restrict__ DnS,
+                                                 const double *__restrict__ ID, double ix, double iy, int scale,
+                                                 double *__restrict__ pack) {
+  const int64_t w = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  if (w >= (int64_t)nch * 2 * kChunk) return;
+  const int c = (int)(w / (2 * kChunk)), m = (int)((w / kChunk) & 1), t = (int)(w % kChunk);
+  const RelaxChunk R = ch[c];
+  double *o = pack + ((size_t)c * 2 + m) * (kPackRows * kChunk) + t;
+  if (t >= R.n) {
+#pragma unroll
+    for (int r = 0; r < kPackRows; ++r) o[r * kChunk] = 0.0;
+    return;
+  }
+  const int s = R.s0 + t, half = R.mx >> 1;
+  const int lj = s / half;
+  const int li = 2 * (s - lj * half) + ((m + lj + R.par0) & 1);
+  double e = DeW[R.dew_off + (li + 1) + lj * (R.mx + 1)], wv = DeW[R.dew_off + li + lj * (R.mx + 1)];
+  double n = DnS[R.dns_off + li + (lj + 1) * R.mx], sv = DnS[R.dns_off + li + lj * R.mx];
+  if (scale) {
+    e = e * ix;
+    wv = wv * ix;
+    n = n * iy;
+    sv = sv * iy;
+  }
+  o[0] = e;
+  o[kChunk] = wv;
+  o[2 * kChunk] = n;
+  o[3 * kChunk] = sv;
+  o[4 * kChunk] = ID[R.c_off + li + lj * R.mx];
+}
+
 // one colour-cell update of chunk ch (thread tc of the chunk); kChain: the
 // grid kernel's programmatic-launch wait sits between the static loads and
 // the first read of the solution
