@@ -368,6 +368,20 @@ int cluster_ctas() {
   return cached;
 }
 
+// resident blocks of the persistent smoother on the whole device
+template <class T, bool kPow2>
+int persistent_blocks() {
+  static int cached = -1;
+  if (cached >= 0) return cached;
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_relax_p<T, kPow2>, kBlock, 0);
+  cudaGetLastError();
+  cached = std::max(1, sms * std::max(per, 1));
+  return cached;
+}
+
 template <class T, bool kPow2, class... Args>
 void launch_cluster(bsam_hier h, int ctas, Args... args) {
   cudaLaunchConfig_t cfg = {};
@@ -424,6 +438,17 @@ void launch_relax(bsam_hier h, int k, int nsweeps, bool first_fresh = false) {
     for (int m = 0; m < 2; ++m) {
       const int fresh = (first_fresh || s > 0 || m > 0) ? 1 : 0;
       Launch l(h, K_RELAX, 24.0 * tscale<T>() * (double)L.ncells, k);
+      if (kn == 3) {   // persistent blocks walking the chunk groups
+        const Rule *pr = (const Rule *)h->perim.p;
+        const T om = (T)h->opts.omega;
+        if (L.pow2)
+          launch_k(h, k_relax_p<T, true>, std::min(grid, persistent_blocks<T, true>()), kBlock, ld, ch, L.rc_n, f, pk,
+                   pr, m, om, unit, fresh, ca, am);
+        else
+          launch_k(h, k_relax_p<T, false>, std::min(grid, persistent_blocks<T, false>()), kBlock, ld, ch, L.rc_n, f,
+                   pk, pr, m, om, unit, fresh, ca, am);
+        continue;
+      }
       if (kn > 1) {
         const int cpb = kBlock * kn / kChunk;     // chunks per block
         const int g = (L.rc_n + cpb - 1) / cpb;
@@ -597,7 +622,8 @@ int launch_iteration(bsam_hier h, int mode) {
 }
 
 // Autotuner of the smoother's launch form, per level and precision: on a
-// level large enough to matter, 1, 2 or 4 colour cells per thread; on a
+// level large enough to matter, 1, 2 or 4 colour cells per thread or the
+// persistent form (kn 3: resident blocks walking the chunk groups); on a
 // level that one thread-block cluster covers with at most 4 cells per
 // thread, separate launches per colour pass or the single cluster launch
 // (kn 0).  Each candidate's relaxation (npre sweeps and the closing fill) is
@@ -605,7 +631,7 @@ int launch_iteration(bsam_hier h, int mode) {
 // cycle runs in; the fastest is kept.  The choice does not change a single
 // bit of the result (each update's arithmetic is the same), so it is tuned
 // on the live state and the FP64 state is restored afterwards.
-// BSAM_RELAX_N=0|1|2|4 forces one form on every level.
+// BSAM_RELAX_N=0|1|2|3|4 forces one form on every level.
 constexpr int64_t kTuneMinCells = 131072;
 constexpr int kClusterMaxPerThread = 4;
 
@@ -627,7 +653,7 @@ int tune_level(bsam_hier h, int k, int set, int *best) {
   float bt = 1e30f;
   *best = 1;
   const int ns = std::max(h->opts.npre, 1);
-  const std::vector<int> cand = set == 1 ? std::vector<int>{1, 2, 4} : std::vector<int>{1, 0};
+  const std::vector<int> cand = set == 1 ? std::vector<int>{1, 2, 4, 3} : std::vector<int>{1, 0};
   for (int kn : cand) {
     rn[k] = kn;
     launch_relax<T>(h, k, ns);         // warm-up
@@ -701,7 +727,7 @@ int autotune(bsam_hier h) {
   if (const char *env = getenv("BSAM_RELAX_N")) {
     int kn = atoi(env);
     if (kn == 0 && cluster_ctas() == 0) kn = 1;
-    rn.assign(h->nlev + 1, (kn == 0 || kn == 2 || kn == 4) ? kn : 1);
+    rn.assign(h->nlev + 1, (kn >= 0 && kn <= 4) ? kn : 1);
     rn[1] = 1;
     return BSAM_OK;
   }

@@ -308,102 +308,169 @@ __global__ void __launch_bounds__(kBlock) k_pack(const RelaxChunk *__restrict__ 
   o[4 * kChunk] = ID[R.c_off + li + lj * R.mx];
 }
 
-// one colour-cell update of chunk ch (thread tc of the chunk); kChain: the
-// grid kernel's programmatic-launch wait sits between the static loads and
-// the first read of the solution
-template <class T, bool kPow2, bool kChain, bool kCG = false>
-__device__ __forceinline__ void relax_cell(const LevelD &L, const RelaxChunkD *__restrict__ chunks, int nchunks,
-                                           const FieldsT<T> &f, const T *__restrict__ pack,
-                                           const Rule *__restrict__ perim, int m, T omega, int unit_omega, int fresh,
-                                           const uint8_t *__restrict__ cact, int amode, int ch, int tc) {
-  // the chunk record, its frozen flag and the packed operands are indexed
-  // by the chunk alone: record and flag are requested together, the
-  // operands (a chunk's pack rows hold kChunk entries whatever its cell
-  // count) as soon as the small, cached flag says the chunk is live, so
-  // they are in flight with the record and a frozen chunk reads nothing else
-  const bool okc = ch < nchunks;
+// One colour-cell update in three stages, so that a persistent block can
+// overlap them across chunk groups (k_relax_p): issue (the chunk record, its
+// frozen flag and the packed operands), derive (the cell's position, its
+// boundary data and ghost rules, all static), update (solution loads, ghost
+// values, the candidate and its store).  relax_cell runs the three in order.
+template <class T>
+struct CellState {
   RelaxChunkD R;
-  bool live = okc;
-  T dE = 0, dW = 0, dN = 0, dS = 0, idg = 0;
+  T dE, dW, dN, dS, idg, gx, gy;
+  int q_off, c, cc, ldq, code, rx, ry;   // code: kx | ky << 2 | sx << 4 | sy << 5
+  bool live;
+};
+
+// the chunk record, its frozen flag and the packed operands are indexed by
+// the chunk alone: record and flag are requested together, the operands (a
+// chunk's pack rows hold kChunk entries whatever its cell count) as soon as
+// the small, cached flag says the chunk is live, so they are in flight with
+// the record and a frozen chunk reads nothing else
+template <class T>
+__device__ __forceinline__ void cell_issue(const RelaxChunkD *__restrict__ chunks, int nchunks,
+                                           const T *__restrict__ pack, int m, const uint8_t *__restrict__ cact,
+                                           int amode, int ch, int tc, CellState<T> &S) {
+  const bool okc = ch < nchunks;
+  S.live = okc;
+  S.dE = S.dW = S.dN = S.dS = S.idg = T(0);
   if (okc) {
-    R = chunks[ch];
-    if (amode == kActChunk) live = cact[ch] != 0;
+    S.R = chunks[ch];
+    if (amode == kActChunk) S.live = cact[ch] != 0;
   }
-  if (live) {
+  if (S.live) {
     const T *__restrict__ pk = pack + (size_t)(ch * 2 + m) * (kPackRows * kChunk) + tc;
-    dE = __ldg(pk);
-    dW = __ldg(pk + kChunk);
-    dN = __ldg(pk + 2 * kChunk);
-    dS = __ldg(pk + 3 * kChunk);
-    idg = __ldg(pk + 4 * kChunk);
+    S.dE = __ldg(pk);
+    S.dW = __ldg(pk + kChunk);
+    S.dN = __ldg(pk + 2 * kChunk);
+    S.dS = __ldg(pk + 3 * kChunk);
+    S.idg = __ldg(pk + 4 * kChunk);
   }
-  if (!live || tc >= R.n || (amode == kActInst && !f.active[R.inst])) {
-    if (kChain) chain_wait();
+}
+
+template <class T>
+__device__ __forceinline__ void cell_derive(const FieldsT<T> &f, const Rule *__restrict__ perim, int m, int fresh,
+                                            int amode, int tc, CellState<T> &S) {
+  if (!S.live || tc >= S.R.n || (amode == kActInst && !f.active[S.R.inst])) {
+    S.live = false;
     return;
   }
+  const RelaxChunkD &R = S.R;
   const int s = R.s0 + tc;
   const int mx = R.mx, my = R.my, half = mx >> 1;
   const int lj = s / half;
   const int li = 2 * (s - lj * half) + ((m + lj + chunk_par0(R.flags)) & 1);
-  const int ldq = mx + 2;
-  const int c = (li + 1) + (lj + 1) * ldq;
-  const int cc = R.c_off + li + lj * mx;
-  // static boundary data and ghost rules
+  S.ldq = mx + 2;
+  S.c = (li + 1) + (lj + 1) * S.ldq;
+  S.cc = R.c_off + li + lj * mx;
+  S.q_off = R.q_off;
+  // static boundary data and ghost rules; a cell touches at most one x side
+  // (W or E) and one y side (S or N): kind 0 interior neighbour, 1
+  // Dirichlet, 2 Neumann, 3 ghost rule
   const T *__restrict__ g4 = f.bcg + R.bcg_off;
-  // a cell touches at most one x side (W or E) and one y side (S or N):
-  // kind 0 interior neighbour, 1 Dirichlet, 2 Neumann, 3 ghost rule
   int kx = 0, ky = 0, sx = 0, sy = 0;       // sx: 0 west 1 east; sy: 0 south 1 north
-  T gx = 0, gy = 0;
-  int rx = 0, ry = 0;                       // ghost rule indices (perimeter table)
+  S.gx = S.gy = T(0);
+  S.rx = S.ry = 0;                          // ghost rule indices (perimeter table)
   if (li == 0 || li == mx - 1) {
     sx = (li == 0) ? 0 : 1;
     const int bc = chunk_bc(R.flags, sx);   // a shift, not an indexed (local-memory) array
-    if (bc) { kx = bc; gx = __ldg(g4 + sx * my + lj); }
-    else if (fresh) { kx = 3; rx = R.pe_off + sx * my + lj; prefetch_l1(perim + rx); }
+    if (bc) { kx = bc; S.gx = __ldg(g4 + sx * my + lj); }
+    else if (fresh) { kx = 3; S.rx = R.pe_off + sx * my + lj; prefetch_l1(perim + S.rx); }
   }
   if (lj == 0 || lj == my - 1) {
     sy = (lj == 0) ? 0 : 1;
     const int bc = chunk_bc(R.flags, 2 + sy);
-    if (bc) { ky = bc; gy = __ldg(g4 + 2 * my + sy * mx + li); }
-    else if (fresh) { ky = 3; ry = R.pe_off + 2 * my + sy * mx + li; prefetch_l1(perim + ry); }
+    if (bc) { ky = bc; S.gy = __ldg(g4 + 2 * my + sy * mx + li); }
+    else if (fresh) { ky = 3; S.ry = R.pe_off + 2 * my + sy * mx + li; prefetch_l1(perim + S.ry); }
   }
-  if (kChain) chain_wait();
+  S.code = kx | (ky << 2) | (sx << 4) | (sy << 5);
+}
+
+template <class T, bool kPow2, bool kCG>
+__device__ __forceinline__ void cell_update(const LevelD &L, const FieldsT<T> &f, const Rule *__restrict__ perim,
+                                            T omega, int unit_omega, const CellState<T> &S) {
+  if (!S.live) return;
   const T c83 = T(8.0 / 3.0), c13 = T(1.0 / 3.0);
   const LevelH<T> H = level_h(L, T(0));
-  T *__restrict__ Q = f.Q + R.q_off;
+  const int c = S.c, ldq = S.ldq;
+  const int kx = S.code & 3, ky = (S.code >> 2) & 3, sx = (S.code >> 4) & 1, sy = (S.code >> 5) & 1;
+  T *__restrict__ Q = f.Q + S.q_off;
   T qe = ld_sol<kCG>(Q + c + 1), qw = ld_sol<kCG>(Q + c - 1), qn = ld_sol<kCG>(Q + c + ldq), qs = ld_sol<kCG>(Q + c - ldq);
-  T t = f.F[cc];
+  T t = f.F[S.cc];
   if (kx > 0) {
     T v;
-    if (kx == 1) v = c83 * gx + c13 * ld_sol<kCG>(Q + (sx ? c - 1 : c + 1));
-    else if (kx == 2) v = H.hx * gx;
-    else v = eval_inline<T, kCG>(perim[rx], f.Q);
+    if (kx == 1) v = c83 * S.gx + c13 * ld_sol<kCG>(Q + (sx ? c - 1 : c + 1));
+    else if (kx == 2) v = H.hx * S.gx;
+    else v = eval_inline<T, kCG>(perim[S.rx], f.Q);
     if (sx) qe = v; else qw = v;
   }
   if (ky > 0) {
     T v;
-    if (ky == 1) v = c83 * gy + c13 * ld_sol<kCG>(Q + (sy ? c - ldq : c + ldq));
-    else if (ky == 2) v = H.hy * gy;
-    else v = eval_inline<T, kCG>(perim[ry], f.Q);
+    if (ky == 1) v = c83 * S.gy + c13 * ld_sol<kCG>(Q + (sy ? c - ldq : c + ldq));
+    else if (ky == 2) v = H.hy * S.gy;
+    else v = eval_inline<T, kCG>(perim[S.ry], f.Q);
     if (sy) qn = v; else qs = v;
   }
   // kPow2: the coefficients arrive pre-scaled by the exact 1/h^2 (a power of
   // two), and (q D) 2^-k == q (D 2^-k) in floating point, so one product
   // per neighbour gives the reference's (q D)/h^2 bit for bit
   if (kPow2) {
-    t = t + qe * dE;
-    t = t + qw * dW;
-    t = t + qn * dN;
-    t = t + qs * dS;
+    t = t + qe * S.dE;
+    t = t + qw * S.dW;
+    t = t + qn * S.dN;
+    t = t + qs * S.dS;
   } else {
-    t = t + (qe * dE) / H.hx2;
-    t = t + (qw * dW) / H.hx2;
-    t = t + (qn * dN) / H.hy2;
-    t = t + (qs * dS) / H.hy2;
+    t = t + (qe * S.dE) / H.hx2;
+    t = t + (qw * S.dW) / H.hx2;
+    t = t + (qn * S.dN) / H.hy2;
+    t = t + (qs * S.dS) / H.hy2;
   }
-  t = t * idg;
+  t = t * S.idg;
   if (unit_omega) Q[c] = t;
   else Q[c] = omega * t + (1 - omega) * ld_sol<kCG>(Q + c);
+}
+
+// one colour-cell update of chunk ch (thread tc of the chunk); kChain: the
+// grid kernel's programmatic-launch wait sits between the static stages and
+// the first read of the solution
+template <class T, bool kPow2, bool kChain, bool kCG = false>
+__device__ __forceinline__ void relax_cell(const LevelD &L, const RelaxChunkD *__restrict__ chunks, int nchunks,
+                                           const FieldsT<T> &f, const T *__restrict__ pack,
+                                           const Rule *__restrict__ perim, int m, T omega, int unit_omega, int fresh,
+                                           const uint8_t *__restrict__ cact, int amode, int ch, int tc) {
+  CellState<T> S;
+  cell_issue<T>(chunks, nchunks, pack, m, cact, amode, ch, tc, S);
+  cell_derive<T>(f, perim, m, fresh, amode, tc, S);
+  if (kChain) chain_wait();
+  cell_update<T, kPow2, kCG>(L, f, perim, omega, unit_omega, S);
+}
+
+// Persistent form of one colour pass: a grid of resident blocks walks the
+// level's chunk groups (kBlock / kChunk chunks each) with a grid stride;
+// while a block updates one group it has the next group's chunk records and
+// operands in flight, and derives that group's static data after the
+// update.  The arithmetic of every update is relax_cell's.
+template <class T, bool kPow2>
+__global__ void __launch_bounds__(kBlock) k_relax_p(LevelD L, const RelaxChunkD *__restrict__ chunks, int nchunks,
+                                                    FieldsT<T> f, const T *__restrict__ pack,
+                                                    const Rule *__restrict__ perim, int m, T omega, int unit_omega,
+                                                    int fresh, const uint8_t *__restrict__ cact, int amode) {
+  chain_trigger();
+  constexpr int cpb = kBlock / kChunk;
+  const int sub = threadIdx.x / kChunk, tc = threadIdx.x & (kChunk - 1);
+  const int ngroups = (nchunks + cpb - 1) / cpb;
+  int g = blockIdx.x;
+  CellState<T> cur, nxt;
+  cell_issue<T>(chunks, nchunks, pack, m, cact, amode, g * cpb + sub, tc, cur);
+  cell_derive<T>(f, perim, m, fresh, amode, tc, cur);
+  chain_wait();
+  while (g < ngroups) {
+    const int gn = g + (int)gridDim.x;
+    cell_issue<T>(chunks, nchunks, pack, m, cact, amode, gn * cpb + sub, tc, nxt);
+    cell_update<T, kPow2, false>(L, f, perim, omega, unit_omega, cur);
+    cell_derive<T>(f, perim, m, fresh, amode, tc, nxt);
+    cur = nxt;
+    g = gn;
+  }
 }
 
 // Coarsened smoother: each thread updates kN colour cells of its chunk

@@ -239,11 +239,13 @@ int bsam_launch_count(bsam_hier h, int64_t *count);
 /* The smoother's launch form per level as the autotuner chose it at the
  * first solve, levels 1..nlev in cells_per_thread[0..nlev-1], for
  * precision 0 (FP64 cycle) or 1 (FP32 correction cycle): 1, 2 or 4 colour
- * cells updated per thread, one launch per colour pass; 0 for the whole
- * relaxation (every pass and the closing ghost fill) in one launch of a
- * single thread-block cluster; -1 where that cycle has not run yet.  The
- * choice never changes a result bit; BSAM_RELAX_N=0|1|2|4 in the
- * environment forces one form.  No reference counterpart (ebRelaxLevel.m
+ * cells updated per thread, one launch per colour pass; 3 for one launch
+ * per pass of resident blocks that walk the level's chunks, the next
+ * chunks' operands in flight during each update; 0 for the whole relaxation
+ * (every pass and the closing ghost fill) in one launch of a single
+ * thread-block cluster; -1 where that cycle has not run yet.  The choice
+ * never changes a result bit; BSAM_RELAX_N=0|1|2|3|4 in the environment
+ * forces one form.  No reference counterpart (ebRelaxLevel.m
  * has one loop order).                                                    */
 int bsam_relax_tuning(bsam_hier h, int precision, int32_t *cells_per_thread, int cap);
 
