@@ -803,6 +803,15 @@ void drop_graph(bsam_hier h) {
   h->while_tried = false;
 }
 
+// BSAM_SOLVE_LOOP=host selects the per-iteration graph with a host check of
+// the stop tests instead of the device-side loop (the same kernels and
+// results): profilers that cannot see the kernel nodes of a graph holding a
+// conditional node (ncu) see every kernel of the solve that way
+bool host_loop() {
+  const char *e = getenv("BSAM_SOLVE_LOOP");
+  return e && std::strcmp(e, "host") == 0;
+}
+
 // ebSolveCycles' loop as one graph: a conditional WHILE node whose body is
 // one iteration followed by k_any_active, which sets the condition from the
 // instances' stop tests.  A solve is then one graph launch and one read of
@@ -1621,7 +1630,7 @@ int bsam_fp64_rate(bsam_ctx ctx, double *gops) {
   CK(cudaSetDevice(ctx->device));
   int sms = 0;
   CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
-  const int blocks = sms * 8, iters = 4096;
+  const int blocks = sms * 8, iters = 1024;
   double *out = nullptr;
   CK(cudaMallocAsync((void **)&out, sizeof(double) * blocks * kBlock, ctx->stream));
   cudaEvent_t a, b;
@@ -1929,7 +1938,7 @@ int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles,
   // its WHILE graph, else one graph launch per V-cycle with a host check.
   bool on_device = false;
   if (nactive && (rc = autotune(h))) return rc;
-  if (nactive && build_while_graph(h)) {
+  if (nactive && !host_loop() && build_while_graph(h)) {
     CK(cudaGraphLaunch(h->wexec, h->stream));
     if ((rc = read_state(h, &nactive))) return rc;
     on_device = true;

@@ -233,6 +233,11 @@ int bsam_profile_vcycles(bsam_hier h, int ncycles, int level, double ms[BSAM_NKI
 int bsam_save_state(bsam_hier h);
 int bsam_restore_state(bsam_hier h);
 
+/* BSAM_SOLVE_LOOP=host in the environment makes bsam_solve_cycles replay a
+ * per-V-cycle graph with a host check of the stop tests instead of its
+ * device-side loop (a conditional graph node); same kernels and results.
+ * For profilers that cannot see kernels inside conditional graphs.       */
+
 /* Kernels launched on this hierarchy so far (eager and graph-replayed). */
 int bsam_launch_count(bsam_hier h, int64_t *count);
 
