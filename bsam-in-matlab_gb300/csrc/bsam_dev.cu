@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -356,29 +357,32 @@ bool cluster_fits(int ctas) {
 // CTAs of the smoother's single-cluster launch: 16 where every variant fits,
 // else 8, else 0 (the variant is then never chosen)
 int cluster_ctas() {
-  static int cached = -1;
-  if (cached >= 0) return cached;
-  cached = 0;
-  for (int c : {16, 8})
-    if (cluster_fits<double, true>(c) && cluster_fits<double, false>(c) && cluster_fits<float, true>(c) &&
-        cluster_fits<float, false>(c)) {
-      cached = c;
-      break;
-    }
+  static std::once_flag once;
+  static int cached = 0;
+  std::call_once(once, [] {
+    for (int c : {16, 8})
+      if (cluster_fits<double, true>(c) && cluster_fits<double, false>(c) && cluster_fits<float, true>(c) &&
+          cluster_fits<float, false>(c)) {
+        cached = c;
+        break;
+      }
+  });
   return cached;
 }
 
 // resident blocks of the persistent smoother on the whole device
 template <class T, bool kPow2>
 int persistent_blocks() {
-  static int cached = -1;
-  if (cached >= 0) return cached;
-  int dev = 0, sms = 0, per = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_relax_p<T, kPow2>, kBlock, 0);
-  cudaGetLastError();
-  cached = std::max(1, sms * std::max(per, 1));
+  static std::once_flag once;
+  static int cached = 1;
+  std::call_once(once, [] {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_relax_p<T, kPow2>, kBlock, 0);
+    cudaGetLastError();
+    cached = std::max(1, sms * std::max(per, 1));
+  });
   return cached;
 }
 
