@@ -26,3 +26,28 @@ def test_reference_arm_line():
     cb = d['cpu_baseline']
     assert set(cb) >= {'value', 'unit', 'cores', 'kind', 'sample'} and cb['value'] == d['value'] and cb['cores'] >= 1
     assert d['e2e'] == {'value': d['value'], 'unit': d['unit'], 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}
+
+
+import pytest
+
+
+@pytest.mark.gpu
+def test_native_line():
+    """The GPU arm (plain FP64 path only): roofline, cpu_baseline, e2e with
+    the bytes actually copied, launch count and clocks."""
+    out = subprocess.run([sys.executable, os.path.join(ROOT, 'bench.py'), '--steps', '3', '--warmup', '3',
+                          '--no-forms', '--cpu-budget', '2'], cwd=ROOT, capture_output=True, text=True, timeout=900)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith('{')]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d['value'] > 0 and d['dtype'] == 'f64' and d['n_gpus'] == 1 and d['config']['final_rel'] <= 1e-10
+    r = d['roofline']
+    assert r['bound'] == 'hbm' and r['unit'] == 'GB/s' and 0 < r['frac'] < 1.5
+    assert abs(r['frac'] - r['achieved'] / r['peak']) < 1e-9 and r['traffic'] and r['traffic'] > 0
+    assert 0 < r['fp64_pipe']['frac'] < 1.5
+    e = d['e2e']
+    assert e['unit'] == 'solves/s' and e['h2d_bytes_per_step'] > 0 and e['d2h_bytes_per_step'] > 0
+    assert d['gpu_launches'] > 1000
+    assert d['cpu_baseline']['kind'] == 'port' and d['cpu_baseline']['value'] > 0
+    assert {'sm_mhz', 'sm_max_mhz', 'reasons'} <= set(d['clocks'])
