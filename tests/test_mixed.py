@@ -29,10 +29,10 @@ def _opts(tag, precision, levels=3):
                      'RelTol', 1e-10, 'Precision', precision)
 
 
-def _solve_mixed_and_oracle(prob, tag, levels=3, mass=True):
+def _solve_mixed_and_oracle(prob, tag, levels=3, mass=True, tree=False):
     o64 = _opts(tag, 'fp64', levels)
     o64['MassCorrection'] = mass
-    H = build_hierarchy(prob, o64, OracleBackend())
+    H = build_hierarchy(prob, o64, OracleBackend(), tree=tree)
     fl = flatten(H)
     oh = OracleHier(fl, o64)
     it_o, hist_o, rel_o, _ = oh.solve_cycles(o64.MaxVCycles + 2)
@@ -46,12 +46,12 @@ def _solve_mixed_and_oracle(prob, tag, levels=3, mass=True):
 
 
 @pytest.mark.parametrize('case', ['config1-circle', 'config1-band', 'vardc-band', 'vardc-band-nomass',
-                                  'neumann-circle'])
+                                  'neumann-circle', 'vardc-band-tree', 'config1-circle-tree'])
 def test_mixed_matches_fp64_oracle(case):
     prob = {'config1': config1_problem, 'vardc': vardc_problem, 'neumann': pureneumann_problem}[case.split('-')[0]]()
     tag = BAND if 'band' in case else CIRCLE
     levels = 2 if case.startswith('neumann') else 3
-    fl, o, m = _solve_mixed_and_oracle(prob, tag, levels, mass='nomass' not in case)
+    fl, o, m = _solve_mixed_and_oracle(prob, tag, levels, mass='nomass' not in case, tree=case.endswith('-tree'))
     assert m[2] <= 1e-10, m[2]
     # the defect correction converges like the FP64 V-cycle
     assert m[0] <= o[0] + 2, (m[0], o[0])
