@@ -229,6 +229,27 @@ Decomp decomp(bsam_hier h, const DecompH &D) {
 
 inline int nblk(int n) { return (n + kBlock - 1) / kBlock; }
 
+// kernels whose kBlock grid has fewer blocks than this run with 64-thread
+// (or one-chunk) blocks: an SM issues about two FP64 operations per clock,
+// so spreading a level's FP64 work over more SMs shortens the launch.  A
+// batch keeps the larger blocks beyond two per SM: in its last V-cycles most
+// instances are frozen and every extra block is scheduled for nothing.
+int sm_count();
+int spread_limit(bsam_hier h) { return (h->ninst > 1 ? 2 : 4) * sm_count(); }
+
+// multiprocessors of the current device (queried once)
+int sm_count() {
+  static std::once_flag once;
+  static int n = 152;
+  std::call_once(once, [] {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+      n = v;
+    cudaGetLastError();
+  });
+  return n;
+}
+
 // Every kernel goes out with programmatic stream serialization: the next
 // kernel is scheduled while the previous one drains and waits for it at its
 // griddepcontrol.wait (kernels.cuh chain_in).
@@ -329,8 +350,12 @@ void launch_fill(bsam_hier h, int k, int need = 0) {
   if (!L.g1_n) return;
   FieldsT<T> f = fields_t<T>(h);
   Launch l(h, K_GHOST, 0, k);
-  launch_k(h, k_ghost<T>, nblk(L.g1_n), kBlock, ghost_items(h), L.g1_off, L.g1_n, f.Q, f.QC, f.bcg, L.hx, L.hy,
-           (const int *)h->active.p, (const int *)h->inst_nlev.p, need);
+  if (nblk(L.g1_n) < spread_limit(h))
+    launch_k(h, k_ghost<T, 64>, (L.g1_n + 63) / 64, 64, ghost_items(h), L.g1_off, L.g1_n, f.Q, f.QC, f.bcg, L.hx,
+             L.hy, (const int *)h->active.p, (const int *)h->inst_nlev.p, need);
+  else
+    launch_k(h, k_ghost<T>, nblk(L.g1_n), kBlock, ghost_items(h), L.g1_off, L.g1_n, f.Q, f.QC, f.bcg, L.hx, L.hy,
+             (const int *)h->active.p, (const int *)h->inst_nlev.p, need);
 }
 
 // can the device co-schedule one cluster of `ctas` CTAs of kClusterBlock
@@ -467,6 +492,15 @@ void launch_relax(bsam_hier h, int k, int nsweeps, bool first_fresh = false) {
         }
         continue;
       }
+      if (grid < spread_limit(h)) {   // one chunk per block: the FP64 work over more SMs
+        if (L.pow2)
+          launch_k(h, k_relax<T, true, kChunk>, L.rc_n, kChunk, ld, ch, L.rc_n, f, pk, (const Rule *)h->perim.p, m,
+                   (T)h->opts.omega, unit, fresh, ca, am);
+        else
+          launch_k(h, k_relax<T, false, kChunk>, L.rc_n, kChunk, ld, ch, L.rc_n, f, pk, (const Rule *)h->perim.p, m,
+                   (T)h->opts.omega, unit, fresh, ca, am);
+        continue;
+      }
       if (L.pow2)
         launch_k(h, k_relax<T, true>, grid, kBlock, ld, ch, L.rc_n, f, pk, (const Rule *)h->perim.p, m,
                  (T)h->opts.omega, unit, fresh, ca, am);
@@ -495,10 +529,16 @@ void launch_coarse_load(bsam_hier h, int k) {
   const LevelPlan &L = h->lev[k];
   Decomp D = decomp(h, L.coarse);
   const int ntgt = h->opts.mass_correction ? L.ct_n : 0;
-  const int grid = nblk(L.ring_n) + D.nblocks + nblk(ntgt);
   Launch l(h, K_LOAD, 50.0 * tscale<T>() * (double)L.ncells, k);
-  launch_k(h, k_load<T>, grid, kBlock, leveld(h, k), leveld(h, k - 1), D, fields_t<T>(h), (const int *)h->ring.p,
-           (const int *)(h->ninst > 1 ? h->ring_inst.p : nullptr), L.ring_off, L.ring_n, corr_csr(h, L), ntgt);
+  const int *ri = (const int *)(h->ninst > 1 ? h->ring_inst.p : nullptr);
+  if (D.nblocks < spread_limit(h)) {   // spread the footprint's FP64 work over more SMs
+    auto nb = [](int n) { return (n + 63) / 64; };
+    launch_k(h, k_load<T, 64>, nb(L.ring_n) + nb(D.n) + nb(ntgt), 64, leveld(h, k), leveld(h, k - 1), D,
+             fields_t<T>(h), (const int *)h->ring.p, ri, L.ring_off, L.ring_n, corr_csr(h, L), ntgt);
+  } else {
+    launch_k(h, k_load<T>, nblk(L.ring_n) + D.nblocks + nblk(ntgt), kBlock, leveld(h, k), leveld(h, k - 1), D,
+             fields_t<T>(h), (const int *)h->ring.p, ri, L.ring_off, L.ring_n, corr_csr(h, L), ntgt);
+  }
 }
 
 template <class T = double>
@@ -506,7 +546,10 @@ void launch_prolong(bsam_hier h, int k, int correct) {
   const LevelPlan &L = h->lev[k];
   Decomp D = decomp(h, L.coarse);
   Launch l(h, K_PROLONG, 20.0 * tscale<T>() * (double)L.ncells, k);
-  launch_k(h, k_prolong<T>, D.nblocks, kBlock, leveld(h, k), D, fields_t<T>(h), correct);
+  if (D.nblocks < spread_limit(h))
+    launch_k(h, k_prolong<T, 64>, (D.n + 63) / 64, 64, leveld(h, k), D, fields_t<T>(h), correct);
+  else
+    launch_k(h, k_prolong<T>, D.nblocks, kBlock, leveld(h, k), D, fields_t<T>(h), correct);
 }
 
 // the FP32 correction cycle solves a homogeneous problem: no boundary rhs
@@ -515,8 +558,9 @@ void launch_coarsest(bsam_hier h) {
   {
     Launch l(h, K_COARSEST, 8.0 * (double)h->Ainv.n, 1);
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)nblk(h->coarse_max_rows * 32), (unsigned)h->ncoarse_patches);
-    cfg.blockDim = dim3(kBlock);
+    const int rows = h->ninst > 1 ? 8 : 1;
+    cfg.gridDim = dim3((unsigned)((h->coarse_max_rows + rows - 1) / rows), (unsigned)h->ncoarse_patches);
+    cfg.blockDim = dim3(32 * rows);
     cfg.stream = h->stream;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -524,8 +568,12 @@ void launch_coarsest(bsam_hier h) {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     const double *rhs = sizeof(T) == sizeof(double) ? (const double *)h->bcRhs.p : nullptr;
-    cudaLaunchKernelEx(&cfg, k_coarsest<T>, (const double *)h->Ainv.p, rhs, (const CoarsestD *)h->coarsest.p,
-                       fields_t<T>(h));
+    if (rows == 1)
+      cudaLaunchKernelEx(&cfg, k_coarsest<T, 1>, (const double *)h->Ainv.p, rhs, (const CoarsestD *)h->coarsest.p,
+                         fields_t<T>(h));
+    else
+      cudaLaunchKernelEx(&cfg, k_coarsest<T, 8>, (const double *)h->Ainv.p, rhs, (const CoarsestD *)h->coarsest.p,
+                         fields_t<T>(h));
   }
   launch_fill<T>(h, 1);
 }

@@ -175,13 +175,15 @@ __device__ __forceinline__ void ghost_item(const GhostItems &G, int i, int8_t ty
   }
 }
 
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_ghost(GhostItems G, int off, int n, T *__restrict__ Q, T *__restrict__ QC,
-                                                  const T *__restrict__ bcg, double hx_, double hy_,
-                                                  const int *__restrict__ active,
-                                                  const int *__restrict__ inst_nlev, int need) {
+// kT threads per block: kBlock, or 64 on a level whose kBlock grid leaves
+// SMs idle
+template <class T, int kT = kBlock>
+__global__ void __launch_bounds__(kT) k_ghost(GhostItems G, int off, int n, T *__restrict__ Q, T *__restrict__ QC,
+                                              const T *__restrict__ bcg, double hx_, double hy_,
+                                              const int *__restrict__ active, const int *__restrict__ inst_nlev,
+                                              int need) {
   chain_trigger();
-  const int t = blockIdx.x * kBlock + threadIdx.x;
+  const int t = blockIdx.x * kT + threadIdx.x;
   const int i = off + t;
   // a converged instance of a batch stays frozen; a fill that follows the
   // restriction from level `need` skips the instances without that level
@@ -602,14 +604,18 @@ __global__ void __launch_bounds__(kBlock) k_relax_n(LevelD L, const RelaxChunkD 
   }
 }
 
-template <class T, bool kPow2>
-__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 8 : 5) k_relax(LevelD L, const RelaxChunkD *__restrict__ chunks, int nchunks,
-                                                  FieldsT<T> f, const T *__restrict__ pack,
-                                                  const Rule *__restrict__ perim, int m, T omega, int unit_omega,
-                                                  int fresh, const uint8_t *__restrict__ cact, int amode) {
+// kT threads per block: kBlock, or kChunk (one chunk per block) on a level
+// whose kBlock grid would leave SMs idle -- an SM issues about two FP64
+// operations per clock, so a block's FP64 work is spread over more SMs
+// (same arithmetic, same register budget per thread)
+template <class T, bool kPow2, int kT = kBlock>
+__global__ void __launch_bounds__(kT, (sizeof(T) == 4 ? 8 : 5) * (kBlock / kT))
+    k_relax(LevelD L, const RelaxChunkD *__restrict__ chunks, int nchunks, FieldsT<T> f, const T *__restrict__ pack,
+            const Rule *__restrict__ perim, int m, T omega, int unit_omega, int fresh,
+            const uint8_t *__restrict__ cact, int amode) {
   chain_trigger();
   relax_cell<T, kPow2, true>(L, chunks, nchunks, f, pack, perim, m, omega, unit_omega, fresh, cact, amode,
-                             blockIdx.x * (kBlock / kChunk) + threadIdx.x / kChunk, threadIdx.x & (kChunk - 1));
+                             blockIdx.x * (kT / kChunk) + threadIdx.x / kChunk, threadIdx.x & (kChunk - 1));
 }
 
 // A small level's whole relaxation in one launch: one thread-block cluster
@@ -781,15 +787,19 @@ __device__ __forceinline__ double op_pre(double q, double qe, double qw, double 
   return (divr(-(feE - feW), L.hx2, L.ihx2, L.pow2) - divr(fnN - fnS, L.hy2, L.ihy2, L.pow2)) + cc * q;
 }
 
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, FieldsT<T> f, const int *__restrict__ ring,
-                                                 const int *__restrict__ ring_inst, int ring_off, int n_ring, CorrCSR C,
-                                                 int n_tgt) {
+// kT threads per block (kBlock, or 64 on a level whose kBlock grid leaves
+// SMs idle: a footprint cell is ~84 FP64 operations, and an SM issues about
+// two per clock); the decomposition's per-block patch table is kBlock-based
+template <class T, int kT = kBlock>
+__global__ void __launch_bounds__(kT) k_load(LevelD L, LevelD Lc, Decomp D, FieldsT<T> f, const int *__restrict__ ring,
+                                             const int *__restrict__ ring_inst, int ring_off, int n_ring, CorrCSR C,
+                                             int n_tgt) {
   chain_trigger();
-  const int nb_ring = (n_ring + kBlock - 1) / kBlock;
+  const int nb_ring = (n_ring + kT - 1) / kT;
+  const int nb_fp = (D.n + kT - 1) / kT;
   int b = blockIdx.x;
   if (b < nb_ring) {
-    const int t = b * kBlock + threadIdx.x;
+    const int t = b * kT + threadIdx.x;
     int src = 0, dst = 0;
     bool on = t < n_ring && (!ring_inst || f.active[__ldg(ring_inst + ring_off + t)]);
     if (on) {
@@ -801,13 +811,13 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
     return;
   }
   b -= nb_ring;
-  if (b < D.nblocks) {
-    const int g = b * kBlock + threadIdx.x;
+  if (b < nb_fp) {
+    const int g = b * kT + threadIdx.x;
     if (g >= D.n) {
       chain_wait();
       return;
     }
-    const int p = find_patch(D, b, g);
+    const int p = find_patch(D, g / kBlock, g);
     const PatchD &P = L.patches[p];
     if (!f.active[P.inst]) {
       chain_wait();
@@ -867,8 +877,8 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
     f.F[dst] = T(rr + lc);
     return;
   }
-  b -= D.nblocks;
-  const int t = b * kBlock + threadIdx.x;
+  b -= nb_fp;
+  const int t = b * kT + threadIdx.x;
   const bool on = t < n_tgt && f.active[Lc.patches[C.patch[t]].inst];
   const int cell = on ? C.cell[t] : 0;
   chain_wait();
@@ -881,15 +891,17 @@ __global__ void __launch_bounds__(kBlock) k_load(LevelD L, LevelD Lc, Decomp D, 
 // (ebTransfer.m:57-71) adds P(W - QC) to the interior; mode 0 writes P(W)
 // (new-level initial guess, ebAddLevel.m:26-31).  One thread per coarse cell
 // writes its four fine cells.
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_prolong(LevelD L, Decomp D, FieldsT<T> f, int correct) {
+// kT threads per block: kBlock, or 64 on a level whose kBlock grid leaves
+// SMs idle (about 37 FP64 operations per coarse cell, two per clock per SM)
+template <class T, int kT = kBlock>
+__global__ void __launch_bounds__(kT) k_prolong(LevelD L, Decomp D, FieldsT<T> f, int correct) {
   chain_trigger();
-  const int g = blockIdx.x * kBlock + threadIdx.x;
+  const int g = blockIdx.x * kT + threadIdx.x;
   if (g >= D.n) {
     chain_wait();
     return;
   }
-  const int p = find_patch(D, blockIdx.x, g);
+  const int p = find_patch(D, g / kBlock, g);
   const PatchD &P = L.patches[p];
   if (!f.active[P.inst]) {   // frozen instance, or an instance whose level k is not new
     chain_wait();
@@ -947,13 +959,18 @@ struct CoarsestD {
 
 // bcRhs null: a homogeneous problem (the correction cycle of the mixed
 // form), whose F is FP32 while the solve itself stays FP64.
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_coarsest(const double *__restrict__ Ainv, const double *__restrict__ bcRhs,
-                                                     const CoarsestD *__restrict__ cd, FieldsT<T> f) {
+// one warp per row, kRows rows per block: one row per block spreads a single
+// hierarchy's rows' FP64 work over as many SMs as there are rows; a batch
+// keeps eight, since most of its instances' blocks exit at once in its last
+// V-cycles
+template <class T, int kRows = 1>
+__global__ void __launch_bounds__(32 * kRows) k_coarsest(const double *__restrict__ Ainv,
+                                                         const double *__restrict__ bcRhs,
+                                                         const CoarsestD *__restrict__ cd, FieldsT<T> f) {
   chain_trigger();
   const CoarsestD D = cd[blockIdx.y];
   const int N = D.N;
-  const int row = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+  const int row = blockIdx.x * kRows + (int)(threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (row >= N || !f.active[D.inst]) {
     chain_wait();
