@@ -235,7 +235,7 @@ inline int nblk(int n) { return (n + kBlock - 1) / kBlock; }
 // batch keeps the larger blocks beyond two per SM: in its last V-cycles most
 // instances are frozen and every extra block is scheduled for nothing.
 int sm_count();
-int spread_limit(bsam_hier h) { return (h->ninst > 1 ? 2 : 4) * sm_count(); }
+int spread_limit(bsam_hier h) { return (h->ninst > 1 ? 2 : 8) * sm_count(); }
 
 // multiprocessors of the current device (queried once)
 int sm_count() {
@@ -619,9 +619,15 @@ void launch_residual(bsam_hier h, int mode) {
   for (int k = 1; k <= h->nlev; ++k) bytes += 41.0 * (double)h->lev[k].ncells;
   {
     Launch l(h, K_RESID, bytes);
-    launch_k(h, k_residual, (h->nrtasks + kBlock / 32 - 1) / (kBlock / 32), kBlock, (const LevelX *)h->levelx.p,
-             (const PatchD *)h->patches.p, (const ResTask *)h->rtasks.p, h->nrtasks, fields(h), (const int *)h->ring.p,
-             h->slots.p, h->nslots, h->opts.mass_correction, mixed(h) ? h->F32.p : (float *)nullptr);
+    const int g256 = (h->nrtasks + kBlock / 32 - 1) / (kBlock / 32);
+    if (g256 < spread_limit(h))
+      launch_k(h, k_residual<64>, (h->nrtasks + 1) / 2, 64, (const LevelX *)h->levelx.p, (const PatchD *)h->patches.p,
+               (const ResTask *)h->rtasks.p, h->nrtasks, fields(h), (const int *)h->ring.p, h->slots.p, h->nslots,
+               h->opts.mass_correction, mixed(h) ? h->F32.p : (float *)nullptr);
+    else
+      launch_k(h, k_residual<>, g256, kBlock, (const LevelX *)h->levelx.p, (const PatchD *)h->patches.p,
+               (const ResTask *)h->rtasks.p, h->nrtasks, fields(h), (const int *)h->ring.p, h->slots.p, h->nslots,
+               h->opts.mass_correction, mixed(h) ? h->F32.p : (float *)nullptr);
   }
   Launch l(h, K_RESID, 0);
   launch_k(h, k_residual_final, h->ninst, kFinal, (const InstRes *)h->instres.p, (const SlotRange *)h->sranges.p,

@@ -1050,12 +1050,15 @@ __device__ __forceinline__ double pmax(double a, double b) {
 // items of one patch or one instance's targets)
 constexpr int kResLane = 4;
 
-__global__ void __launch_bounds__(kBlock) k_residual(const LevelX *__restrict__ X, const PatchD *__restrict__ patches,
-                                                     const ResTask *__restrict__ tasks, int ntask, Fields f,
-                                                     const int *__restrict__ ring, double *slots, int nslots,
-                                                     int mass_corr, float *__restrict__ rout) {
+// kT threads per block (kBlock, or 64 where the kBlock grid would leave
+// SMs with unequal shares of the FP64 work)
+template <int kT = kBlock>
+__global__ void __launch_bounds__(kT) k_residual(const LevelX *__restrict__ X, const PatchD *__restrict__ patches,
+                                                 const ResTask *__restrict__ tasks, int ntask, Fields f,
+                                                 const int *__restrict__ ring, double *slots, int nslots,
+                                                 int mass_corr, float *__restrict__ rout) {
   chain_trigger();
-  const int w = blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
+  const int w = blockIdx.x * (kT / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   // a frozen instance's residual is neither reported nor needed (its QC
   // refresh would rewrite the same values), so its warps only wait
