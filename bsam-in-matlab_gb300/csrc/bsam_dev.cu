@@ -516,7 +516,10 @@ void launch_restrict(bsam_hier h, int k, int to_parent) {
   const LevelPlan &L = h->lev[k];
   Decomp D = decomp(h, L.coarse);
   Launch l(h, K_RESTRICT, 12.0 * tscale<T>() * (double)L.ncells, k);
-  launch_k(h, k_restrict<T>, D.nblocks, kBlock, leveld(h, k), D, fields_t<T>(h), to_parent);
+  if (D.nblocks < spread_limit(h))
+    launch_k(h, k_restrict<T, 64>, (D.n + 63) / 64, 64, leveld(h, k), D, fields_t<T>(h), to_parent);
+  else
+    launch_k(h, k_restrict<T>, D.nblocks, kBlock, leveld(h, k), D, fields_t<T>(h), to_parent);
 }
 
 CorrCSR corr_csr(bsam_hier h, const LevelPlan &L) {

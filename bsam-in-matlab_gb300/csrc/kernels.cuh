@@ -668,15 +668,17 @@ __device__ __forceinline__ T restrict_cell(const T *Q, int ldq, int ci, int cj) 
   return T(0.25) * (((Q[c] + Q[c + 1]) + Q[c + ldq]) + Q[c + ldq + 1]);
 }
 
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_restrict(LevelD L, Decomp D, FieldsT<T> f, int to_parent) {
+// kT threads per block: kBlock, or 64 on a level whose kBlock grid leaves
+// SMs idle
+template <class T, int kT = kBlock>
+__global__ void __launch_bounds__(kT) k_restrict(LevelD L, Decomp D, FieldsT<T> f, int to_parent) {
   chain_trigger();
-  const int g = blockIdx.x * kBlock + threadIdx.x;
+  const int g = blockIdx.x * kT + threadIdx.x;
   if (g >= D.n) {
     chain_wait();
     return;
   }
-  const int p = find_patch(D, blockIdx.x, g);
+  const int p = find_patch(D, g / kBlock, g);
   const PatchD &P = L.patches[p];
   if (!f.active[P.inst]) {
     chain_wait();
