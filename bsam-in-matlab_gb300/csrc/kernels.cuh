@@ -1168,6 +1168,7 @@ struct SlotRange {
 // ebSolveCycles.m:17-46: an instance stays active while it < MaxVCycles and
 // rel > RelTol.
 constexpr int kFinal = 512;
+constexpr int kFinalGroup = 8;   // levels whose L2 trees share barrier steps
 __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__restrict__ ir,
                                                           const SlotRange *__restrict__ ranges, const double *slots,
                                                           int nslots, ResAcc *acc, int *active, int *iters,
@@ -1209,27 +1210,35 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__rest
   const double linf = s_a[0];
   double fnorm = s_b[0];
   __syncthreads();
+  // L2: per level (range) a fixed-order tree over the threads' partial
+  // sums; the levels of a group are loaded together and reduced in the same
+  // barrier steps (each level's pairings unchanged), then summed in level
+  // order with their areas
+  __shared__ double s_p[kFinalGroup][kFinal];
   double l2sq = 0;
-  for (int r = R.range0; r < R.range1; ++r) {
-    // fixed order: four strided partial sums per thread, then their sum
-    const int s0 = ranges[r].s0, s1 = ranges[r].s1;
-    double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
-    int i = s0 + t;
-    for (; i + 3 * kFinal < s1; i += 4 * kFinal) {
-      p0 = p0 + slots[nslots + i];
-      p1 = p1 + slots[nslots + i + kFinal];
-      p2 = p2 + slots[nslots + i + 2 * kFinal];
-      p3 = p3 + slots[nslots + i + 3 * kFinal];
+  for (int r0 = R.range0; r0 < R.range1; r0 += kFinalGroup) {
+    const int nr = min(kFinalGroup, R.range1 - r0);
+    for (int q = 0; q < nr; ++q) {
+      // fixed order: four strided partial sums per thread, then their sum
+      const int s0 = ranges[r0 + q].s0, s1 = ranges[r0 + q].s1;
+      double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+      int i = s0 + t;
+      for (; i + 3 * kFinal < s1; i += 4 * kFinal) {
+        p0 = p0 + slots[nslots + i];
+        p1 = p1 + slots[nslots + i + kFinal];
+        p2 = p2 + slots[nslots + i + 2 * kFinal];
+        p3 = p3 + slots[nslots + i + 3 * kFinal];
+      }
+      for (; i < s1; i += kFinal) p0 = p0 + slots[nslots + i];
+      s_p[q][t] = (p0 + p1) + (p2 + p3);
     }
-    for (; i < s1; i += kFinal) p0 = p0 + slots[nslots + i];
-    const double sum = (p0 + p1) + (p2 + p3);
-    s_a[t] = sum;
     __syncthreads();
     for (int off = kFinal / 2; off >= 1; off >>= 1) {
-      if (t < off) s_a[t] = s_a[t] + s_a[t + off];
+      if (t < off)
+        for (int q = 0; q < nr; ++q) s_p[q][t] = s_p[q][t] + s_p[q][t + off];
       __syncthreads();
     }
-    l2sq = l2sq + s_a[0] * ranges[r].area;
+    for (int q = 0; q < nr; ++q) l2sq = l2sq + s_p[q][0] * ranges[r0 + q].area;
     __syncthreads();
   }
   if (t == 0) {
