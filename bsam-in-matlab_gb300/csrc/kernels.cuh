@@ -1197,19 +1197,33 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__rest
       fn = pmax(fn, slots[2 * nslots + i]);
     }
   }
-  s_a[t] = li;
-  s_b[t] = fn;
-  __syncthreads();
-  for (int off = kFinal / 2; off >= 1; off >>= 1) {
-    if (t < off) {
-      s_a[t] = pmax(s_a[t], s_a[t + off]);
-      s_b[t] = pmax(s_b[t], s_b[t + off]);
-    }
-    __syncthreads();
+  // a max is order-free: warp shuffles, then one shared stage
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) {
+    li = pmax(li, __shfl_xor_sync(0xffffffffu, li, off));
+    fn = pmax(fn, __shfl_xor_sync(0xffffffffu, fn, off));
   }
-  const double linf = s_a[0];
-  double fnorm = s_b[0];
+  if ((t & 31) == 0) {
+    s_a[t >> 5] = li;
+    s_b[t >> 5] = fn;
+  }
   __syncthreads();
+  if (t < 32) {
+    li = t < kFinal / 32 ? s_a[t] : 0.0;
+    fn = t < kFinal / 32 ? s_b[t] : 0.0;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+      li = pmax(li, __shfl_xor_sync(0xffffffffu, li, off));
+      fn = pmax(fn, __shfl_xor_sync(0xffffffffu, fn, off));
+    }
+    if (t == 0) {
+      s_a[kFinal / 32] = li;
+      s_b[kFinal / 32] = fn;
+    }
+  }
+  __syncthreads();
+  const double linf = s_a[kFinal / 32];
+  double fnorm = s_b[kFinal / 32];
   // L2: per level (range) a fixed-order tree over the threads' partial
   // sums; the levels of a group are loaded together and reduced in the same
   // barrier steps (each level's pairings unchanged), then summed in level
