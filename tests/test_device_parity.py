@@ -105,3 +105,22 @@ def test_device_tag_mask_equals_host(indicator, tree):
         assert host.shape[0] > 0
         H = hier.add_level(H, host, be)
         H = ebSolveCycles(H, be)
+
+
+@pytest.mark.parametrize('tree', [False, True])
+def test_non_power_of_two_spacing_bitwise(tree):
+    """A [0,3] x [0,1.5] domain: no cell size is a power of two, so every
+    kernel divides by h^2 as the reference does (the exact-reciprocal
+    products of power-of-two levels do not apply); solved on both paths."""
+    from bsam import ebProblem
+    D = lambda x, y: 1 + 0.2 * x * y
+    f = lambda x, y: np.sin(2 * x) * np.cos(3 * y) + 0.5
+    prob = ebProblem([0, 3, 0, 1.5], D, 1, f, ('dirichlet', 0))
+    opts = ebOptions('BaseCells', 32, 'MaxLevels', 3, 'Indicator', 'fun',
+                     'TagFunction', lambda x, y: np.abs(x - 2 * y) < 0.3, 'Verbose', 0, 'RelTol', 1e-10)
+    H = build_hierarchy(prob, opts, OracleBackend(), tree=tree)
+    fl = flatten(H)
+    for hx, hy in np.asarray(fl.hs).reshape(-1, 2):
+        assert np.frexp(hx * hx)[0] != 0.5 or np.frexp(hy * hy)[0] != 0.5
+    o, d = _both(prob, opts, tree)
+    _assert_bitwise(o, d)
