@@ -68,6 +68,19 @@ def test_mixed_matches_fp64_oracle(case):
     assert l2 <= TOL and mx <= TOL, (l2, mx)
 
 
+def test_mixed_non_power_of_two_spacing():
+    """[0,3] x [0,1.5]: the FP32 correction cycle divides by h^2 in FP32;
+    the mixed solve still reaches the FP64 stop test within the tolerance."""
+    from bsam import ebProblem
+    D = lambda x, y: 1 + 0.2 * x * y
+    f = lambda x, y: np.sin(2 * x) * np.cos(3 * y) + 0.5
+    prob = ebProblem([0, 3, 0, 1.5], D, 1, f, ('dirichlet', 0))
+    fl, o, m = _solve_mixed_and_oracle(prob, lambda x, y: np.abs(x - 2 * y) < 0.3)
+    assert m[2] <= 1e-10 and m[0] <= o[0] + 2, (m[0], o[0], m[2])
+    l2, mx = rel_errors(m[3], o[3], visible_q_index(fl))
+    assert l2 <= TOL and mx <= TOL, (l2, mx)
+
+
 def test_mixed_batch_equals_solo():
     from bsam.device import DeviceBackend, DevHier, BSAM_FIELD_Q
     from bsam.batch import merge_flats, split_field
