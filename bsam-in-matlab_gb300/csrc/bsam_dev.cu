@@ -163,7 +163,7 @@ struct bsam_hier_s {
   DBuf<RelaxChunkD> rchunks;       // relax chunk records as the kernels read them, all levels
   DBuf<uint8_t> cact;              // per chunk: its instance still iterates (batches, kActChunk)
   DBuf<int> crange;                // per instance and level: its chunk range [begin, end)
-  int act_mode = 0;                // kActNone / kActChunk / kActInst
+  int act_mode = 0;                // kActNone (one instance) / kActChunk (batch)
   DBuf<LevelX> levelx;             // per-level descriptors for the residual
   DBuf<ResTask> rtasks;            // residual warp tasks
   DBuf<InstRes> instres;           // per-instance residual reduction plan
@@ -1247,6 +1247,13 @@ int validate(const bsam_hier_desc *d) {
       if (d->inst_root[i] < 1 || d->inst_root[i] > d->nlev) return fail(BSAM_ERR_ARG, "instance root out of range");
       if (d->patch_inst[i] != i) return fail(BSAM_ERR_ARG, "level-1 patches must be in instance order");
     }
+    // each level holds its patches instance by instance
+    for (int k = 1; k <= d->nlev; ++k) {
+      const int32_t *L = d->levels + (size_t)(k - 1) * LDN;
+      for (int p = L[LD_P0] + 1; p < L[LD_P1]; ++p)
+        if (d->patch_inst[p] < d->patch_inst[p - 1])
+          return fail(BSAM_ERR_ARG, "batch patches of a level must be grouped by instance, in instance order");
+    }
   }
   for (int p = 0; p < d->npatch; ++p) {
     const int32_t *r = d->patches + (size_t)p * PDN;
@@ -1427,9 +1434,9 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
   if ((rc = h->perim.upload(B.perim.data(), B.perim.size(), s)) ||
       (rc = h->rchunks.upload(dchunks.data(), dchunks.size(), s)))
     return rc;
-  // frozen-chunk flags of a batch: each instance's chunks must form one
-  // range per level (instances stored one after another within a level),
-  // else the smoother reads the instance flag through the chunk record
+  // frozen-chunk flags of a batch: each instance's chunks form one range per
+  // level (instances stored one after another within a level, checked in
+  // validate)
   h->act_mode = h->ninst > 1 ? kActChunk : kActNone;
   if (h->ninst > 1) {
     const int nl = d->nlev;
@@ -1444,8 +1451,9 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
       }
     }
     for (size_t e = 0; e < cnt.size(); ++e)
-      if (cnt[e] && cnt[e] != cr[2 * e + 1] - cr[2 * e]) h->act_mode = kActInst;
-    if (h->act_mode == kActChunk) {
+      if (cnt[e] && cnt[e] != cr[2 * e + 1] - cr[2 * e])
+        return fail(BSAM_ERR_ARG, "batch chunks of an instance are not one range per level");
+    {
       if ((rc = h->crange.upload(cr.data(), cr.size(), s)) || (rc = h->cact.alloc(std::max<size_t>(B.chunks.size(), 1))))
         return rc;
       CK(cudaMemsetAsync(h->cact.p, 1, h->cact.n, s));

@@ -232,9 +232,9 @@ struct __align__(16) RelaxChunkD {
 
 // how a smoother chunk learns that its instance is frozen: kActNone, one
 // instance (always live while a V-cycle runs); kActChunk, the per-chunk flag
-// array k_residual_final keeps (instances' chunks contiguous per level);
-// kActInst, the instance's flag through the chunk record
-enum { kActNone = 0, kActChunk = 1, kActInst = 2 };
+// array k_residual_final keeps (a batch's instances' chunks are contiguous
+// per level)
+enum { kActNone = 0, kActChunk = 1 };
 
 __device__ __forceinline__ int chunk_bc(int flags, int side) { return (flags >> (2 * side)) & 3; }
 __device__ __forceinline__ int chunk_par0(int flags) { return (flags >> 8) & 1; }
@@ -352,7 +352,7 @@ __device__ __forceinline__ void cell_issue(const RelaxChunkD *__restrict__ chunk
 template <class T>
 __device__ __forceinline__ void cell_derive(const FieldsT<T> &f, const Rule *__restrict__ perim, int m, int fresh,
                                             int amode, int tc, CellState<T> &S) {
-  if (!S.live || tc >= S.R.n || (amode == kActInst && !f.active[S.R.inst])) {
+  if (!S.live || tc >= S.R.n) {
     S.live = false;
     return;
   }
@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(kBlock) k_relax_n(LevelD L, const RelaxChunkD 
       idg[u] = __ldg(pk + 4 * kChunk);
     }
   }
-  if (!live || t0 >= R.n || (amode == kActInst && !f.active[R.inst])) {
+  if (!live || t0 >= R.n) {
     chain_wait();
     return;
   }

@@ -87,7 +87,8 @@ typedef struct {
   int32_t ncoarse, singular;  /* coarsest unknowns (all instances), singular flag */
   /* A batch of independent instances (ninst >= 2) solved together: every
    * level k holds the level-k patches of every instance (instance by
-   * instance, all instances sharing the level's cell size); patch_inst
+   * instance, in instance order -- checked at upload -- all instances
+   * sharing the level's cell size); patch_inst
    * [npatch] gives each patch's 0-based instance, inst_root [ninst] each
    * instance's root level, and level 1 holds one patch per instance whose
    * inverse blocks are concatenated in Ainv / bcRhs in instance order.

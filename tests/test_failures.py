@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from bsam import ebOptions
-from bsam.flat import flatten, PD_QOFF, PD_RING0, LD_P1
+from bsam.flat import flatten, PD_QOFF, PD_RING0, LD_P0, LD_P1
 from bsam.solve import build_hierarchy
 from bsam_oracle import OracleBackend, OracleHier
 from cases import config1_problem, vardc_problem
@@ -29,7 +29,8 @@ def _upload(fl, opts):
     return DevHier(DeviceBackend.get(0).ctx, fl, opts)
 
 
-@pytest.mark.parametrize('corruption', ['q_offset', 'ring_index', 'level_tiling', 'coarsest_size', 'batch_instance'])
+@pytest.mark.parametrize('corruption', ['q_offset', 'ring_index', 'level_tiling', 'coarsest_size', 'batch_instance',
+                                        'batch_order'])
 def test_malformed_tables_are_rejected(corruption):
     from bsam.device import DeviceError
     from bsam.batch import merge_flats
@@ -45,10 +46,15 @@ def test_malformed_tables_are_rejected(corruption):
         fl.levels[0, LD_P1] += 1                     # levels overlap
     elif corruption == 'coarsest_size':
         fl.bcRhs = fl.bcRhs[:-1]
-    else:
+    elif corruption == 'batch_instance':
         fl = merge_flats([fl, _flat()[0]])
         fl.patch_inst = fl.patch_inst.copy()
         fl.patch_inst[-1] = 7                        # no such instance
+    else:
+        fl = merge_flats([fl, _flat()[0]])
+        fl.patch_inst = fl.patch_inst.copy()
+        p0 = int(fl.levels[fl.nlev - 1, LD_P0])
+        fl.patch_inst[p0] = 1                        # finest level: instance 1 before instance 0
     with pytest.raises(DeviceError) as ei:
         _upload(fl, opts)
     assert 'bsam:device:arg' in str(ei.value) or ei.value.args[0] == 1
