@@ -351,7 +351,7 @@ __device__ __forceinline__ void cell_issue(const RelaxChunkD *__restrict__ chunk
 
 template <class T>
 __device__ __forceinline__ void cell_derive(const FieldsT<T> &f, const Rule *__restrict__ perim, int m, int fresh,
-                                            int amode, int tc, CellState<T> &S) {
+                                            int tc, CellState<T> &S) {
   if (!S.live || tc >= S.R.n) {
     S.live = false;
     return;
@@ -441,7 +441,7 @@ __device__ __forceinline__ void relax_cell(const LevelD &L, const RelaxChunkD *_
                                            const uint8_t *__restrict__ cact, int amode, int ch, int tc) {
   CellState<T> S;
   cell_issue<T>(chunks, nchunks, pack, m, cact, amode, ch, tc, S);
-  cell_derive<T>(f, perim, m, fresh, amode, tc, S);
+  cell_derive<T>(f, perim, m, fresh, tc, S);
   if (kChain) chain_wait();
   cell_update<T, kPow2, kCG>(L, f, perim, omega, unit_omega, S);
 }
@@ -463,13 +463,13 @@ __global__ void __launch_bounds__(kBlock) k_relax_p(LevelD L, const RelaxChunkD 
   int g = blockIdx.x;
   CellState<T> cur, nxt;
   cell_issue<T>(chunks, nchunks, pack, m, cact, amode, g * cpb + sub, tc, cur);
-  cell_derive<T>(f, perim, m, fresh, amode, tc, cur);
+  cell_derive<T>(f, perim, m, fresh, tc, cur);
   chain_wait();
   while (g < ngroups) {
     const int gn = g + (int)gridDim.x;
     cell_issue<T>(chunks, nchunks, pack, m, cact, amode, gn * cpb + sub, tc, nxt);
     cell_update<T, kPow2, false>(L, f, perim, omega, unit_omega, cur);
-    cell_derive<T>(f, perim, m, fresh, amode, tc, nxt);
+    cell_derive<T>(f, perim, m, fresh, tc, nxt);
     cur = nxt;
     g = gn;
   }
