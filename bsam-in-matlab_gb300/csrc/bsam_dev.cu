@@ -1670,7 +1670,7 @@ int bsam_ctx_create(int device, bsam_ctx *out) {
   }
   // this process's device buffers come from the device's default memory
   // pool in stream order; freed blocks stay in the pool for the next
-  // hierarchy instead of going back to the driver at every synchronisation
+  // hierarchy instead of being released to the CUDA driver at every synchronisation
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
     uint64_t keep = UINT64_MAX;
