@@ -1,0 +1,56 @@
+"""Host set-up helpers (CPU): the vectorised box filter that replaces the
+all-pairs patch-box loops returns every box an inclusive rectangle test can
+hit, in order; the memoised coarsest inverse returns the very same bits as a
+fresh inverse."""
+import threading
+
+import numpy as np
+
+from bsam.hierarchy import near_boxes, rect_isect, dense_inverse
+
+
+def test_near_boxes_superset_in_order():
+    rng = np.random.default_rng(5)
+    boxes = []
+    for _ in range(300):
+        i0, j0 = rng.integers(1, 200, 2)
+        boxes.append([i0, i0 + rng.integers(0, 20), j0, j0 + rng.integers(0, 20)])
+    boxes = np.array(boxes, dtype=np.int64)
+    for _ in range(200):
+        i0, j0 = rng.integers(1, 200, 2)
+        r = [int(i0), int(i0 + rng.integers(0, 30)), int(j0), int(j0 + rng.integers(0, 30))]
+        cand = near_boxes(boxes, r)
+        assert cand == sorted(cand)
+        # the cell test and both face tests of the coefficient and window loops
+        for q in range(len(boxes)):
+            qb = [int(v) for v in boxes[q]]
+            hits = (rect_isect(r, qb) is not None or
+                    rect_isect([r[0], r[1] + 1, r[2], r[3]], [qb[0], qb[1] + 1, qb[2], qb[3]]) is not None or
+                    rect_isect([r[0], r[1], r[2], r[3] + 1], [qb[0], qb[1], qb[2], qb[3] + 1]) is not None)
+            if hits:
+                assert q in cand
+        exact = near_boxes(boxes, r, pad=0)
+        assert exact == [q for q in range(len(boxes)) if rect_isect(r, [int(v) for v in boxes[q]]) is not None]
+
+
+def test_dense_inverse_memo_is_bitwise_and_threadsafe():
+    rng = np.random.default_rng(1)
+    mats = [np.eye(40) * 4 + rng.standard_normal((40, 40)) * 0.1 for _ in range(3)]
+    fresh = [np.linalg.inv(a) for a in mats]
+    out = {}
+
+    def work(t):
+        out[t] = [dense_inverse(mats[(t + i) % 3]) for i in range(12)]
+
+    th = [threading.Thread(target=work, args=(t,)) for t in range(4)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    for t, res in out.items():
+        for i, r in enumerate(res):
+            np.testing.assert_array_equal(r, fresh[(t + i) % 3])
+    # a returned inverse is a copy: changing it leaves the cache intact
+    a = dense_inverse(mats[0])
+    a[0, 0] = 1e9
+    np.testing.assert_array_equal(dense_inverse(mats[0]), fresh[0])
