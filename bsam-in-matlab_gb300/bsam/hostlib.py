@@ -44,3 +44,16 @@ def tanh(x): return _v1('tanh', x)
 def cosh(x): return _v1('cosh', x)
 def sin(x): return _v1('sin', x)
 def cos(x): return _v1('cos', x)
+
+
+def _v2(name, a, b):
+    a, b = np.broadcast_arrays(np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64))
+    ac = np.ascontiguousarray(a.ravel(order='F'))
+    bc = np.ascontiguousarray(b.ravel(order='F'))
+    y = np.empty_like(ac)
+    getattr(lib(), 'bsam_v' + name)(ac.ctypes.data, bc.ctypes.data, y.ctypes.data, ac.size)
+    return y.reshape(a.shape, order='F') if a.ndim else float(y[0])
+
+
+def atan2(y, x): return _v2('atan2', y, x)
+def hypot(x, y): return _v2('hypot', x, y)

@@ -122,6 +122,23 @@ for which, tag in ((0, ''), (1, '_tree')):
         if m:
             t8.append({'patches': int(m[1]), 'minw': int(m[2]), 'factor': m[3], 'err': m[4], 'mass': m[5]})
     out['suite_T8_scattered' + tag] = t8
+# Diffuse-domain suite (DiffuseDomainBSAM/tests/runDdTests.m): D1 star /
+# Neumann (uniform, adaptive, adaptive without corrections) and D2 disc /
+# Dirichlet penalty.
+d1 = []
+for line in section('D1', 0):
+    m = re.match(r'\s+eps=([0-9.]+)\s+uni\(L2\)=([0-9.e+-]+)\s+amr\(L2\)=([0-9.e+-]+)\s+noCorr\(L2\)=([0-9.e+-]+)'
+                 r'\s+\| mass: ([0-9.e+-]+) / ([0-9.e+-]+) / ([0-9.e+-]+) \| amr factor ([0-9.]+)', line)
+    if m:
+        d1.append({'eps': float(m[1]), 'uni_l2': m[2], 'amr_l2': m[3], 'nocorr_l2': m[4], 'mass_uni': m[5],
+                   'mass_amr': m[6], 'mass_nocorr': m[7], 'amr_factor': m[8]})
+out['suite_D1_star_neumann'] = d1
+d2 = []
+for line in section('D2', 0):
+    m = re.match(r'\s+eps=([0-9.]+)\s+L2=([0-9.e+-]+)\s+Linf=([0-9.e+-]+)\s+factor=([0-9.]+)\s+dof=(\d+)', line)
+    if m:
+        d2.append({'eps': float(m[1]), 'l2': m[2], 'linf': m[3], 'factor': m[4], 'dof': int(m[5])})
+out['suite_D2_disc_dirichlet'] = d2
 out['source'] = {'repository': 'BSAM-in-MATLAB', 'files': ['verification/starfish-full-residual.csv',
                                                           'verification/starfish-full.json',
                                                           'verification/readme-examples.txt',
