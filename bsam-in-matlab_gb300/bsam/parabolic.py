@@ -91,8 +91,10 @@ def ebpOptions(*args, **kwargs) -> Options:
         raise ValueError('ebp_options:scheme: Scheme must be be, bdf2 or cn.')
     if opts.Dt is None or opts.TFinal is None:
         raise ValueError('ebp_options:time: Dt and TFinal are required.')
-    if not (opts.Dt > 0 and opts.TFinal > 0):
-        raise ValueError('ebp_options:time: Dt and TFinal must be positive.')
+    for nm in ('Dt', 'TFinal'):
+        v = opts[nm]
+        if not (np.isscalar(v) and np.isreal(v) and np.isfinite(v) and v > 0):
+            raise ValueError(f'ebp_options:time: {nm} must be a positive finite real scalar.')
     eb = ebOptions(*rest)
     eb.Verbose = 0
     eb.MaxVCycles = int(opts.MaxVCyclesStep)

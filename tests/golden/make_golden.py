@@ -139,6 +139,54 @@ for line in section('D2', 0):
     if m:
         d2.append({'eps': float(m[1]), 'l2': m[2], 'linf': m[3], 'factor': m[4], 'dof': int(m[5])})
 out['suite_D2_disc_dirichlet'] = d2
+# Parabolic suite (ParabolicBSAM/tests/runParabolicTests.m P1-P4) and its
+# regressions (runParabolicRegressions.m, the 'PASS CN' lines).
+par = {'P1a': {}, 'P1b': [], 'P2_steps': [], 'CN_mass': []}
+for line in section('P1', 0):
+    m = re.match(r'\s+(be|bdf2|cn)\s+Cauchy diffs \[([^\]]+)\]', line)
+    if m:
+        par['P1a'][m[1]] = m[2].split()
+    m = re.match(r'\s+bdf2\s+h=1/(\d+)\s+Dt=([0-9.]+)\s+err_inf=([0-9.e+-]+)\s+<V>=([0-9.]+)\s+regrids=(\d+)', line)
+    if m:
+        par['P1b'].append({'h_inv': int(m[1]), 'Dt': float(m[2]), 'err_inf': m[3], 'meanV': m[4],
+                           'regrids': int(m[5])})
+for line in section('P2', 0):
+    m = heat_re.search(line)
+    if m:
+        par['P2_steps'].append({'step': int(m[1]), 'V': int(m[4]), 'rel': m[5], 'levels': int(m[6]),
+                                'cells': int(m[7]), 'mass': m[8]})
+    m = re.match(r'\s+steps=(\d+)\s+regrids=(\d+)\s+<V/step>=([0-9.]+)\s+mass drift=([0-9.e+-]+) \(mass=([0-9.]+)\)',
+                 line)
+    if m:
+        par['P2'] = {'steps': int(m[1]), 'regrids': int(m[2]), 'meanV': m[3], 'drift': m[4], 'mass': m[5]}
+    m = re.match(r'\s+final levels: (\d+)', line)
+    if m:
+        par['P2']['final_levels'] = int(m[1])
+for line in section('P3', 0):
+    m = re.search(r'finest level covers it: (\d)', line)
+    if m:
+        par['P3'] = {'covered': int(m[1])}
+    m = re.match(r'\s+cells=(\d+) .*regrids=(\d+), <V>=([0-9.]+)', line)
+    if m:
+        par['P3'].update({'cells': int(m[1]), 'regrids': int(m[2]), 'meanV': m[3]})
+for line in section('P4', 0):
+    m = re.match(r'\s+P2 mean V-cycles/step: ([0-9.]+)', line)
+    if m:
+        par['P4'] = {'meanV': m[1]}
+    m = re.search(r'max\|u\| = ([0-9.]+)', line)
+    if m:
+        par['P4']['umax_big_dt'] = m[1]
+for line in suite:
+    m = re.match(r'PASS CN time-dependent C: errors \[([^\]]+)\]', line)
+    if m:
+        par['CN_reaction_errors'] = m[1].split()
+    m = re.match(r'PASS CN time-dependent D/BC: Cauchy \[([^\]]+)\]', line)
+    if m:
+        par['CN_diffusion_cauchy'] = m[1].split()
+    m = re.match(r'PASS CN composite mass: regrid=(\d) drift=([0-9.e+-]+) rel=([0-9.e+-]+)', line)
+    if m:
+        par['CN_mass'].append({'regrid': int(m[1]), 'drift': m[2], 'rel': m[3]})
+out['suite_parabolic'] = par
 out['source'] = {'repository': 'BSAM-in-MATLAB', 'files': ['verification/starfish-full-residual.csv',
                                                           'verification/starfish-full.json',
                                                           'verification/readme-examples.txt',
