@@ -122,6 +122,31 @@ for which, tag in ((0, ''), (1, '_tree')):
         if m:
             t8.append({'patches': int(m[1]), 'minw': int(m[2]), 'factor': m[3], 'err': m[4], 'mass': m[5]})
     out['suite_T8_scattered' + tag] = t8
+# T9 (EllipticBSAMTree/tests/runAllTreeTests.m:242-283): tree invariants and
+# the straddling-feature scenario; T6 (runAllTests.m:148-155): the 2-level
+# QIF factors of T3 for m0 = 32..256.
+t9 = {}
+for line in section('T9', 0):
+    m = re.match(r'\s+T5 hierarchy: (\d+) AMR level\(s\), per-level patches \[([^\]]+)\], max children (\d+)', line)
+    if m:
+        t9.update({'depth': int(m[1]), 'per_level': [int(v) for v in m[2].split()], 'max_children': int(m[3])})
+    m = re.match(r'\s+straddle scenario: level-2 patches=(\d+), level-3 patches=(\d+), parents=\[([^\]]+)\]', line)
+    if m:
+        t9.update({'np2': int(m[1]), 'np3': int(m[2]), 'parents': [int(v) for v in m[3].split()]})
+    m = re.match(r'\s+solver: V=(\d+) rel=([0-9.e+-]+) factor=([0-9.]+) mass=([0-9.e+-]+) err=([0-9.e+-]+)', line)
+    if m:
+        t9.update({'V': int(m[1]), 'rel': m[2], 'factor': m[3], 'mass': m[4], 'err': m[5]})
+out['suite_T9_tree'] = t9
+for which, tag in ((0, ''), (1, '_tree')):
+    t6 = {}
+    for line in section('T6', which):
+        m = re.match(r'\s+m0 = \[([^\]]+)\]', line)
+        if m:
+            t6['m0'] = [int(v) for v in m[1].split()]
+        m = re.match(r'\s+factors = \[([^\]]+)\]', line)
+        if m:
+            t6['factors'] = m[1].split()
+    out['suite_T6_h_independence' + tag] = t6
 # Diffuse-domain suite (DiffuseDomainBSAM/tests/runDdTests.m): D1 star /
 # Neumann (uniform, adaptive, adaptive without corrections) and D2 disc /
 # Dirichlet penalty.

@@ -57,21 +57,39 @@ def test_uniform_mms_T1():
         assert printed_close(st['avgFactor'], g['factor']), (st['avgFactor'], g['factor'])
 
 
+@pytest.mark.parametrize('tree', [False, True])
 @pytest.mark.parametrize('interp', ['qif', 'lif'])
-def test_box_in_box_T3(interp):
-    """G5: T3 fixed box-in-box hierarchies, m0 = 32 and 64, 2-4 levels
-    (suite-output.txt:22-47): error, factor, V-cycles, mass defect < 1e-13."""
-    rows = [g for g in GOLD['suite_T3_box_in_box'] if g['interp'] == interp and g['m0'] in (32, 64)]
-    assert len(rows) == 6
+@pytest.mark.parametrize('m0', [32, 64, 128, 256])
+def test_box_in_box_T3(interp, m0, tree):
+    """G5: T3 fixed box-in-box hierarchies, 2-4 levels, QC-ring and tree
+    (suite-output.txt:17-44, 99-126): error, factor, V-cycles, mass defect
+    < 1e-13."""
+    key = 'suite_T3_box_in_box_tree' if tree else 'suite_T3_box_in_box'
+    rows = [g for g in GOLD[key] if g['interp'] == interp and g['m0'] == m0]
+    assert len(rows) == 3
+    solve = ebtSolve if tree else ebSolve
     for g in rows:
-        sol = ebSolve(gauss51_problem(), 'BaseCells', g['m0'], 'MaxLevels', g['L'], 'Indicator', 'fun',
-                      'TagFunction', box_in_box_tag, 'TagBuffer', 0, 'GhostInterp', interp, 'Verbose', 0,
-                      'RelTol', 1e-10, 'MaxVCycles', 40, backend=OracleBackend())
+        sol = solve(gauss51_problem(), 'BaseCells', g['m0'], 'MaxLevels', g['L'], 'Indicator', 'fun',
+                    'TagFunction', box_in_box_tag, 'TagBuffer', 0, 'GhostInterp', interp, 'Verbose', 0,
+                    'RelTol', 1e-10, 'MaxVCycles', 40, backend=OracleBackend())
         st = sol['stats']['stages'][-1]
         assert st['vcycles'] == g['V'], (g, st['vcycles'])
         assert printed_close(sol['err']['linf'], g['err']), (sol['err']['linf'], g)
         assert printed_close(st['avgFactor'], g['factor']), (st['avgFactor'], g)
         assert sol['mass']['rel'] < 1e-13
+
+
+@pytest.mark.parametrize('tree', [False, True])
+def test_h_independence_T6(tree):
+    """T6 (runAllTests.m:148-155): the 2-level QIF V-cycle factor of T3 is
+    h-independent, recorded to 3 significant digits for m0 = 32..256."""
+    g = GOLD['suite_T6_h_independence_tree' if tree else 'suite_T6_h_independence']
+    solve = ebtSolve if tree else ebSolve
+    for m0, fac in zip(g['m0'], g['factors']):
+        sol = solve(gauss51_problem(), 'BaseCells', m0, 'MaxLevels', 2, 'Indicator', 'fun',
+                    'TagFunction', box_in_box_tag, 'TagBuffer', 0, 'GhostInterp', 'qif', 'Verbose', 0,
+                    'RelTol', 1e-10, 'MaxVCycles', 40, backend=OracleBackend())
+        assert printed_close(sol['stats']['stages'][-1]['avgFactor'], fac), (m0, fac)
 
 
 @pytest.mark.slow
