@@ -157,7 +157,20 @@ for line in section('D1', 0):
     if m:
         d1.append({'eps': float(m[1]), 'uni_l2': m[2], 'amr_l2': m[3], 'nocorr_l2': m[4], 'mass_uni': m[5],
                    'mass_amr': m[6], 'mass_nocorr': m[7], 'amr_factor': m[8]})
+for line in section('D3', 0):           # cells(uni) / cells(amr) = the D1 solves' dof
+    m = re.match(r'\s+([0-9.]+)\s+(\d+)\s+(\d+)\s+[0-9.]+x', line)
+    if m:
+        for row in d1:
+            if row['eps'] == float(m[1]):
+                row.update({'dof_uni': int(m[2]), 'dof_amr': int(m[3])})
 out['suite_D1_star_neumann'] = d1
+d1b = []
+for line in section('D1b', 0):
+    m = re.match(r'\s+eps=([0-9.]+)\s+E\(eps/h=12.8\)=([0-9.e+-]+)\s+E\(25.6\)=([0-9.e+-]+)\s+h-rate=(-?[0-9.]+)'
+                 r'\s+model M=([0-9.e+-]+)', line)
+    if m:
+        d1b.append({'eps': float(m[1]), 'E1': m[2], 'E2': m[3], 'h_rate': m[4], 'M': m[5]})
+out['suite_D1b_circle_model_error'] = d1b
 d2 = []
 for line in section('D2', 0):
     m = re.match(r'\s+eps=([0-9.]+)\s+L2=([0-9.e+-]+)\s+Linf=([0-9.e+-]+)\s+factor=([0-9.]+)\s+dof=(\d+)', line)

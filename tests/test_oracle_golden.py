@@ -47,8 +47,8 @@ def test_readme_config1_stage_lines(tree):
 
 
 def test_uniform_mms_T1():
-    """G5: T1 uniform MMS with variable D, C (suite-output.txt:3-7)."""
-    for g in GOLD['suite_T1_uniform_mms'][:3]:
+    """G5: T1 uniform MMS with variable D, C, m = 32..256 (suite-output.txt:3-7)."""
+    for g in GOLD['suite_T1_uniform_mms']:
         sol = ebSolve(vardc_problem(), 'BaseCells', g['m'], 'Verbose', 0, 'RelTol', 1e-11, backend=OracleBackend())
         st = sol['stats']['stages'][-1]
         assert st['vcycles'] == g['V']
