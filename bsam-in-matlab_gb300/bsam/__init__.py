@@ -9,11 +9,11 @@ through its C-ABI (``include/bsam_dev.h``).  There is no CPU solve path.
 """
 from .options import ebOptions, ebtOptions, Options
 from .problem import ebProblem, ebtProblem
-from .solve import ebSolve, ebtSolve, ebSolveCycles, ebtSolveCycles, build_hierarchy, error_norms
+from .solve import ebSolve, ebtSolve, ebSolveCycles, ebtSolveCycles, build_hierarchy, error_norms, ebSample, ebtSample
 from .treecheck import ebtTreeCheck
 from .ddsolve import ddGeometry, ddProblem, ddSolve, ddErrorInside, ddToUniform
 from . import hierarchy, tagcluster, flat
 
 __all__ = ['ebOptions', 'ebtOptions', 'Options', 'ebProblem', 'ebtProblem', 'ebSolve', 'ebtSolve',
-           'ebSolveCycles', 'ebtSolveCycles', 'build_hierarchy', 'error_norms', 'hierarchy', 'tagcluster',
+           'ebSolveCycles', 'ebtSolveCycles', 'build_hierarchy', 'error_norms', 'ebSample', 'ebtSample', 'hierarchy', 'tagcluster',
            'flat', 'ddGeometry', 'ddProblem', 'ddSolve', 'ddErrorInside', 'ddToUniform', 'ebtTreeCheck']

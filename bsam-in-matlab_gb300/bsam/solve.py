@@ -170,3 +170,44 @@ def error_norms(H, ufun=None):
             l2sq += float(np.sum(ev ** 2)) * da
             dof += ev.size
     return {'linf': linf, 'l2': math.sqrt(l2sq), 'dof': dof, 'meanShift': m}
+
+
+def ebSample(H, xq, yq):
+    """Bilinear sample of the composite solution at points (``ebSample.m``,
+    tree copy ``ebtSample.m``): each point takes the finest patch that
+    contains it (boundary included), interpolating the padded Q, ghosts
+    included, at its fractional cell-centre index."""
+    xq = np.asarray(xq, dtype=np.float64)
+    yq = np.asarray(yq, dtype=np.float64)
+    dom = H.prob.domain
+    vals = np.full(xq.shape, np.nan)
+    assigned = np.zeros(xq.shape, dtype=bool)
+    for k in range(H.nlev, H.rootIdx - 1, -1):
+        lev = H.lev[k]
+        hx, hy = lev.h
+        for p in range(lev.np):
+            b = lev.box[p]
+            x0 = dom[0] + (b[0] - 1) * hx
+            x1 = dom[0] + b[1] * hx
+            y0 = dom[2] + (b[2] - 1) * hy
+            y1 = dom[2] + b[3] * hy
+            inside = ~assigned & (xq >= x0) & (xq <= x1) & (yq >= y0) & (yq <= y1)
+            if not inside.any():
+                continue
+            Q = lev.Q[p]
+            m2, n2 = Q.shape
+            s = (xq[inside] - x0) / hx + 1.5          # fractional 1-based padded index
+            t = (yq[inside] - y0) / hy + 1.5
+            i0 = np.minimum(np.maximum(np.floor(s), 1), m2 - 1).astype(np.int64)
+            j0 = np.minimum(np.maximum(np.floor(t), 1), n2 - 1).astype(np.int64)
+            fr = s - i0
+            ft = t - j0
+            vals[inside] = ((1 - fr) * (1 - ft) * Q[i0 - 1, j0 - 1] + fr * (1 - ft) * Q[i0, j0 - 1]
+                            + (1 - fr) * ft * Q[i0 - 1, j0] + fr * ft * Q[i0, j0])
+            assigned[inside] = True
+    if not assigned.all():
+        raise ValueError(('ebt' if H.tree else 'eb') + '_sample:cover: query points outside the domain.')
+    return vals
+
+
+ebtSample = ebSample
