@@ -1,5 +1,5 @@
-"""Adversarial interface geometries (EllipticBSAM/tests/stressInterfaces.m,
-S1-S9).
+"""Adversarial interface geometries (EllipticBSAM/tests/stressInterfaces.m
+S1-S9, EllipticBSAMTree/tests/stressTreeInterfaces.m S1-S10).
 
 CPU (oracle): each case's pass criterion restated -- Linf rates above 1.75
 over m = 32, 64, 128, V-cycle factor <= 0.2, relative mass defect <= 5e-10
@@ -8,16 +8,19 @@ nodes on Dirichlet / Neumann / mixed sides, minimum-width patches,
 hand-built checkerboards / spirals / corridors / edge kisses / surrounded
 patches, a 5-level cross point, the conservation discriminators (the defect
 scales with RelTol; corrections off break it) and singular Neumann with
-SourceQuad 3.  GPU: every layout solved on the CUDA path equals the oracle
-bit for bit (residual history and composite field).
+SourceQuad 3; the tree form of every layout passes ebtTreeCheck and agrees
+with the ring form on identical meshes (S10).  GPU: every layout, ring and
+tree, solved on the CUDA path equals the oracle bit for bit (residual
+history and composite field).
 """
 import warnings
 
 import numpy as np
 import pytest
 
-from bsam import ebOptions, ebProblem, ebSolve, hierarchy as hier
+from bsam import ebOptions, ebProblem, ebSolve, ebtSolve, hierarchy as hier
 from bsam.solve import ebSolveCycles, error_norms
+from bsam.treecheck import ebtTreeCheck
 from bsam_oracle import OracleBackend
 from cases import vardc_problem
 
@@ -181,33 +184,41 @@ def scale_boxes(b, s):
     return np.stack([(b[:, 0] - 1) * s + 1, b[:, 1] * s, (b[:, 2] - 1) * s + 1, b[:, 3] * s], axis=1)
 
 
-def build_boxes(prob, m, levels, rtol, maxv, backend, **opts):
+def build_boxes(prob, m, levels, rtol, maxv, backend, tree=False, **opts):
     """ebSetup + ebAddLevel per box list + ebSolveCycles (stressInterfaces.m
-    buildBoxes)."""
+    buildBoxes); the tree form resolves each box's single parent by
+    containment and checks every tree invariant before the solve
+    (stressTreeInterfaces.m buildBoxesT)."""
+    o = ebOptions('BaseCells', [m, m], 'Verbose', 0, 'RelTol', rtol, 'MaxVCycles', maxv, **opts)
+    H = hier.setup(prob, o, backend, tree=tree)
     for bx in levels:
-        bx = np.asarray(bx)
+        bx = np.asarray(bx, dtype=np.int64)
         for a in range(len(bx)):
             for b in range(a + 1, len(bx)):
                 assert not (bx[a, 0] <= bx[b, 1] and bx[a, 1] >= bx[b, 0] and bx[a, 2] <= bx[b, 3]
                             and bx[a, 3] >= bx[b, 2]), 'stress:overlap'
-    o = ebOptions('BaseCells', [m, m], 'Verbose', 0, 'RelTol', rtol, 'MaxVCycles', maxv, **opts)
-    H = hier.setup(prob, o, backend)
-    for bx in levels:
+        if tree:
+            levC = H.lev[H.nlev]
+            par = [next(q + 1 for q, qb in enumerate(levC.box)
+                        if qb[0] <= b[0] and b[1] <= qb[1] and qb[2] <= b[2] and b[3] <= qb[3]) for b in bx]
+            bx = np.column_stack([par, bx])
         H = hier.add_level(H, bx, backend)
+    if tree:
+        ebtTreeCheck(H)
     return ebSolveCycles(H, backend)
 
 
-def box_case(name, m, backend, rtol=1e-10, maxv=60):
+def box_case(name, m, backend, rtol=1e-10, maxv=60, tree=False):
     pname, levels = BOX_CASES[name]
     s = m // 32
-    return build_boxes(problem(pname), m, [scale_boxes(b, s) for b in levels], rtol, maxv, backend)
+    return build_boxes(problem(pname), m, [scale_boxes(b, s) for b in levels], rtol, maxv, backend, tree=tree)
 
 
-def tag_case(name, m, backend, prob=None, rtol=1e-10, maxv=60, **extra):
+def tag_case(name, m, backend, prob=None, rtol=1e-10, maxv=60, tree=False, **extra):
     tag, fill, ghost, _ = TAG_CASES[name]
     with warnings.catch_warnings():
         warnings.simplefilter('ignore')
-        return ebSolve(prob or problem('V'), 'BaseCells', [m, m], 'MaxLevels', 2, 'Indicator', 'fun',
+        return (ebtSolve if tree else ebSolve)(prob or problem('V'), 'BaseCells', [m, m], 'MaxLevels', 2, 'Indicator', 'fun',
                        'TagFunction', tag, 'TagBuffer', 0, 'MinBoxWidth', 2, 'MinFillRatio', fill,
                        'GhostInterp', ghost, 'Verbose', 0, 'RelTol', rtol, 'MaxVCycles', maxv, backend=backend,
                        **extra)
@@ -221,16 +232,20 @@ def _check_sweep(errs, facs, mass):
 
 
 # ------------------------------------------------------------------ CPU tests
+@pytest.mark.parametrize('tree', [False, True])
 @pytest.mark.parametrize('name', list(TAG_CASES) + ['COMBB-NN'])
-def test_tag_driven_interfaces(name):
+def test_tag_driven_interfaces(name, tree):
     """S1 comb interfaces (QIF, LIF, boundary comb, Neumann-side comb) and
-    S3 reentrant shapes; ANNULUS keeps its coarse hole at every size."""
+    S3 reentrant shapes, ring and tree; ANNULUS keeps its coarse hole at
+    every size; every tree hierarchy passes ebtTreeCheck."""
     be = OracleBackend()
     base = 'COMBB' if name == 'COMBB-NN' else name
     prob = problem(TAG_PROBLEM.get(name, 'V'))
     errs, facs, mass = [], [], []
     for m in MS:
-        sol = tag_case(base, m, be, prob=prob)
+        sol = tag_case(base, m, be, prob=prob, tree=tree)
+        if tree:
+            ebtTreeCheck(sol['H'])
         errs.append(sol['err']['linf'])
         facs.append(sol['stats']['stages'][-1]['avgFactor'])
         mass.append(sol['mass']['rel'])
@@ -259,25 +274,28 @@ def test_comb_anisotropic_cells():
     assert np.all(r >= RATE_BAR) and max(facs) <= 0.25 and max(abs(v) for v in mass) <= MASS_BAR
 
 
+@pytest.mark.parametrize('tree', [False, True])
 @pytest.mark.parametrize('name', list(BOX_CASES))
-def test_hand_built_layouts(name):
+def test_hand_built_layouts(name, tree):
     """S2 corner-only adjacency, S4 hanging nodes at the boundary, S5
-    minimum-width patches, S6 adversarial layouts, S7 the 5-level cross."""
+    minimum-width patches, S6 adversarial layouts, S7 the 5-level cross,
+    ring and tree."""
     be = OracleBackend()
     errs, facs, mass = [], [], []
     for m in MS:
-        H = box_case(name, m, be)
+        H = box_case(name, m, be, tree=tree)
         errs.append(error_norms(H)['linf'])
         facs.append(H.stats['stages'][-1]['avgFactor'])
         mass.append(be.mass_check(H)['rel'])
     _check_sweep(errs, facs, mass)
 
 
-@pytest.mark.parametrize('name', ['EDGEKISS', 'EDGEKISS2'])
-def test_fill_down_face_copies_identical(name):
+@pytest.mark.parametrize('name,tree', [('EDGEKISS', False), ('EDGEKISS2', False), ('CHECKER', True),
+                                       ('CHECKER3', True), ('EDGEKISS', True), ('EDGEKISS2', True)])
+def test_fill_down_face_copies_identical(name, tree):
     """S6: both stored copies of a face shared by abutting same-level patches
     carry the same coefficient after the fill-down."""
-    H = box_case(name, 32, OracleBackend(), rtol=1e-9, maxv=2)
+    H = box_case(name, 32, OracleBackend(), rtol=1e-9, maxv=2, tree=tree)
     dup = 0.0
     for k in range(1, H.nlev + 1):
         lev = H.lev[k]
@@ -361,6 +379,28 @@ def test_singular_neumann_exotic_meshes():
     assert np.log2(errs[0] / errs[1]) >= RATE_BAR and max(facs) <= FAC_BAR
 
 
+S10 = [('CORNER4', 32), ('CORNER4', 64), ('CHAIN', 32), ('RINGTOUCH', 32), ('SKINNY3', 32), ('CHECKER', 32),
+       ('CHECKER', 64), ('CHECKER3', 32), ('SPIRAL', 32), ('CORRIDORS', 32), ('EDGEKISS2', 32), ('EDGEKISS2', 64),
+       ('DEEPCROSS5', 32), ('DEEPCROSS5', 64), ('HANGQ3-V', 32)]
+
+
+@pytest.mark.parametrize('name,m', S10)
+def test_ring_and_tree_agree_on_identical_meshes(name, m):
+    """S10 (stressTreeInterfaces.m:317-345): the ring and tree solvers on the
+    same hand-built mesh agree to 1e-11 with equal V-cycle counts."""
+    be = OracleBackend()
+    levels = BOX_CASES['HANGQ3-MX'][1] if name == 'HANGQ3-V' else BOX_CASES[name][1]
+    lv = [scale_boxes(b, m // 32) for b in levels]
+    Hr = build_boxes(problem('V'), m, lv, 1e-10, 60, be)
+    Ht = build_boxes(problem('V'), m, lv, 1e-10, 60, be, tree=True)
+    assert Hr.stats['stages'][-1]['vcycles'] == Ht.stats['stages'][-1]['vcycles']
+    d = 0.0
+    for k in range(Hr.rootIdx, Hr.nlev + 1):
+        for qa, qb in zip(Hr.lev[k].Q, Ht.lev[k].Q):
+            d = max(d, float(np.max(np.abs(qa[1:-1, 1:-1] - qb[1:-1, 1:-1]))))
+    assert d <= 1e-11, d
+
+
 # ------------------------------------------------------------------ GPU tests
 def _assert_same(Ho, Hd):
     for so, sd in zip(Ho.stats['stages'], Hd.stats['stages']):
@@ -372,18 +412,20 @@ def _assert_same(Ho, Hd):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize('tree', [False, True])
 @pytest.mark.parametrize('name', list(BOX_CASES))
-def test_hand_built_layouts_device_bitwise(name):
+def test_hand_built_layouts_device_bitwise(name, tree):
     from bsam.device import DeviceBackend
-    _assert_same(box_case(name, 64, OracleBackend()), box_case(name, 64, DeviceBackend.get(0)))
+    _assert_same(box_case(name, 64, OracleBackend(), tree=tree), box_case(name, 64, DeviceBackend.get(0), tree=tree))
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize('tree', [False, True])
 @pytest.mark.parametrize('name', list(TAG_CASES) + ['COMBB-NN'])
-def test_tag_driven_interfaces_device_bitwise(name):
+def test_tag_driven_interfaces_device_bitwise(name, tree):
     from bsam.device import DeviceBackend
     base = 'COMBB' if name == 'COMBB-NN' else name
     prob = problem(TAG_PROBLEM.get(name, 'V'))
-    o = tag_case(base, 64, OracleBackend(), prob=prob)
-    d = tag_case(base, 64, DeviceBackend.get(0), prob=prob)
+    o = tag_case(base, 64, OracleBackend(), prob=prob, tree=tree)
+    d = tag_case(base, 64, DeviceBackend.get(0), prob=prob, tree=tree)
     _assert_same(o['H'], d['H'])
