@@ -95,6 +95,12 @@ def ebpOptions(*args, **kwargs) -> Options:
         v = opts[nm]
         if not (np.isscalar(v) and np.isreal(v) and np.isfinite(v) and v > 0):
             raise ValueError(f'ebp_options:time: {nm} must be a positive finite real scalar.')
+    for nm, lo in (('RegridEvery', 0), ('StepVerbose', 0), ('MaxVCyclesStep', 1)):
+        v = opts[nm]
+        if not (np.isscalar(v) and np.isreal(v) and np.isfinite(v) and float(v) == int(v) and v >= lo):
+            raise ValueError(f'ebp_options:{nm.lower()}: {nm} must be an integer >= {lo}.')
+    if opts.Callback is not None and not callable(opts.Callback):
+        raise ValueError('ebp_options:callback: Callback must be empty or a function handle.')
     eb = ebOptions(*rest)
     eb.Verbose = 0
     eb.MaxVCycles = int(opts.MaxVCyclesStep)

@@ -197,3 +197,20 @@ def test_P1b_device_matches_oracle_pipeline():
         for qa, qb in zip(Ha.lev[k].Q, Hb.lev[k].Q):
             np.testing.assert_array_equal(qa, qb)
     assert a['err'] == b['err']
+
+
+@pytest.mark.parametrize('name,bad', [('RegridEvery', -1), ('RegridEvery', 2.5), ('StepVerbose', np.inf),
+                                      ('MaxVCyclesStep', 0), ('Callback', 3)])
+def test_invalid_time_options_rejected(name, bad):
+    """ebpOptions.m:47-54."""
+    with pytest.raises(ValueError, match='ebp_options:'):
+        ebpOptions('Dt', 0.1, 'TFinal', 1, name, bad)
+
+
+def test_callback_called_after_every_step():
+    seen = []
+    s = ebpSolve(heat2_problem(), 'Scheme', 'be', 'Dt', 0.1, 'TFinal', 0.3, 'RegridEvery', 0, 'StepVerbose', 0,
+                 'BaseCells', [32, 32], 'MaxLevels', 1, 'RelTol', 1e-9,
+                 'Callback', lambda H, t, n: seen.append((round(t, 12), n)), backend=OracleBackend())
+    assert seen == [(0.1, 1), (0.2, 2), (0.3, 3)]
+    assert len(s['cycles']) == 3
