@@ -131,43 +131,56 @@ static double box_lb(const Node *nd, double x, double y) {
   return dx * dx + dy * dy;
 }
 
+static inline double seg_d2(const Starfish *g, int j, double x, double y) {
+  const double ax = g->a[2 * (j - 1)], ay = g->a[2 * (j - 1) + 1];
+  const double ex = g->e[2 * (j - 1)], ey = g->e[2 * (j - 1) + 1];
+  double t = ((x - ax) * ex + (y - ay) * ey) / g->len2[j - 1];
+  t = fmax(0.0, fmin(1.0, t));
+  const double px = (x - ax) - t * ex, py = (y - ay) - t * ey;
+  return px * px + py * py;
+}
+
 /* The tree search of ddStarfishGeometry.m: a node is entered when its box's
    squared distance is within best + 64 eps.  The result is the minimum over
    every segment whose leaf is entered, and the leaf of the nearest segment
-   is always entered, so the order in which children are tried changes only
-   how much is pruned: the nearer child goes first. */
-static void visit(const Starfish *g, int id, double lb, double x, double y, double *best) {
+   is always entered, so neither the order in which children are tried nor a
+   starting bound that is itself some segment's distance changes the result,
+   only how much is pruned: the nearer child goes first, and *arg returns
+   the segment that gave the minimum. */
+static void visit(const Starfish *g, int id, double lb, double x, double y, double *best, int *arg) {
   if (!(lb <= *best + 64 * DBL_EPSILON)) return;
   const Node *nd = &g->nodes[id - 1];
   if (nd->left != 0) {
     const double ll = box_lb(&g->nodes[nd->left - 1], x, y), lr = box_lb(&g->nodes[nd->right - 1], x, y);
     if (ll < lr) {
-      visit(g, nd->left, ll, x, y, best);
-      visit(g, nd->right, lr, x, y, best);
+      visit(g, nd->left, ll, x, y, best, arg);
+      visit(g, nd->right, lr, x, y, best, arg);
     } else {
-      visit(g, nd->right, lr, x, y, best);
-      visit(g, nd->left, ll, x, y, best);
+      visit(g, nd->right, lr, x, y, best, arg);
+      visit(g, nd->left, ll, x, y, best, arg);
     }
     return;
   }
   double local = *best;
+  int a = *arg;
   for (int j = nd->first; j <= nd->last; ++j) {
-    const double ax = g->a[2 * (j - 1)], ay = g->a[2 * (j - 1) + 1];
-    const double ex = g->e[2 * (j - 1)], ey = g->e[2 * (j - 1) + 1];
-    double t = ((x - ax) * ex + (y - ay) * ey) / g->len2[j - 1];
-    t = fmax(0.0, fmin(1.0, t));
-    const double px = (x - ax) - t * ex, py = (y - ay) - t * ey;
-    const double dd = px * px + py * py;
-    local = fmin(local, dd);
+    const double dd = seg_d2(g, j, x, y);
+    if (dd < local) { local = dd; a = j; }
   }
   *best = local;
+  *arg = a;
 }
 
-/* Signed distance, positive inside (ddStarfishGeometry.m:140-177). */
+/* Signed distance, positive inside (ddStarfishGeometry.m:140-177).  Points
+   are visited in order and each search starts from the smaller of the
+   distance to the first vertex of the segment its polar angle falls in and
+   the distance to the previous point's nearest segment: on grid-ordered
+   samples that bound is tight and prunes most of the tree. */
 void bsam_starfish_distance(void *p, const double *X, const double *Y, double *d, int64_t n) {
   const Starfish *g = (const Starfish *)p;
   const double twopi = 2 * M_PI;
   const int ns = g->ns;
+  int prev = 0;
   for (int64_t i = 0; i < n; ++i) {
     const double x = X[i], y = Y[i];
     double ang = atan2(y, x);
@@ -176,7 +189,13 @@ void bsam_starfish_distance(void *p, const double *X, const double *Y, double *d
     if (seg > ns) seg = ns;
     const double ax = g->a[2 * (seg - 1)], ay = g->a[2 * (seg - 1) + 1];
     double best = (x - ax) * (x - ax) + (y - ay) * (y - ay);
-    visit(g, 1, box_lb(&g->nodes[0], x, y), x, y, &best);
+    int arg = seg;
+    if (prev > 0) {
+      const double dp = seg_d2(g, prev, x, y);
+      if (dp < best) { best = dp; arg = prev; }
+    }
+    visit(g, 1, box_lb(&g->nodes[0], x, y), x, y, &best, &arg);
+    prev = arg;
     const double ux = cos(ang), uy = sin(ang);
     const double ex = g->e[2 * (seg - 1)], ey = g->e[2 * (seg - 1) + 1];
     const double radius = (ax * ey - ay * ex) / (ux * ey - uy * ex);

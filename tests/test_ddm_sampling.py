@@ -72,3 +72,30 @@ def test_starfish_hierarchy_device_sampling_identical():
     np.testing.assert_array_equal(a.patches, b.patches)
     for name in ('DeW', 'DnS', 'CC', 'InvDiagS', 'FTrue', 'Q', 'pcoef', 'cfd', 'Ainv'):
         np.testing.assert_array_equal(getattr(a, name), getattr(b, name), err_msg=name)
+
+
+@pytest.mark.parametrize('order', ['grid', 'reversed', 'shuffled'])
+def test_distance_equals_brute_force_in_any_point_order(order):
+    """Each point's search starts from its predecessor's nearest segment; the
+    result is still the minimum over all segments, bit for bit, whatever
+    the order of the points."""
+    g = StarGeometry(3000, 0.9, 1.2, 0.7, 5.0, 0.0)
+    c = -2 + (np.arange(48) + 0.5) * 4 / 48
+    X, Y = np.meshgrid(c, c, indexing='ij')
+    x, y = X.ravel(order='F'), Y.ravel(order='F')
+    if order == 'reversed':
+        x, y = x[::-1].copy(), y[::-1].copy()
+    elif order == 'shuffled':
+        p = np.random.Generator(np.random.PCG64(3)).permutation(x.size)
+        x, y = x[p], y[p]
+    d = g.signedDistance(x, y)
+    v = g.vertices
+    a, e = v[:-1], v[1:] - v[:-1]
+    len2 = e[:, 0] * e[:, 0] + e[:, 1] * e[:, 1]
+    best = np.full(x.size, np.inf)
+    for j in range(a.shape[0]):            # same operation order as the library's segment distance
+        dxa, dya = x - a[j, 0], y - a[j, 1]
+        t = np.clip((dxa * e[j, 0] + dya * e[j, 1]) / len2[j], 0.0, 1.0)
+        px, py = dxa - t * e[j, 0], dya - t * e[j, 1]
+        best = np.minimum(best, px * px + py * py)
+    np.testing.assert_array_equal(np.abs(d), np.sqrt(best))
