@@ -472,27 +472,30 @@ def _landscape(H, k, p, OF):
 
 
 def _resolve_cells(levC, OC, gis, gjs, Il, Jl, cmx, cmy):
-    """``resolveCells`` (``ebBuildOps.m:221-252``)."""
+    """``resolveCells`` (``ebBuildOps.m:221-252``): for each ring cell its
+    owning parent patch and the padded source / destination indices,
+    grouped by parent in ascending order (cell order kept inside a group).
+    The first offending cell raises, as the per-cell loop does."""
     nC = levC.n
-    npnt = len(gis)
-    sp = np.zeros(npnt, np.int64)
-    src = np.zeros(npnt, np.int64)
-    dst = np.zeros(npnt, np.int64)
-    for t in range(npnt):
-        gi, gj = int(gis[t]), int(gjs[t])
-        gic = min(max(gi, 1), nC[0])
-        gjc = min(max(gj, 1), nC[1])
-        q = int(OC[gic - 1, gjc - 1])
-        if q == 0:
-            raise ValueError(f'eb_build_ops:ring: parent cell ({gi},{gj}) not covered - proper nesting violated.')
-        qb = levC.box[q - 1]
-        li, lj = gi - int(qb[0]) + 2, gj - int(qb[2]) + 2
-        mqx, mqy = int(qb[1] - qb[0] + 1), int(qb[3] - qb[2] + 1)
-        if li < 1 or li > mqx + 2 or lj < 1 or lj > mqy + 2:
-            raise ValueError('eb_build_ops:overhang: ring cell overhang exceeds ghost ring.')
-        sp[t] = q
-        src[t] = sub2ind(mqx + 2, li, lj)
-        dst[t] = sub2ind(cmx + 2, gi - Il + 2, gj - Jl + 2)
+    gi = np.asarray(gis, dtype=np.int64).ravel()
+    gj = np.asarray(gjs, dtype=np.int64).ravel()
+    if gi.size == 0:
+        return []
+    sp = OC[np.clip(gi, 1, nC[0]) - 1, np.clip(gj, 1, nC[1]) - 1].astype(np.int64)
+    unc = sp == 0
+    qb = np.asarray(levC.box, dtype=np.int64)[np.where(unc, 1, sp) - 1]
+    li, lj = gi - qb[:, 0] + 2, gj - qb[:, 2] + 2
+    mqx, mqy = qb[:, 1] - qb[:, 0] + 1, qb[:, 3] - qb[:, 2] + 1
+    over = ~unc & ((li < 1) | (li > mqx + 2) | (lj < 1) | (lj > mqy + 2))
+    bad = np.nonzero(unc | over)[0]
+    if bad.size:
+        t = int(bad[0])
+        if unc[t]:
+            raise ValueError(f'eb_build_ops:ring: parent cell ({gi[t]},{gj[t]}) not covered - proper nesting '
+                             f'violated.')
+        raise ValueError('eb_build_ops:overhang: ring cell overhang exceeds ghost ring.')
+    src = sub2ind(mqx + 2, li, lj)
+    dst = sub2ind(cmx + 2, gi - Il + 2, gj - Jl + 2)
     ops = []
     for q in np.unique(sp):
         ii = sp == q
@@ -506,18 +509,13 @@ def _corr_face(levC, OC, mask, gis, gjs):
     idx = np.nonzero(mask)[0]
     if idx.size == 0:
         return cs
-    gis = np.broadcast_to(np.asarray(gis), mask.shape)
-    gjs = np.broadcast_to(np.asarray(gjs), mask.shape)
-    dp = np.zeros(idx.size, np.int64)
-    dst = np.zeros(idx.size, np.int64)
-    for t, j in enumerate(idx):
-        q = int(OC[gis[j] - 1, gjs[j] - 1])
-        if q == 0:
-            raise ValueError('eb_build_ops:corr: mass-correction target cell uncovered.')
-        qb = levC.box[q - 1]
-        mqx = int(qb[1] - qb[0] + 1)
-        dp[t] = q
-        dst[t] = sub2ind(mqx, gis[j] - qb[0] + 1, gjs[j] - qb[2] + 1)
+    gi = np.broadcast_to(np.asarray(gis), mask.shape)[idx].astype(np.int64)
+    gj = np.broadcast_to(np.asarray(gjs), mask.shape)[idx].astype(np.int64)
+    dp = OC[gi - 1, gj - 1].astype(np.int64)
+    if (dp == 0).any():
+        raise ValueError('eb_build_ops:corr: mass-correction target cell uncovered.')
+    qb = np.asarray(levC.box, dtype=np.int64)[dp - 1]
+    dst = sub2ind(qb[:, 1] - qb[:, 0] + 1, gi - qb[:, 0] + 1, gj - qb[:, 2] + 1)
     for q in np.unique(dp):
         ii = dp == q
         cs['ops'].append((int(q), idx[ii].astype(np.int64), dst[ii]))
