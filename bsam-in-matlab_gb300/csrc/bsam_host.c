@@ -5,15 +5,17 @@
  *    sqrt) so coefficient sampling gives the same bits on every host,
  *    independent of a vector-math library's approximations.
  *  - The starfish polygon geometry of DiffuseDomainBSAM/src/ddStarfishGeometry.m:
- *    the radially sampled closed polygon, its bounding-box tree (leaves of
- *    at most eight segments, midpoint splits), and the exact point-to-
- *    segment signed distance with the tree pruning of the reference's
- *    vectorised traversal (right child first; prune when the box distance
- *    exceeds the current best plus 64 eps).  The sign comes from the
- *    radial-ray intersection with the enclosing segment.
+ *    the radially sampled closed polygon, a bounding-box tree over its
+ *    segments (midpoint splits; leaves of at most 16 segments where the
+ *    reference's have 8 -- the tree's shape decides only how much is
+ *    pruned, never the minimum), and the exact point-to-segment signed
+ *    distance with the reference's pruning rule (prune when the box
+ *    distance exceeds the current best plus 64 eps).  The sign comes from
+ *    the radial-ray intersection with the enclosing segment.
  *
- * Compiled with -ffp-contract=off so the arithmetic is the same on x86-64
- * and aarch64 hosts.
+ * Compiled with -ffp-contract=off -fno-fast-math (at -O3) so the arithmetic
+ * is the same on x86-64 and aarch64 hosts: no contraction, no reassociation,
+ * no vector math library.
  */
 #include <float.h>
 #include <math.h>
@@ -70,7 +72,7 @@ static int build_node(Starfish *g, int first, int last) {
   nd->box[0] = mnx; nd->box[1] = mny; nd->box[2] = mxx; nd->box[3] = mxy;
   nd->left = nd->right = 0;
   nd->first = first; nd->last = last;
-  if (last - first > 7) {
+  if (last - first > 15) {
     const int mid = (first + last) / 2;
     const int l = build_node(g, first, mid);
     const int r = build_node(g, mid + 1, last);
