@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import threading
 import time
 
 import numpy as np
@@ -178,6 +179,11 @@ class Context:
         except Exception:
             pass
 
+    def __copy__(self):
+        raise TypeError('bsam_device:copy: a device context cannot be copied')
+
+    __deepcopy__ = lambda self, memo: self.__copy__()
+
 
 class DevHier:
     """One uploaded hierarchy (device-resident)."""
@@ -197,6 +203,11 @@ class DevHier:
             lib().bsam_hier_free(self.h)
         except Exception:
             pass
+
+    def __copy__(self):
+        raise TypeError('bsam_device:copy: an uploaded hierarchy cannot be copied (its handle would be freed twice)')
+
+    __deepcopy__ = lambda self, memo: self.__copy__()
 
     def set_opts(self, opts):
         self.opts = solve_opts(opts)
@@ -382,11 +393,16 @@ class DeviceBackend:
     name = 'device'
     _instances = {}
 
+    _lock = threading.Lock()
+
     @classmethod
     def get(cls, device=0):
-        if device not in cls._instances:
-            cls._instances[device] = cls(device)
-        return cls._instances[device]
+        """The process-wide backend of a device (one context per device,
+        created once even when several threads ask at the same time)."""
+        with cls._lock:
+            if device not in cls._instances:
+                cls._instances[device] = cls(device)
+            return cls._instances[device]
 
     # the parabolic driver keeps its state (solution, BDF2 history, source)
     # on the device between steps

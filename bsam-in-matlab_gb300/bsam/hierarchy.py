@@ -73,6 +73,19 @@ class Hierarchy:
         self._dev = None        # resident device copy (bsam.device)
         self.dirty = set()      # fields edited on the host since the last sync
 
+    def __deepcopy__(self, memo):
+        """A deep copy owns no device state: the resident copy (whose handle
+        only this hierarchy frees) is left out, and the copy uploads its own
+        arrays when it is next solved.  A copy whose host arrays are older
+        than the device (``host_stale``) keeps that flag, so using it fails
+        loudly until the original is synced."""
+        import copy
+        new = self.__class__.__new__(self.__class__)
+        memo[id(self)] = new
+        for k, v in self.__dict__.items():
+            setattr(new, k, None if k == '_dev' else copy.deepcopy(v, memo))
+        return new
+
     def touch(self):
         self.version += 1
 

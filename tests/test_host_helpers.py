@@ -5,6 +5,7 @@ fresh inverse."""
 import threading
 
 import numpy as np
+import pytest
 
 from bsam.hierarchy import near_boxes, rect_isect, dense_inverse
 
@@ -54,3 +55,35 @@ def test_dense_inverse_memo_is_bitwise_and_threadsafe():
     a = dense_inverse(mats[0])
     a[0, 0] = 1e9
     np.testing.assert_array_equal(dense_inverse(mats[0]), fresh[0])
+
+
+def test_deepcopy_of_a_hierarchy_leaves_its_device_copy_behind():
+    """A deep copy must not duplicate the resident device handle (both copies
+    would free it); it drops it and re-uploads when next solved."""
+    import copy
+    from bsam import ebOptions, ebProblem, hierarchy as hier
+    from bsam.device import DevHier, Context
+    from bsam_oracle import OracleBackend
+    H = hier.setup(ebProblem([0, 1, 0, 1], 1, 1, 1, ('dirichlet', 0)), ebOptions('BaseCells', 16, 'Verbose', 0),
+                   OracleBackend())
+    class NoDevHier(DevHier):                  # stands in for an uploaded copy: no handle, no device
+        def __del__(self):
+            pass
+
+    class NoContext(Context):
+        def __del__(self):
+            pass
+
+    fake = NoDevHier.__new__(NoDevHier)
+    H._dev = (H.version, fake)
+    H.host_stale = True
+    G = copy.deepcopy(H)
+    assert G._dev is None and H._dev[1] is fake
+    assert G.host_stale is True                # using the copy still requires a host sync of the original
+    np.testing.assert_array_equal(G.lev[1].Q[0], H.lev[1].Q[0])
+    assert G.lev[1].Q[0] is not H.lev[1].Q[0]
+    with pytest.raises(TypeError, match='bsam_device:copy'):
+        copy.deepcopy(fake)
+    ctx = NoContext.__new__(NoContext)
+    with pytest.raises(TypeError, match='bsam_device:copy'):
+        copy.copy(ctx)
