@@ -393,7 +393,7 @@ class DeviceBackend:
     name = 'device'
     _instances = {}
 
-    _lock = threading.Lock()
+    _lock = threading.RLock()
 
     @classmethod
     def get(cls, device=0):
