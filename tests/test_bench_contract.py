@@ -51,3 +51,5 @@ def test_native_line():
     assert d['gpu_launches'] > 1000
     assert d['cpu_baseline']['kind'] == 'port' and d['cpu_baseline']['value'] > 0
     assert {'sm_mhz', 'sm_max_mhz', 'reasons'} <= set(d['clocks'])
+    s = d['setup']
+    assert 0 < s['host_build_s'] < s['setup_and_solve_s'] and s['first_solve_s'] > 0
