@@ -37,7 +37,7 @@ def build_host(force=False):
     src = os.path.join(CSRC, 'bsam_host.c')
     if force or _stale(HOST_LIB, [src]):
         subprocess.check_call(['gcc', '-O3', '-ffp-contract=off', '-fno-fast-math', '-fPIC', '-shared',
-                               '-o', HOST_LIB, src, '-lm'])
+                               '-pthread', '-o', HOST_LIB, src, '-lm'])
     return HOST_LIB
 
 

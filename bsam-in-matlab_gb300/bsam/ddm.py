@@ -37,6 +37,7 @@ class StarGeometry:
         self.name = name or f'star: r = {s0}({s1} + {s2} sin({k} theta + {th0}))'
         self.device = device          # a bsam.device.Context: the segment minimum runs on the GPU
         self._cache = []              # recent (key, d): phi, delta, D, C, F sample the same points
+        self._pref = {}               # key -> (x, y, d) of the point sets handed to prefetch()
 
     def __del__(self):
         try:
@@ -62,20 +63,48 @@ class StarGeometry:
         for k, (kk, xx, yy, dd) in enumerate(self._cache):
             if kk == key and np.array_equal(xx, x) and np.array_equal(yy, y):
                 return dd.reshape(X.shape, order='F').copy()
-        if self.device is None:
-            d = np.empty_like(x)
-            hostlib.lib().bsam_starfish_distance(self._h, x.ctypes.data, y.ctypes.data, d.ctypes.data, x.size)
+        hit = self._pref.get(key)
+        if hit is not None and np.array_equal(hit[0], x) and np.array_equal(hit[1], y):
+            d = hit[2]
         else:
-            from .device import polygon_dist2
-            best = np.empty_like(x)
-            sign = np.empty_like(x)
-            hostlib.lib().bsam_starfish_init_sign(self._h, x.ctypes.data, y.ctypes.data, best.ctypes.data,
-                                                  sign.ctypes.data, x.size)
-            polygon_dist2(self.device, self.vertices, x, y, best)
-            d = sign * np.sqrt(best)
+            d = self._distance(x, y)
         self._cache.insert(0, (key, x, y, d))
         del self._cache[6:]
         return d.reshape(X.shape, order='F').copy()
+
+    def _distance(self, x, y):
+        if self.device is None:
+            d = np.empty_like(x)
+            hostlib.lib().bsam_starfish_distance_mt(self._h, x.ctypes.data, y.ctypes.data, d.ctypes.data, x.size,
+                                                    hostlib.host_threads())
+            return d
+        from .device import polygon_dist2
+        best = np.empty_like(x)
+        sign = np.empty_like(x)
+        hostlib.lib().bsam_starfish_init_sign(self._h, x.ctypes.data, y.ctypes.data, best.ctypes.data,
+                                              sign.ctypes.data, x.size)
+        polygon_dist2(self.device, self.vertices, x, y, best)
+        return sign * np.sqrt(best)
+
+    def prefetch(self, sets):
+        """Compute the distances of many point sets (pairs of X, Y arrays)
+        in one call -- on every host thread, or in one device launch -- and
+        keep them until the next prefetch, so the per-patch calls that
+        follow are lookups.  Each point's distance is its own minimum over
+        the segments, so the values are the ones a call per set gives."""
+        self._pref = {}
+        xs, ys = [], []
+        for X, Y in sets:
+            xs.append(np.asarray(X, dtype=np.float64).ravel(order='F'))
+            ys.append(np.asarray(Y, dtype=np.float64).ravel(order='F'))
+        if not xs:
+            return
+        d = self._distance(np.ascontiguousarray(np.concatenate(xs)), np.ascontiguousarray(np.concatenate(ys)))
+        o = 0
+        for x, y in zip(xs, ys):
+            x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
+            self._pref[(x.size, hash(x.tobytes()), hash(y.tobytes()))] = (x, y, d[o:o + x.size])
+            o += x.size
 
     def psi(self, X, Y):
         return -self.signedDistance(X, Y)
@@ -138,6 +167,7 @@ def ddTransmissionProblem(geom, epsilon, box, data):
 
     bc = data.get('OuterBC', ('neumann', 0))
     prob = ebProblem(box, D, Cf, Ff, bc, data.get('exact'))
+    prob.prefetch = geom.prefetch       # make_level hands over a level's sample points first
     aux = {'phi': phi, 'delta': delta, 'epsilon': eps, 'signedDistance': geom.signedDistance,
            'vertices': geom.vertices}
     return prob, aux

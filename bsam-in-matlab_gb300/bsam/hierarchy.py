@@ -262,6 +262,21 @@ def make_level(H, k, n, boxes, parents=None):
         lev.parent = (np.zeros(lev.np, dtype=np.int64) if parents is None
                       else np.asarray(parents, dtype=np.int64).reshape(-1))
         lev.mbounds = np.zeros((lev.np, 4), dtype=np.int64)
+    pre = prob.get('prefetch') if isinstance(prob, dict) else None
+    if callable(pre):
+        # a problem whose coefficients share one costly point function (a
+        # geometry's distance) takes every sample point of the level at once;
+        # the per-patch evaluations below are unchanged
+        sets = []
+        hx, hy = lev.h
+        for b in boxes:
+            xf = dom[0] + np.arange(b[0] - 1, b[1] + 1) * hx
+            yc = dom[2] + (np.arange(b[2], b[3] + 1) - 0.5) * hy
+            xc = dom[0] + (np.arange(b[0], b[1] + 1) - 0.5) * hx
+            yf = dom[2] + np.arange(b[2] - 1, b[3] + 1) * hy
+            sets += [np.meshgrid(xf, yc, indexing='ij'), np.meshgrid(xc, yf, indexing='ij'),
+                     np.meshgrid(xc, yc, indexing='ij')]
+        pre(sets)
     for p in range(lev.np):
         b = [int(v) for v in boxes[p]]
         if (b[0] < 1 or b[0] > n[0] or b[1] < 1 or b[1] > n[0] or b[2] < 1 or b[2] > n[1]

@@ -2,6 +2,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -26,9 +27,20 @@ def lib():
         L.bsam_starfish_nvert.argtypes = [P]
         L.bsam_starfish_vertices.argtypes = [P, P]
         L.bsam_starfish_distance.argtypes = [P, P, P, P, I64]
+        L.bsam_starfish_distance_mt.argtypes = [P, P, P, P, I64, C.c_int]
         L.bsam_starfish_init_sign.argtypes = [P, P, P, P, P, I64]
         _lib = L
     return _lib
+
+
+def host_threads():
+    """Host threads for the set-up's point searches: ``BSAM_HOST_THREADS``
+    if set (processes of a builder pool set 1), else the host's cores, at
+    most 16."""
+    v = os.environ.get('BSAM_HOST_THREADS')
+    if v:
+        return max(1, int(v))
+    return max(1, min(16, os.cpu_count() or 1))
 
 
 def _v1(name, x):

@@ -89,6 +89,7 @@ def run_parabolic(spec, backend):
 def _worker_init():
     os.environ['OMP_NUM_THREADS'] = '1'
     os.environ['OPENBLAS_NUM_THREADS'] = '1'
+    os.environ['BSAM_HOST_THREADS'] = '1'       # the pool already uses every core
 
 
 def _warm(_):

@@ -19,6 +19,7 @@
  */
 #include <float.h>
 #include <math.h>
+#include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
 
@@ -178,8 +179,7 @@ static void visit(const Starfish *g, int id, double lb, double x, double y, doub
    distance to the first vertex of the segment its polar angle falls in and
    the distance to the previous point's nearest segment: on grid-ordered
    samples that bound is tight and prunes most of the tree. */
-void bsam_starfish_distance(void *p, const double *X, const double *Y, double *d, int64_t n) {
-  const Starfish *g = (const Starfish *)p;
+static void distance_range(const Starfish *g, const double *X, const double *Y, double *d, int64_t n) {
   const double twopi = 2 * M_PI;
   const int ns = g->ns;
   int prev = 0;
@@ -204,6 +204,55 @@ void bsam_starfish_distance(void *p, const double *X, const double *Y, double *d
     const double s = (hypot(x, y) > radius) ? -1.0 : 1.0;
     d[i] = s * sqrt(best);
   }
+}
+
+void bsam_starfish_distance(void *p, const double *X, const double *Y, double *d, int64_t n) {
+  distance_range((const Starfish *)p, X, Y, d, n);
+}
+
+/* The same distances on up to `threads` host threads, each over a
+   contiguous range of the points (its own warm-start chain).  A point's
+   result does not depend on the other points, so any split gives the same
+   bits; small calls run on the calling thread. */
+typedef struct {
+  const Starfish *g;
+  const double *X, *Y;
+  double *d;
+  int64_t n;
+} DistJob;
+
+static void *distance_job(void *a) {
+  const DistJob *j = (const DistJob *)a;
+  distance_range(j->g, j->X, j->Y, j->d, j->n);
+  return NULL;
+}
+
+void bsam_starfish_distance_mt(void *p, const double *X, const double *Y, double *d, int64_t n, int threads) {
+  enum { kMaxThreads = 64, kMinPerThread = 2048 };
+  if (threads > kMaxThreads) threads = kMaxThreads;
+  if (threads > n / kMinPerThread) threads = (int)(n / kMinPerThread);
+  if (threads <= 1) {
+    distance_range((const Starfish *)p, X, Y, d, n);
+    return;
+  }
+  pthread_t tid[kMaxThreads];
+  DistJob job[kMaxThreads];
+  int started[kMaxThreads];
+  for (int t = 0; t < threads; ++t) {
+    const int64_t lo = n * t / threads, hi = n * (t + 1) / threads;
+    job[t].g = (const Starfish *)p;
+    job[t].X = X + lo;
+    job[t].Y = Y + lo;
+    job[t].d = d + lo;
+    job[t].n = hi - lo;
+    /* thread 0's range runs on the calling thread; a range whose thread
+       cannot be started runs there too */
+    started[t] = t > 0 && pthread_create(&tid[t], NULL, distance_job, &job[t]) == 0;
+  }
+  for (int t = 0; t < threads; ++t)
+    if (!started[t]) distance_job(&job[t]);
+  for (int t = 1; t < threads; ++t)
+    if (started[t]) pthread_join(tid[t], NULL);
 }
 
 /* The O(n) parts of bsam_starfish_distance for a device minimum: per point

@@ -99,3 +99,41 @@ def test_distance_equals_brute_force_in_any_point_order(order):
         px, py = dxa - t * e[j, 0], dya - t * e[j, 1]
         best = np.minimum(best, px * px + py * py)
     np.testing.assert_array_equal(np.abs(d), np.sqrt(best))
+
+
+def test_level_prefetch_builds_the_same_hierarchy(monkeypatch):
+    """make_level hands a level's sample points to the geometry first; the
+    hierarchy (every uploaded table) is the one the per-patch calls build."""
+    import warnings
+    from bsam import ebOptions
+    from bsam.ddm import ddTransmissionProblem, starfish_q, starfish_h, starfish_tag
+    from bsam.flat import flatten
+    from bsam.solve import build_hierarchy
+    from bsam_oracle import OracleBackend
+    data = {'alpha': 3, 'beta': 2, 'gamma': 1, 'kappa': 0.01, 'q': starfish_q, 'h': starfish_h, 'g': 4}
+    fls = []
+    for pre, threads in ((True, '4'), (False, '1')):
+        monkeypatch.setenv('BSAM_HOST_THREADS', threads)
+        g = StarGeometry(3000, 0.9, 1.2, 0.7, 5.0, 0.0)
+        prob, _ = ddTransmissionProblem(g, 0.05, [-2, 2, -2, 2], data)
+        if not pre:
+            del prob['prefetch']
+        opts = ebOptions('BaseCells', 64, 'MaxLevels', 3, 'Indicator', 'fun', 'TagFunction', starfish_tag(g),
+                         'TagBuffer', 2, 'Verbose', 0)
+        with warnings.catch_warnings():
+            warnings.simplefilter('ignore')
+            fls.append(flatten(build_hierarchy(prob, opts, OracleBackend())))
+    a, b = fls
+    for name, v in vars(a).items():
+        if isinstance(v, np.ndarray):
+            np.testing.assert_array_equal(v, getattr(b, name), err_msg=name)
+
+
+def test_threaded_distance_equals_serial(monkeypatch):
+    g = StarGeometry(3000, 1.1, 1.0, 0.6, 3.0, 2.1)
+    X, Y = _points(300000, seed=5)
+    monkeypatch.setenv('BSAM_HOST_THREADS', '1')
+    d1 = g._distance(np.ascontiguousarray(X), np.ascontiguousarray(Y))
+    monkeypatch.setenv('BSAM_HOST_THREADS', '7')
+    d7 = g._distance(np.ascontiguousarray(X), np.ascontiguousarray(Y))
+    np.testing.assert_array_equal(d1, d7)
