@@ -159,15 +159,20 @@ def sub2ind(m, i, j):
     return (np.asarray(i) - 1) + (np.asarray(j) - 1) * m
 
 
-def _evalgrid(fh, X, Y):
+def _eid(tree, tail):
+    """Error identifier: the tree copies (EllipticBSAMTree) raise ``ebt_*``."""
+    return ('ebt_' if tree else 'eb_') + tail
+
+
+def _evalgrid(fh, X, Y, tree=False):
     v = fh(X, Y)
     if np.isscalar(v) or np.ndim(v) == 0:
         v = float(v) * np.ones(X.shape)
     v = np.asarray(v, dtype=np.float64)
     if v.shape != X.shape:
-        raise ValueError('eb_make_level:eval: coefficient function returned wrong size.')
+        raise ValueError(_eid(tree, 'make_level:eval: coefficient function returned wrong size.'))
     if not np.all(np.isfinite(v)):
-        raise ValueError('eb_make_level:eval: coefficient function returned non-finite values.')
+        raise ValueError(_eid(tree, 'make_level:eval: coefficient function returned non-finite values.'))
     return np.asfortranarray(v)
 
 
@@ -182,16 +187,16 @@ def _gauss_legendre(n):
     return d[idx], 2 * V[0, idx] ** 2
 
 
-def _srcquad(fh, XC, YC, hx, hy, nq):
+def _srcquad(fh, XC, YC, hx, hy, nq, tree=False):
     """``srcquad`` (``ebMakeLevel.m:108-131``)."""
     if nq <= 1:
-        return _evalgrid(fh, XC, YC)
+        return _evalgrid(fh, XC, YC, tree)
     xi, w = _gauss_legendre(int(nq))
     w = w / 2
     out = np.zeros(XC.shape, order=F)
     for i in range(int(nq)):
         for j in range(int(nq)):
-            out = out + (w[i] * w[j]) * _evalgrid(fh, XC + xi[i] * hx / 2, YC + xi[j] * hy / 2)
+            out = out + (w[i] * w[j]) * _evalgrid(fh, XC + xi[i] * hx / 2, YC + xi[j] * hy / 2, tree)
     return out
 
 
@@ -281,7 +286,7 @@ def make_level(H, k, n, boxes, parents=None):
         b = [int(v) for v in boxes[p]]
         if (b[0] < 1 or b[0] > n[0] or b[1] < 1 or b[1] > n[0] or b[2] < 1 or b[2] > n[1]
                 or b[3] < 1 or b[3] > n[1] or b[0] > b[1] or b[2] > b[3]):
-            raise ValueError('eb_make_level:box: invalid patch box.')
+            raise ValueError(_eid(H.tree, 'make_level:box: invalid patch box.'))
         if H.tree and k > 1:
             if b[0] % 2 != 1 or b[1] % 2 != 0 or b[2] % 2 != 1 or b[3] % 2 != 0:
                 raise ValueError(f'ebt_make_level:align: patch {p+1} of level {k} not aligned to parent cells.')
@@ -304,16 +309,16 @@ def make_level(H, k, n, boxes, parents=None):
         xc = dom[0] + (np.arange(b[0], b[1] + 1) - 0.5) * hx
         yf = dom[2] + np.arange(b[2] - 1, b[3] + 1) * hy
         XF, YCF = np.meshgrid(xf, yc, indexing='ij')
-        lev.DeW.append(_evalgrid(prob.D, XF, YCF))
+        lev.DeW.append(_evalgrid(prob.D, XF, YCF, H.tree))
         XCF, YF = np.meshgrid(xc, yf, indexing='ij')
-        lev.DnS.append(_evalgrid(prob.D, XCF, YF))
+        lev.DnS.append(_evalgrid(prob.D, XCF, YF, H.tree))
         XC, YC = np.meshgrid(xc, yc, indexing='ij')
-        lev.CC.append(_evalgrid(prob.C, XC, YC))
-        ft = _srcquad(prob.f, XC, YC, hx, hy, H.opts.SourceQuad)
+        lev.CC.append(_evalgrid(prob.C, XC, YC, H.tree))
+        ft = _srcquad(prob.f, XC, YC, hx, hy, H.opts.SourceQuad, H.tree)
         lev.FTrue.append(ft)
         lev.F.append(ft.copy(order=F))
         if np.any(lev.DeW[p] <= 0) or np.any(lev.DnS[p] <= 0):
-            raise ValueError('eb_make_level:D: D(x,y) must be strictly positive at faces.')
+            raise ValueError(_eid(H.tree, 'make_level:D: D(x,y) must be strictly positive at faces.'))
         lev.par0.append((b[0] + b[2]) % 2)
         fint = (b[0] > 1, b[1] < n[0], b[2] > 1, b[3] < n[1])
         lev.faceInternal.append(fint)
@@ -531,7 +536,7 @@ def _resolve_cells(levC, OC, gis, gjs, Il, Jl, cmx, cmy):
     return ops
 
 
-def _corr_face(levC, OC, mask, gis, gjs):
+def _corr_face(levC, OC, mask, gis, gjs, tree=False):
     """``corrFace`` (``ebBuildOps.m:255-281``)."""
     cs = {'mask': mask, 'ops': []}
     idx = np.nonzero(mask)[0]
@@ -541,7 +546,7 @@ def _corr_face(levC, OC, mask, gis, gjs):
     gj = np.broadcast_to(np.asarray(gjs), mask.shape)[idx].astype(np.int64)
     dp = OC[gi - 1, gj - 1].astype(np.int64)
     if (dp == 0).any():
-        raise ValueError('eb_build_ops:corr: mass-correction target cell uncovered.')
+        raise ValueError(_eid(tree, 'build_ops:corr: mass-correction target cell uncovered.'))
     qb = np.asarray(levC.box, dtype=np.int64)[dp - 1]
     dst = sub2ind(qb[:, 1] - qb[:, 0] + 1, gi - qb[:, 0] + 1, gj - qb[:, 2] + 1)
     for q in np.unique(dp):
@@ -572,10 +577,10 @@ def build_ops(H, k):
             ops['win'] = [Il, Ih + 2, Jl, Jh + 2]
             ops['tree'] = True
             fpg = [(ilo + 1) // 2, ihi // 2, (jlo + 1) // 2, jhi // 2]
-            ops['corrW'] = _corr_face(levC, OC, land['W'][1::2] == 3, fpg[0] - 1, np.arange(fpg[2], fpg[3] + 1))
-            ops['corrE'] = _corr_face(levC, OC, land['E'][1::2] == 3, fpg[1] + 1, np.arange(fpg[2], fpg[3] + 1))
-            ops['corrS'] = _corr_face(levC, OC, land['S'][1::2] == 3, np.arange(fpg[0], fpg[1] + 1), fpg[2] - 1)
-            ops['corrN'] = _corr_face(levC, OC, land['N'][1::2] == 3, np.arange(fpg[0], fpg[1] + 1), fpg[3] + 1)
+            ops['corrW'] = _corr_face(levC, OC, land['W'][1::2] == 3, fpg[0] - 1, np.arange(fpg[2], fpg[3] + 1), True)
+            ops['corrE'] = _corr_face(levC, OC, land['E'][1::2] == 3, fpg[1] + 1, np.arange(fpg[2], fpg[3] + 1), True)
+            ops['corrS'] = _corr_face(levC, OC, land['S'][1::2] == 3, np.arange(fpg[0], fpg[1] + 1), fpg[2] - 1, True)
+            ops['corrN'] = _corr_face(levC, OC, land['N'][1::2] == 3, np.arange(fpg[0], fpg[1] + 1), fpg[3] + 1, True)
             levF.ops[p] = ops
             continue
         Il, Ih, Jl, Jh = (ilo + 1) // 2, ihi // 2, (jlo + 1) // 2, jhi // 2
@@ -689,6 +694,9 @@ def gather_parent_coeffs(H):
         for p in range(levF.np):
             PDeW, PDnS, _ = parent_coeffs(H, k, p)
             if np.any(np.isnan(PDeW)) or np.any(np.isnan(PDnS)):
+                if H.tree:
+                    raise ValueError(f'ebt_gather_parent_coeffs:size: parent coefficient window of patch {p+1} '
+                                     f'level {k} has wrong size.')
                 raise ValueError(f'eb_gather_parent_coeffs:cover: footprint of patch {p+1} level {k} '
                                  f'not covered by parent level.')
             levF.cfD[p] = {'W': PDeW[0, :].copy(), 'E': PDeW[-1, :].copy(),

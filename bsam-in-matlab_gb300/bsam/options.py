@@ -99,4 +99,13 @@ def ebOptions(*args, **kwargs) -> Options:
     return opts
 
 
-ebtOptions = ebOptions
+def ebtOptions(*args, **kwargs) -> Options:
+    """``ebtOptions`` (``EllipticBSAMTree/src/ebtOptions.m``): the same
+    options; its errors carry the tree identifiers (``ebt_options:*``)."""
+    try:
+        return ebOptions(*args, **kwargs)
+    except ValueError as e:
+        m = str(e)
+        if m.startswith('eb_options:'):
+            raise ValueError('ebt_' + m[3:]) from None
+        raise

@@ -60,4 +60,13 @@ def ebProblem(domain, D, C, f, bc, exact=None) -> Problem:
     return prob
 
 
-ebtProblem = ebProblem
+def ebtProblem(domain, D, C, f, bc, exact=None) -> Problem:
+    """``ebtProblem`` (``EllipticBSAMTree/src/ebtProblem.m``): the same
+    problem; its errors carry the tree identifiers (``ebt_problem:*``)."""
+    try:
+        return ebProblem(domain, D, C, f, bc, exact)
+    except ValueError as e:
+        m = str(e)
+        if m.startswith('eb_problem:'):
+            raise ValueError('ebt_' + m[3:]) from None
+        raise

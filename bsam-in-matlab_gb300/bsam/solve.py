@@ -15,7 +15,7 @@ import math
 import numpy as np
 
 from . import hierarchy as hier
-from .options import ebOptions
+from .options import ebOptions, ebtOptions
 from .tagcluster import tag_cluster
 
 
@@ -76,10 +76,11 @@ def build_hierarchy(prob, opts, backend, tree=False):
 
 
 def _solve(prob, args, kwargs, tree, backend):
+    parse = ebtOptions if tree else ebOptions
     if len(args) == 1 and isinstance(args[0], dict) and not kwargs:
-        opts = ebOptions(args[0])
+        opts = parse(args[0])
     else:
-        opts = ebOptions(*args, **kwargs)
+        opts = parse(*args, **kwargs)
     backend = backend or default_backend(opts)
     H = hier.setup(prob, opts, backend, tree=tree)
     if str(opts.Indicator).lower() == 'fun':
@@ -140,6 +141,8 @@ def error_norms(H, ufun=None):
     of the visible cells against the exact solution; the singular
     all-Neumann problem is compared modulo its composite mean."""
     ufun = ufun or H.prob.exact
+    if ufun is None:
+        raise ValueError(('ebt' if H.tree else 'eb') + '_error_norms:noexact: no exact solution available.')
     dom = H.prob.domain
     E = {}
     for k in range(H.rootIdx, H.nlev + 1):

@@ -210,7 +210,7 @@ def _grow_min(boxes, allowed, minW, n):
     return boxes
 
 
-def _merge_or_drop_thin(boxes, allowed):
+def _merge_or_drop_thin(boxes, allowed, tree=False):
     """``mergeOrDropThin`` (``ebTagCluster.m:299-356``)."""
     boxes = [list(b) for b in boxes]
 
@@ -261,8 +261,8 @@ def _merge_or_drop_thin(boxes, allowed):
             merged = True
             break
         if not merged:
-            warnings.warn('eb_tag_cluster:dropthin: dropping an ungrowable sliver cluster box '
-                          '(less local refinement)', RuntimeWarning, stacklevel=2)
+            warnings.warn(('ebt' if tree else 'eb') + '_tag_cluster:dropthin: dropping an ungrowable sliver '
+                          'cluster box (less local refinement)', RuntimeWarning, stacklevel=2)
             del boxes[b]
     return boxes
 
@@ -316,7 +316,7 @@ def tag_cluster(H, backend=None):
         b = [int(v) for v in lev.box[p]]
         if ind == 'fun':
             if opts.TagFunction is None:
-                raise ValueError('eb_tag_cluster:tagfun: Indicator=fun needs TagFunction.')
+                raise ValueError(('ebt' if H.tree else 'eb') + '_tag_cluster:tagfun: Indicator=fun needs TagFunction.')
             xc = dom[0] + (np.arange(b[0], b[1] + 1) - 0.5) * lev.h[0]
             yc = dom[2] + (np.arange(b[2], b[3] + 1) - 0.5) * lev.h[1]
             XC, YC = np.meshgrid(xc, yc, indexing='ij')
@@ -341,7 +341,7 @@ def tag_cluster(H, backend=None):
                 thr = thr(k - H.rootIdx + 1)
             tp = s > thr
         else:
-            raise ValueError(f'eb_tag_cluster:ind: unknown Indicator {opts.Indicator}')
+            raise ValueError(('ebt' if H.tree else 'eb') + f'_tag_cluster:ind: unknown Indicator {opts.Indicator}')
         T[b[0] - 1:b[1], b[2] - 1:b[3]] |= tp
     cover = np.zeros((n[0], n[1]), dtype=bool)
     for p in range(lev.np):
@@ -372,7 +372,7 @@ def tag_cluster(H, backend=None):
         bq = _br_cluster(Tq, minW, eff)
         bq = _clip_allowed(bq, Tq, Aq)
         bq = _grow_min(bq, Aq, minW, nq)
-        bq = _merge_or_drop_thin(bq, Aq)
+        bq = _merge_or_drop_thin(bq, Aq, True)
         for bb in bq:
             out.append([q + 1, bb[0] + b[0] - 1, bb[1] + b[0] - 1, bb[2] + b[2] - 1, bb[3] + b[2] - 1])
     return np.array(out, dtype=np.int64).reshape(-1, 5)

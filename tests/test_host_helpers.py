@@ -87,3 +87,47 @@ def test_deepcopy_of_a_hierarchy_leaves_its_device_copy_behind():
     ctx = NoContext.__new__(NoContext)
     with pytest.raises(TypeError, match='bsam_device:copy'):
         copy.copy(ctx)
+
+
+@pytest.mark.parametrize('tree', [False, True])
+def test_error_norms_without_exact_solution(tree):
+    """ebErrorNorms.m:14-16 / ebtErrorNorms: no exact solution is an error."""
+    from bsam import ebOptions, ebProblem, hierarchy as hier
+    from bsam.solve import error_norms
+    from bsam_oracle import OracleBackend
+    H = hier.setup(ebProblem([0, 1, 0, 1], 1, 1, 1, ('dirichlet', 0)), ebOptions('BaseCells', 16, 'Verbose', 0),
+                   OracleBackend(), tree=tree)
+    with pytest.raises(ValueError, match=('ebt' if tree else 'eb') + '_error_norms:noexact'):
+        error_norms(H)
+    assert error_norms(H, lambda x, y: 0 * x)['linf'] == 0.0
+
+
+@pytest.mark.parametrize('tree', [False, True])
+def test_error_identifiers_follow_the_hierarchy_form(tree):
+    """The tree copies raise ``ebt_*`` identifiers (ebtProblem.m, ebtOptions.m,
+    ebtMakeLevel.m, ebtTagCluster.m), the QC-ring code ``eb_*``."""
+    from bsam import ebOptions, ebtOptions, ebProblem, ebtProblem, ebSolve, ebtSolve, hierarchy as hier
+    from bsam.tagcluster import tag_cluster
+    from bsam_oracle import OracleBackend
+    pre = 'ebt_' if tree else 'eb_'
+    mkprob, mkopts, solve = (ebtProblem, ebtOptions, ebtSolve) if tree else (ebProblem, ebOptions, ebSolve)
+    with pytest.raises(ValueError, match=pre + 'problem:domain'):
+        mkprob([1, 0, 0, 1], 1, 1, 1, ('dirichlet', 0))
+    with pytest.raises(ValueError, match=pre + 'options:ghost'):
+        mkopts('GhostInterp', 'cubic')
+    prob = mkprob([0, 1, 0, 1], 1, 1, 1, ('dirichlet', 0))
+    with pytest.raises(ValueError, match=pre + 'options:ghost'):
+        solve(prob, 'GhostInterp', 'cubic', 'Verbose', 0, backend=OracleBackend())
+    with pytest.raises(ValueError, match=pre + 'make_level:D'):
+        hier.setup(mkprob([0, 1, 0, 1], lambda x, y: 0 * x, 1, 1, ('dirichlet', 0)),
+                   mkopts('BaseCells', 16, 'Verbose', 0), OracleBackend(), tree=tree)
+    with pytest.raises(ValueError, match=pre + 'make_level:eval'):
+        hier.setup(mkprob([0, 1, 0, 1], 1, lambda x, y: x[:1], 1, ('dirichlet', 0)),
+                   mkopts('BaseCells', 16, 'Verbose', 0), OracleBackend(), tree=tree)
+    H = hier.setup(prob, mkopts('BaseCells', 16, 'MaxLevels', 2, 'Indicator', 'fun', 'Verbose', 0), OracleBackend(),
+                   tree=tree)
+    with pytest.raises(ValueError, match=pre + 'tag_cluster:tagfun'):
+        tag_cluster(H, OracleBackend())
+    H.opts.Indicator = 'gradient'
+    with pytest.raises(ValueError, match=pre + 'tag_cluster:ind'):
+        tag_cluster(H, OracleBackend())
