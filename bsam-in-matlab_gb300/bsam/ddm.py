@@ -146,12 +146,26 @@ def ddTransmissionProblem(geom, epsilon, box, data):
         if data[f] < 0:
             raise ValueError(f'dd_transmission:{f}: {f} must be nonnegative')
     eps = float(epsilon)
+    recent = []            # (X, Y, phi, delta) of the last point sets: D, C and F sample the same points
+
+    def _fields(X, Y):
+        X = np.asarray(X, dtype=np.float64)
+        Y = np.asarray(Y, dtype=np.float64)
+        for XX, YY, ph, de in recent:
+            if XX.shape == X.shape and np.array_equal(XX, X) and np.array_equal(YY, Y):
+                return ph, de
+        d = geom.signedDistance(X, Y)
+        ph = (1 + hostlib.tanh(d / eps)) / 2
+        de = (1.0 / hostlib.cosh(d / eps)) ** 2 / (2 * eps)
+        recent.insert(0, (X.copy(), Y.copy(), ph, de))
+        del recent[3:]
+        return ph, de
 
     def phi(X, Y):
-        return (1 + hostlib.tanh(geom.signedDistance(X, Y) / eps)) / 2
+        return _fields(X, Y)[0].copy()
 
     def delta(X, Y):
-        return (1.0 / hostlib.cosh(geom.signedDistance(X, Y) / eps)) ** 2 / (2 * eps)
+        return _fields(X, Y)[1].copy()
 
     q, h, g = _tofun(data['q']), _tofun(data['h']), _tofun(data['g'])
     al, be, ga, ka = float(data['alpha']), float(data['beta']), float(data['gamma']), float(data['kappa'])
