@@ -177,12 +177,30 @@ def ddProblem(geom, eps, box, bctype, data, PhiFloor=1e-8, Mu=1.0, OuterBC=('neu
     eps = float(eps)
     Dfun, ffun, gfun = _tof(_get(data, 'D', 1)), _tof(_get(data, 'f', 0)), _tof(_get(data, 'g', 0))
     psi = geom.psi
+    recent = []            # the last point sets: D, C and f sample the same points
+
+    def _entry(X, Y):
+        X = np.asarray(X, dtype=np.float64)
+        Y = np.asarray(Y, dtype=np.float64)
+        for e in recent:
+            if e['X'].shape == X.shape and np.array_equal(e['X'], X) and np.array_equal(e['Y'], Y):
+                return e
+        e = {'X': X.copy(), 'Y': Y.copy(), 'psi': np.asarray(psi(X, Y), dtype=np.float64)}
+        recent.insert(0, e)
+        del recent[3:]
+        return e
 
     def phi(X, Y):
-        return 0.5 * (1 - hostlib.tanh(3 * psi(X, Y) / eps))
+        e = _entry(X, Y)
+        if 'phi' not in e:
+            e['phi'] = 0.5 * (1 - hostlib.tanh(3 * e['psi'] / eps))
+        return e['phi'].copy()
 
     def gphimag(X, Y):
-        return (3 / (2 * eps)) * (1.0 / hostlib.cosh(3 * psi(X, Y) / eps)) ** 2 * geom.gpsimag(X, Y)
+        e = _entry(X, Y)
+        if 'gpm' not in e:
+            e['gpm'] = (3 / (2 * eps)) * (1.0 / hostlib.cosh(3 * e['psi'] / eps)) ** 2 * geom.gpsimag(X, Y)
+        return e['gpm'].copy()
 
     def phifl(X, Y):
         return np.maximum(phi(X, Y), PhiFloor)
