@@ -5,7 +5,7 @@ from bsam import ebProblem
 
 
 def config1_problem(tree=False):
-    """README elliptic example (README.md: -Laplace(u) + u = f, Dirichlet 0)."""
+    """The reference's README elliptic example (its top-level README.md: -Laplace(u) + u = f, Dirichlet 0)."""
     u = lambda x, y: np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y)
     f = lambda x, y: (1 + 8 * np.pi ** 2) * u(x, y)
     return ebProblem([0, 1, 0, 1], 1, 1, f, ('dirichlet', 0), u)
