@@ -70,10 +70,13 @@ def test_restrict_prolong_affine():
     assert np.max(np.abs(lev.QC[0][1:-1, 1:-1] - aff(Xc, Yc))) <= 1e-13
 
 
-def test_uniform_vcycle_matches_direct():
-    """unitKernels.m:80-89: uniform 64^2, RelTol 1e-11: rel <= 1e-11, err <= 5e-3."""
-    sol = ebSolve(vardc_problem(), 'BaseCells', 64, 'MaxLevels', 1, 'Verbose', 0, 'RelTol', 1e-11,
-                  backend=OracleBackend())
+@pytest.mark.parametrize('tree', [False, True])
+def test_uniform_vcycle_matches_direct(tree):
+    """unitKernels.m:80-89 (tree copy unitTreeKernels.m): uniform 64^2, RelTol
+    1e-11: rel <= 1e-11, err <= 5e-3."""
+    from bsam import ebtSolve
+    sol = (ebtSolve if tree else ebSolve)(vardc_problem(), 'BaseCells', 64, 'MaxLevels', 1, 'Verbose', 0,
+                                          'RelTol', 1e-11, backend=OracleBackend())
     st = sol['stats']['stages'][0]
     assert st['finalRel'] <= 1e-11
     assert sol['err']['linf'] <= 5e-3
