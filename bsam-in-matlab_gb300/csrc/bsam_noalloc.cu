@@ -3,9 +3,12 @@
 // Some callers cannot call cudaMalloc: a host that hands the library memory
 // from its own pool (a MATLAB gpuArray, a framework's caching allocator), or
 // code that must not allocate while it runs.  bsam_patch_residual_noalloc
-// evaluates the composite residual norms of one patch (ebCompResidual.m:54-83
-// for a single-patch level: r = FTrue - op2d(Q) over the cells not covered by
-// a finer level) on caller-owned device arrays.  Its block-reduction scratch
+// evaluates the plain residual norms of one patch on caller-owned device
+// arrays: r = FTrue - op2d(Q) (ebKernels.m:13-25) over the cells whose
+// `covered` byte is 0, with linf, l2, fnorm and rel formed as in
+// ebCompResidual.m:66-83.  It adds no coarse-fine flux corrections
+// (ebCompResidual.m:40-65), so it equals the reference's composite residual
+// only for a patch that no finer level touches.  Its block-reduction scratch
 // is the file-scope device array below, so the call performs no device
 // allocation of any kind.
 //
@@ -17,14 +20,15 @@
 // it and must be serialised by the caller.
 //
 // Host code must not pass the array's name to a kernel: on the host the
-// symbol is a stand-in, not a device address.  The device address comes from
-// cudaGetSymbolAddress, taken once per device (with that device current) by
-// the first call made on that device; make that first call before any
-// stream capture.
+// symbol is a stand-in, not a device address.  Every call looks the device
+// address up with cudaGetSymbolAddress for the current device (a host-side
+// lookup that enqueues no work), so the address stays right after a device
+// reset, which reloads the library's device code in a new context.  The
+// first call on a device may load that code; make it before any stream
+// capture.
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <mutex>
 #include <string>
 
 #include "bsam_dev.h"
@@ -36,14 +40,10 @@ int bsam_internal_set_error(int code, const std::string &msg);
 namespace {
 
 constexpr int kMaxBlocks = BSAM_NOALLOC_MAX_BLOCKS;
-constexpr int kMaxDevices = 64;
 
 // [0..kMaxBlocks) per-block L2 partials; [kMaxBlocks] linf bits,
 // [kMaxBlocks+1] fnorm bits, [kMaxBlocks+2] visible-cell count
 static __device__ __align__(256) double g_noalloc_scratch[kMaxBlocks + 4];
-
-std::mutex g_mu;
-double *g_scratch_addr[kMaxDevices] = {nullptr};
 
 __global__ void k_noalloc_clear(double *scratch) {
   unsigned long long *w = reinterpret_cast<unsigned long long *>(scratch + kMaxBlocks);
@@ -90,6 +90,12 @@ __global__ void __launch_bounds__(bsam::kBlock) k_noalloc_residual(const double 
       Fn = fmax(Fn, s_fn[i]);
       N = N + s_nv[i];
     }
+    // fmax drops a NaN operand, so L (Fn) is NaN only when every value of
+    // the block was; a NaN then counts as 0, like MATLAB's max, which
+    // ignores NaN (the bit-pattern maximum below would otherwise rank it
+    // above +Inf)
+    if (!(L >= 0.0)) L = 0.0;
+    if (!(Fn >= 0.0)) Fn = 0.0;
     unsigned long long *acc = reinterpret_cast<unsigned long long *>(scratch + kMaxBlocks);
     atomicMax(acc + 0, (unsigned long long)__double_as_longlong(L));
     atomicMax(acc + 1, (unsigned long long)__double_as_longlong(Fn));
@@ -121,21 +127,13 @@ bool pow2(double x) {
   return x > 0 && std::frexp(x, &e) == 0.5;
 }
 
-// device address of the scratch array on the current device (taken once)
+// device address of the scratch array on the current device, looked up on
+// every call (the address belongs to the device's current context)
 int scratch_for_current_device(double **out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return nerr(BSAM_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return nerr(BSAM_ERR_ARG, "device ordinal beyond the supported range");
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess)
-      return nerr(BSAM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_scratch_addr[dev] = static_cast<double *>(p);
-  }
-  *out = g_scratch_addr[dev];
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return nerr(BSAM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  *out = static_cast<double *>(p);
   return BSAM_OK;
 }
 

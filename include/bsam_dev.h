@@ -258,24 +258,6 @@ int bsam_relax_tuning(bsam_hier h, int precision, int32_t *cells_per_thread, int
 /* Number of kernels one V-cycle (+ fill-down + residual) launches. */
 int bsam_kernels_per_vcycle(bsam_hier h, int64_t *count);
 
-/* Residual norms of one patch on caller-owned device memory, with no device
- * allocation at all.  No counterpart in the reference: it serves callers
- * that cannot call cudaMalloc -- a host that lends the library memory from
- * its own pool (a MATLAB gpuArray, a framework's caching allocator) or code
- * that must not allocate while it runs.  Computes, like ebCompResidual.m:54-83
- * for a single-patch level, r = FTrue - op2d(Q) over the cells whose
- * `covered` byte is 0 (covered may be NULL), and writes
- * out[0..4] = {linf, l2, fnorm, rel, ncell} to DEVICE memory `out`.
- * Q is the padded (mx+2)x(my+2) solution, FTrue/CC/covered mx*my, DeW
- * (mx+1)*my, DnS mx*(my+1), all column-major device arrays; `stream` is a
- * cudaStream_t (NULL = legacy default stream); the call is asynchronous.
- * Its reduction scratch is one static device array of
- * BSAM_NOALLOC_MAX_BLOCKS + 4 doubles (128 KiB) held by every GPU that loads
- * the library until exit, so mx*my is limited to BSAM_NOALLOC_MAX_BLOCKS*256
- * cells (BSAM_ERR_ARG beyond).  All calls share that array: calls that
- * overlap on the GPU race and must be serialised by the caller.  The first
- * call on each device looks up the array's device address with that device
- * current; make it before any stream capture. */
 /* Diffuse-domain coefficient sampling on the device (the O(n x segments)
  * part of DiffuseDomainBSAM/src/ddStarfishGeometry.m:140-177): for each of
  * the n points (x[i], y[i]), best[i] <- min(best[i], min_j dd_j) where dd_j
@@ -287,6 +269,28 @@ int bsam_kernels_per_vcycle(bsam_hier h, int64_t *count);
 int bsam_polygon_dist2(bsam_ctx ctx, const double *verts, int nverts, const double *x, const double *y, double *best,
                        int64_t n);
 
+/* Residual norms of one patch on caller-owned device memory, with no device
+ * allocation at all.  No counterpart in the reference: it serves callers
+ * that cannot call cudaMalloc -- a host that lends the library memory from
+ * its own pool (a MATLAB gpuArray, a framework's caching allocator) or code
+ * that must not allocate while it runs.  Computes the PLAIN residual
+ * r = FTrue - op2d(Q) (ebKernels.m:13-25) over the cells whose `covered`
+ * byte is 0 (covered may be NULL) and writes out[0..4] = {linf, l2, fnorm,
+ * rel, ncell} (formed as in ebCompResidual.m:66-83) to DEVICE memory `out`.
+ * It adds no coarse-fine flux corrections (ebCompResidual.m:40-65), so it
+ * equals the reference's composite residual only for a patch that no finer
+ * level touches.  The max-norms ignore NaN values, as MATLAB's max does.
+ * Q is the padded (mx+2)x(my+2) solution, FTrue/CC/covered mx*my, DeW
+ * (mx+1)*my, DnS mx*(my+1), all column-major device arrays; `stream` is a
+ * cudaStream_t (NULL = legacy default stream); the call is asynchronous.
+ * Its reduction scratch is one static device array of
+ * BSAM_NOALLOC_MAX_BLOCKS + 4 doubles (128 KiB) held by every GPU that loads
+ * the library until exit, so mx*my is limited to BSAM_NOALLOC_MAX_BLOCKS*256
+ * = 4,194,304 cells (BSAM_ERR_ARG beyond).  All calls share that array:
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * Each call looks up the array's device address for the current device
+ * (valid after a device reset too); the first call on a device may load the
+ * library's device code, so make it before any stream capture. */
 #define BSAM_NOALLOC_MAX_BLOCKS 16384
 int bsam_patch_residual_noalloc(const double *Q, const double *FTrue, const double *DeW, const double *DnS,
                                 const double *CC, const uint8_t *covered, int mx, int my, double hx, double hy,
