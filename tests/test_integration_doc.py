@@ -1,4 +1,4 @@
-"""The MEX gateway that INTEGRATION.md gives a MATLAB maintainer compiles
+"""The MEX gateway source (bsam-in-matlab_gb300/mex/bsam_mex.cpp) compiles
 against include/bsam_dev.h (a syntax check with g++: MATLAB's mex.h is not
 installed, so the handful of MEX API functions the gateway calls are
 declared here with plain C types)."""
@@ -39,14 +39,11 @@ int mexAtExit(void (*)(void));
 def test_mex_gateway_compiles_against_the_header(tmp_path):
     if shutil.which('g++') is None:
         pytest.skip('g++ not available')
-    doc = open(os.path.join(ROOT, 'INTEGRATION.md')).read()
-    sec = doc[doc.index('## 2. The MEX gateway'):]
-    start = sec.index('```cpp') + len('```cpp')
-    code = sec[start:sec.index('```', start)]
+    src = os.path.join(ROOT, 'bsam-in-matlab_gb300', 'mex', 'bsam_mex.cpp')
+    code = open(src).read()
     assert 'bsam_hier_upload' in code and 'bsam_solve_cycles' in code
     (tmp_path / 'mex.h').write_text(MEX_DECLS)
-    (tmp_path / 'bsam_mex.cpp').write_text(code)
     out = subprocess.run(['g++', '-std=c++17', '-fsyntax-only', '-Wall', '-Werror', '-I', str(tmp_path), '-I',
-                          os.path.join(ROOT, 'include'), str(tmp_path / 'bsam_mex.cpp')],
+                          os.path.join(ROOT, 'include'), src],
                          capture_output=True, text=True)
     assert out.returncode == 0, out.stderr[-3000:]
