@@ -121,3 +121,21 @@ def scattered_tag():
         hit = np.any((Xv - px[None, :]) ** 2 + (Yv - py[None, :]) ** 2 < 0.0004, axis=1)
         return hit.reshape(np.shape(X), order='F')
     return tag
+
+
+def starfish_config2(backend):
+    """The diffuse-domain starfish of examples/demoStarfish.m:11-20 (64^2 base
+    refined through 5 levels, tag |d| < max(3 eps, 3*4/(64 2^(L-1))), buffer 2,
+    RelTol 1e-10, MaxVCycles 100): the hierarchy of the benchmarked solve,
+    built on `backend`, and its options."""
+    import warnings
+    from bsam import ebOptions
+    from bsam.ddm import starfish_problem, starfish_tag
+    from bsam.solve import build_hierarchy
+    prob, aux, g = starfish_problem()
+    opts = ebOptions('BaseCells', 64, 'MaxLevels', 5, 'Indicator', 'fun', 'TagFunction', starfish_tag(g),
+                     'TagBuffer', 2, 'RelTol', 1e-10, 'MaxVCycles', 100, 'Verbose', 0)
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        H = build_hierarchy(prob, opts, backend)
+    return H, opts
