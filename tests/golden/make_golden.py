@@ -1,8 +1,7 @@
 """Extract the reference's recorded outputs into tests/golden/reference_outputs.json.
 
-Run in a container where the reference repository is mounted (default
-/root/reference, or pass a path).  The reference is MATLAB and cannot run
-here; its own verification run (MATLAB R2026a) recorded these numbers in
+Usage: python make_golden.py <path of the reference repository>.  The
+reference is MATLAB and cannot run here; its own verification run (MATLAB R2026a) recorded these numbers in
 verification/, and they are the golden values the oracle is pinned to.
 """
 import csv
@@ -11,7 +10,9 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+if len(sys.argv) != 2:
+    sys.exit('usage: make_golden.py <path of the reference repository>')
+REF = sys.argv[1]
 VER = os.path.join(REF, 'verification')
 out = {}
 
