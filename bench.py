@@ -37,8 +37,12 @@ composite residual 1e-10 (10 cycles).
 
 `--impl reference` times the reference's CPU path instead: MATLAB is not
 available, so the C oracle restatement runs on all host cores.
-With several ranks (torchrun) every rank solves its own replica; the
-hierarchy does not shard (replicas only).
+With several GPUs (`--gpus N`: the script starts N ranks under
+torch.distributed.run unless it already runs under it) every rank solves its
+own replica of the starfish -- the hierarchy does not shard -- and the
+batching form's instances shard by instance across the ranks; neither has a
+data-path collective, and every rate is the units of all ranks over the
+slowest rank's time.
 """
 import argparse
 import json
@@ -234,29 +238,36 @@ def mixed_form(backend, fl, opts, ref_Q, steps, warmup, flush, local):
             'note': 'error against the FP64 path, which equals the C oracle bit for bit'}
 
 
-def batched_form(backend, n, steps, warmup, flush, local):
+def batched_form(backend, n, steps, warmup, flush, local, dist=None):
     """Batching form: n seeded random elliptic instances (BaseCells
     {32,64,128}, MaxLevels {2,3,4}, TagThreshold 1e-2), each taken through
     ebSolve's solution-driven pipeline to its last stage; that last solve of
     every instance runs (a) alone, one after another (the plain FP64 path),
-    (b) as one batch in FP64, (c) as one batch in the mixed form."""
+    (b) as one batch in FP64, (c) as one batch in the mixed form.  With
+    several ranks the instances shard by instance (rank r takes instances
+    r, r + N, ...), each rank batching its own share with no collective; the
+    rates count every rank's instances over the slowest rank's time."""
     import torch
     import warnings
     from bsam.device import DevHier, BSAM_FIELD_Q
     from bsam.instances import random_elliptic, final_stage
     from bsam.batch import merge_flats, split_field
     from bsam.flat import FIELD_Q, visible_q_index, rel_errors
+    from bsam.replicas import shard, job_rate_units, gather
+    rank = dist.get_rank() if dist else 0
+    world = dist.get_world_size() if dist else 1
+    ids = shard(n, rank, world)
+    dev = torch.device('cuda', local)
     t0 = time.perf_counter()
     parts, opts = [], None
     with warnings.catch_warnings():
         warnings.simplefilter('ignore')
-        for s in range(n):
+        for s in ids:
             prob, o = random_elliptic(1000 + s)
             fl, H = final_stage(prob, o, backend)
             parts.append(fl)
             opts = opts or H.opts
     setup_s = time.perf_counter() - t0
-    dev = torch.device('cuda', local)
     # (a) solo, plain FP64
     solo_ms, solo = [], []
     for p in parts:
@@ -267,12 +278,15 @@ def batched_form(backend, n, steps, warmup, flush, local):
         solo.append((r, dh.get(BSAM_FIELD_Q, p.Q.size)))
         del dh
     solo_total = sum(solo_ms)
+    solo_rate, solo_t = job_rate_units(len(ids), solo_total / 1e3, dist, dev)
+    all_solo = [v for r in gather(solo_ms, dist) for v in r]
     out = {'workload': f'{n} seeded random elliptic instances on [0,1]^2 (log D: 16 Fourier modes, C in [0,1], '
                        f'f: 4 Gaussian bumps; BaseCells {{32,64,128}}, MaxLevels {{2,3,4}}, TagThreshold 1e-2), '
                        f'last ebSolve stage of each, RelTol 1e-10',
-           'instances': n, 'stored_cells': int(sum(p.F.size for p in parts)), 'setup_s': setup_s,
-           'solo_fp64': {'value': n / (solo_total / 1e3), 'unit': 'solves/s', 'ms_total': solo_total,
-                         'p50_ms': float(np.percentile(solo_ms, 50)), 'p99_ms': float(np.percentile(solo_ms, 99))}}
+           'instances': n, 'ranks': world, 'instances_per_rank': [len(shard(n, r, world)) for r in range(world)],
+           'stored_cells': int(sum(gather(int(sum(p.F.size for p in parts)), dist))), 'setup_s': setup_s,
+           'solo_fp64': {'value': solo_rate, 'unit': 'solves/s', 'ms_total': 1e3 * solo_t,
+                         'p50_ms': float(np.percentile(all_solo, 50)), 'p99_ms': float(np.percentile(all_solo, 99))}}
     b = merge_flats(parts)
     for prec in ('fp64', 'mixed'):
         ob = opts.copy()
@@ -291,7 +305,11 @@ def batched_form(backend, n, steps, warmup, flush, local):
             else:
                 l2, mx = rel_errors(qi, q, visible_q_index(parts[i]))
                 worst_l2, worst_max = max(worst_l2, l2), max(worst_max, mx)
-        d = {'value': n * steps / (ms.sum() / 1e3), 'unit': 'solves/s', 'ms_per_batch': float(ms.mean()),
+        rate, tmax = job_rate_units(len(ids) * steps, ms.sum() / 1e3, dist, dev)
+        equal = all(gather(bool(equal), dist))
+        maxit = max(gather(maxit, dist))
+        worst_l2, worst_max = max(gather(worst_l2, dist)), max(gather(worst_max, dist))
+        d = {'value': rate, 'unit': 'solves/s', 'ms_per_batch': 1e3 * tmax / steps,
              'p50_ms': float(np.percentile(ms, 50)), 'p99_ms': float(np.percentile(ms, 99)),
              'vcycles_slowest': maxit, 'kernels_per_vcycle': bh.kernels_per_vcycle(),
              'relax_cells_per_thread': bh.relax_tuning(1 if prec == 'mixed' else 0).tolist()}
@@ -399,9 +417,21 @@ def main():
     ap.add_argument('--no-forms', action='store_true', help='skip the mixed, batching and serving forms')
     ap.add_argument('--serve-rates', default='5,10,20', help='offered request rates of the serving form')
     args = ap.parse_args()
+    if 'WORLD_SIZE' not in os.environ and args.gpus > 1 and args.impl == 'native':
+        # one process per GPU: start the ranks under torch.distributed.run
+        import socket
+        sk = socket.socket()
+        sk.bind(('127.0.0.1', 0))
+        port = sk.getsockname()[1]
+        sk.close()
+        os.execv(sys.executable, [sys.executable, '-m', 'torch.distributed.run', '--nnodes=1',
+                                  f'--nproc-per-node={args.gpus}', '--master-addr', '127.0.0.1',
+                                  '--master-port', str(port), os.path.abspath(__file__)] + sys.argv[1:])
     rank = int(os.environ.get('RANK', 0))
     world = int(os.environ.get('WORLD_SIZE', 1))
     local = int(os.environ.get('LOCAL_RANK', 0))
+    if args.impl == 'native' and world != args.gpus:
+        sys.exit(f'bench.py: --gpus {args.gpus} but WORLD_SIZE is {world}: one rank per GPU is required')
     if args.impl == 'reference':
         return run_reference(args, rank, world)
 
@@ -508,7 +538,8 @@ def main():
         forms = {'mixed': mixed_form(backend, fl, opts, ref_Q, args.steps, args.warmup, flush, local)}
         forms['mixed']['speedup_vs_fp64'] = forms['mixed']['value'] / value
         if args.batch > 0:
-            forms['batched'] = batched_form(backend, args.batch, max(3, args.steps // 4), args.warmup, flush, local)
+            forms['batched'] = batched_form(backend, args.batch, max(3, args.steps // 4), args.warmup, flush, local,
+                                            dist)
         forms['parabolic'] = parabolic_form(backend)
         rates = [float(r) for r in args.serve_rates.split(',') if r.strip()]
         if rates and rank == 0:
