@@ -402,8 +402,33 @@ def parabolic_form(backend):
                     'mass_drift_per_step_max': float(np.max(np.abs(np.diff(m)))),
                     'mass_drift_total': float(abs(m[-1] - m[0])),
                     'final_levels': [lv['np'] for lv in sol['levels']]})
+    # a run whose hierarchy keeps three levels through every regrid: the
+    # reference's rotating-source case (ParabolicBSAM/tests/runParabolicTests.m
+    # P3: BDF2, Dt 5e-3, TFinal 1, RegridEvery 4, BaseCells 64, MaxLevels 3,
+    # 'ulap' tagging), history moved device to device at each regrid
+    import warnings
+    from bsam.device import DeviceBackend
+    om, Rc, ss = 2 * np.pi, 0.22, 0.03
+    src = lambda x, y, t: 25 * np.exp(-((x - (0.5 + Rc * np.cos(om * t))) ** 2 +
+                                        (y - (0.5 + Rc * np.sin(om * t))) ** 2) / (2 * ss ** 2))
+    p3 = ebpProblem([0, 1, 0, 1], 1, 0, src, ('dirichlet', 0), lambda x, y: 0 * x)
+    h0 = DeviceBackend.history_downloads
+    t0 = time.perf_counter()
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        sol = ebpSolve(p3, 'Scheme', 'bdf2', 'Dt', 5e-3, 'TFinal', 1.0, 'RegridEvery', 4, 'StepVerbose', 0,
+                       'BaseCells', [64, 64], 'MaxLevels', 3, 'Indicator', 'ulap',
+                       'TagThreshold', lambda L: 2e-3 / 4 ** (L - 1), 'TagBuffer', 3, 'RelTol', 1e-8,
+                       backend=backend)
+    wall = time.perf_counter() - t0
+    rot = {'workload': 'rotating Gaussian source (P3), BDF2, Dt 5e-3, TFinal 1, RegridEvery 4, BaseCells 64, '
+                       'MaxLevels 3, ulap tagging', 'steps': len(sol['cycles']), 'wall_s': wall,
+           'steps_per_s': len(sol['cycles']) / wall, 'vcycles_total': int(np.sum(sol['cycles'])),
+           'max_step_rel': float(np.max(sol['relres'])), 'regrids': sol['nregrids'],
+           'final_levels': [lv['np'] for lv in sol['levels']], 'final_cells': [lv['cells'] for lv in sol['levels']],
+           'history_downloads': DeviceBackend.history_downloads - h0}
     return {'workload': 'README heat example, BDF2, Dt 0.002, TFinal 0.1, RegridEvery 5 (wall time includes the '
-                        'host regrids)', 'runs': out}
+                        'host regrids)', 'runs': out, 'rotating_source': rot}
 
 
 def main():

@@ -103,6 +103,7 @@ def lib():
         L.bsam_setup_levels.argtypes = [P]
         L.bsam_parabolic_rhs.argtypes = [P, C.c_int, D, P, I64]
         L.bsam_history_push.argtypes = [P]
+        L.bsam_history_transfer.argtypes = [P, P, P, I64, C.c_int]
         L.bsam_tag_level.argtypes = [P, C.c_int, C.c_int, D, C.c_int, C.c_int, C.c_int, P]
         _lib = L
     return _lib
@@ -276,6 +277,12 @@ class DevHier:
         if f is not None:
             f = np.ascontiguousarray(f, dtype=np.float64)
         check(lib().bsam_parabolic_rhs(self.h, int(scheme), float(dt), _ptr(f), 0 if f is None else f.size))
+
+    def history_transfer(self, old, src_old, has_uoo):
+        """BDF2 history from the hierarchy `old` (a DevHier on the same
+        device) after a regrid; see bsam_history_transfer."""
+        src = np.ascontiguousarray(src_old, dtype=np.int32)
+        check(lib().bsam_history_transfer(self.h, old.h, src.ctypes.data, src.size, int(bool(has_uoo))))
 
     def history_push(self):
         check(lib().bsam_history_push(self.h))
@@ -492,10 +499,14 @@ class DeviceBackend:
         n = H.lev[H.nlev].n
         return dh.tag_level(H.nlev, indicator, threshold, buffer, n[0], n[1])
 
+    # history downloads so far (a regrid on the device makes none)
+    history_downloads = 0
+
     def history_get(self, H):
         """(Uo, Uoo) as per-patch arrays {(k, p): (mx, my)}."""
         from .flat import PD_COFF, PD_MX, PD_MY
         dh = self.ensure(H)
+        DeviceBackend.history_downloads += 1
         out = []
         for which in (BSAM_FIELD_UO, BSAM_FIELD_UOO):
             v = dh.get(which, dh.fl.F.size)
@@ -506,6 +517,16 @@ class DeviceBackend:
                 d[(k, p)] = v[o:o + mx * my].reshape((mx, my), order='F').copy(order='F')
             out.append(d)
         return out[0], out[1]
+
+    def history_transfer(self, Hn, Hold, has_uoo):
+        """ebpRegrid's history transfer from Hold's resident state to Hn's,
+        on the device (Hn uploaded here; Hold's copy must be current)."""
+        from .parabolic import history_sources
+        cur = getattr(Hold, '_dev', None)
+        if cur is None or cur[0] != Hold.version:
+            raise RuntimeError('bsam_device:state: the old hierarchy is not resident')
+        dn = self.ensure(Hn)
+        dn.history_transfer(cur[1], history_sources(Hn, dn.fl, Hold, cur[1].fl), has_uoo)
 
     def history_set(self, H, Uo, Uoo):
         dh = self.ensure(H)

@@ -331,11 +331,40 @@ def regrid_keeps(H, pprob, aDtNext, backend):
     return tag_cluster(H, backend).shape[0] == 0
 
 
-def ebpRegrid(Hold, pprob, t, aDtNext, opts, backend):
+def history_sources(Hn, fln, Hold, flo):
+    """For every cell of the new hierarchy's flat tables at or above its
+    root: the old hierarchy's flat cell that holds the same cell of the same
+    level (the overwrite of ebpRegrid.m:73-90; the root copies itself,
+    :22-26), or -1 where no old patch covers it."""
+    from .flat import PD_COFF, PD_MX
+    src = np.full(fln.F.size, -1, dtype=np.int32)
+    for k in range(Hn.rootIdx, Hn.nlev + 1):
+        if k > Hold.nlev:
+            break
+        for p in range(Hn.lev[k].np):
+            b = [int(v) for v in Hn.lev[k].box[p]]
+            rn = fln.patches[fln.pglob[(k, p)]]
+            con, mxn = int(rn[PD_COFF]), int(rn[PD_MX])
+            for q in range(Hold.lev[k].np):
+                qb = [int(v) for v in Hold.lev[k].box[q]]
+                r = [max(b[0], qb[0]), min(b[1], qb[1]), max(b[2], qb[2]), min(b[3], qb[3])]
+                if r[0] > r[1] or r[2] > r[3]:
+                    continue
+                ro = flo.patches[flo.pglob[(k, q)]]
+                coo, mxo = int(ro[PD_COFF]), int(ro[PD_MX])
+                i, j = np.meshgrid(np.arange(r[0], r[1] + 1), np.arange(r[2], r[3] + 1), indexing='ij')
+                src[con + (i - b[0]) + (j - b[2]) * mxn] = coo + (i - qb[0]) + (j - qb[2]) * mxo
+    return src
+
+
+def ebpRegrid(Hold, pprob, t, aDtNext, opts, backend, history='host'):
     """``ebpRegrid.m:16-59``: new hierarchy on the current solution, with a
-    conservative transfer of u and the BDF2 history."""
+    conservative transfer of u and the BDF2 history.  history='device': the
+    history stays where it is (resident on the device); the caller moves it
+    with the backend's history_transfer once the new hierarchy is built, and
+    the returned hierarchy carries no host copy of it."""
     Hn = hier.setup(ebpEprob(pprob, t, aDtNext), opts.eb, backend)
-    have_uoo = Hold.par['Uoo'] is not None
+    have_uoo = Hold.par['Uoo'] is not None and history == 'host'
     r = Hn.rootIdx
     Hn.lev[r].Q[0][1:-1, 1:-1] = Hold.lev[r].Q[0][1:-1, 1:-1]
     uoo_n = {}
@@ -382,8 +411,8 @@ def ebpRegrid(Hold, pprob, t, aDtNext, opts, backend):
         backend.run(Hn, [('fill', kN)])
     backend.run(Hn, [('filldown',)])
     td = pprob.tdD or pprob.tdC or pprob.tdBC
-    Hn.par = {'Uo': _interiors(Hn), 'Uoo': uoo_n if have_uoo else None, 'stateKey': (t * td, aDtNext),
-              'aDt': aDtNext}
+    Hn.par = {'Uo': _interiors(Hn) if history == 'host' else None, 'Uoo': uoo_n if have_uoo else None,
+              'stateKey': (t * td, aDtNext), 'aDt': aDtNext}
     Hn.stats = Hold.stats
     return Hn
 
@@ -471,15 +500,22 @@ def ebpSolve(pprob, *args, backend=None, **kwargs):
             print(f'[ebsam-p] step {n:4d}/{nsteps}  t={t1:.4f}  V={cycles[n - 1]}  rel={relres[n - 1]:.1e}  '
                   f'levels={H.nlev - H.rootIdx + 1}  cells={nc}  mass={mass[n]:.6e}')
         if opts.RegridEvery > 0 and n % int(opts.RegridEvery) == 0 and n < nsteps and opts.eb.MaxLevels > 1:
-            if dev:
-                to_host(H)
             aNext = _alpha(opts.Scheme) / Dt
-            if not regrid_keeps(H, pprob, aNext, backend):
+            if dev:
+                # the solution comes to the host for the new hierarchy's
+                # build (tagging, conservative transfer of u); the BDF2
+                # history moves device to device
+                backend.sync_host(H)
+                if not regrid_keeps(H, pprob, aNext, backend):
+                    Hold = H
+                    H = ebpRegrid(Hold, pprob, t1, aNext, opts, backend, history='device')
+                    H.par['resident'] = True
+                    H.par['hasUoo'] = bool(Hold.par.get('hasUoo'))
+                    backend.history_transfer(H, Hold, H.par['hasUoo'])
+                    del Hold
+            elif not regrid_keeps(H, pprob, aNext, backend):
                 H = ebpRegrid(H, pprob, t1, aNext, opts, backend)
             nregrids += 1
-            if dev:
-                H.par['hasUoo'] = H.par['Uoo'] is not None
-                to_device(H)
     if dev:
         to_host(H)
     sol = {'H': H, 't': np.arange(nsteps + 1) * Dt, 'mass': mass, 'cycles': cycles, 'relres': relres,

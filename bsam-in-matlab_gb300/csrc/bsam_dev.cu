@@ -1924,10 +1924,51 @@ int bsam_history_push(bsam_hier h) {
   if (rc || (rc = ensure_history(h))) return rc;
   Decomp D = decomp(h, h->all_cells);
   launch_k(h, k_history, D.nblocks, kBlock, D, (const PatchD *)h->patches.p, (const double *)h->Q.p, h->Uo.p,
-           h->Uoo.p);
+           h->Uoo.p, 1);
   h->launch_count++;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(h->stream));
+  return BSAM_OK;
+}
+
+int bsam_history_transfer(bsam_hier hn, bsam_hier hold, const int32_t *src_old, int64_t n, int has_uoo) {
+  if (!hn || !hold || !src_old) return fail(BSAM_ERR_ARG, "null argument");
+  if (hn == hold) return fail(BSAM_ERR_ARG, "the new and the old hierarchy must differ");
+  if (n != hn->n_cells) return fail(BSAM_ERR_ARG, "source table length mismatch");
+  if (hn->ctx->device != hold->ctx->device) return fail(BSAM_ERR_ARG, "hierarchies on different devices");
+  // every cell at or above the root reads a valid old cell or derives from
+  // its parent; the root has no parent, so every root cell has an old source
+  const int root = std::max(hn->root, 1);
+  for (int k = root; k <= hn->nlev; ++k) {
+    const int64_t c0 = hn->hlevels[(size_t)(k - 1) * LDN + LD_CELL0], c1 = hn->hlevels[(size_t)(k - 1) * LDN + LD_CELL1];
+    for (int64_t c = c0; c < c1; ++c) {
+      if (src_old[c] >= hold->n_cells) return fail(BSAM_ERR_ARG, "source cell beyond the old hierarchy");
+      if (src_old[c] < -1 || (k == root && src_old[c] < 0))
+        return fail(BSAM_ERR_ARG, "root cell without an old source");
+    }
+  }
+  int rc = set_device(hold);
+  if (rc || (rc = ensure_history(hold))) return rc;
+  CK(cudaStreamSynchronize(hold->stream));   // the old history is complete
+  if ((rc = set_device(hn)) || (rc = ensure_history(hn))) return rc;
+  DBuf<int> src;
+  if ((rc = src.upload(src_old, (size_t)n, hn->stream))) return rc;
+  if (has_uoo) {
+    for (int k = root; k <= hn->nlev; ++k) {
+      const LevelPlan &L = hn->lev[k];
+      Decomp D = decomp(hn, L.cell);
+      launch_k(hn, k_uoo_transfer, D.nblocks, kBlock, leveld(hn, k), D, (const int *)hn->fp.p, (const int *)src.p,
+               (const double *)hold->Uoo.p, hn->Uoo.p);
+      hn->launch_count++;
+    }
+  }
+  Decomp D = decomp(hn, hn->all_cells);
+  launch_k(hn, k_history, D.nblocks, kBlock, D, (const PatchD *)hn->patches.p, (const double *)hn->Q.p, hn->Uo.p,
+           hn->Uoo.p, 0);
+  hn->launch_count++;
+  src.release();
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(hn->stream));
   return BSAM_OK;
 }
 

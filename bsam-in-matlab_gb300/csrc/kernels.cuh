@@ -1375,11 +1375,12 @@ __global__ void __launch_bounds__(kBlock) k_update(Decomp D, const PatchD *__res
 }
 
 // Parabolic driver on the device.  k_history: Uoo = Uo, Uo = interior of Q
-// (ebpSolve.m:52-56).  k_prhs: FTrue of the step on the cells of levels at
-// or above the root (ebpRhs.m:25-47): BE f + Uo/Dt, BDF2 f + (2 Uo - 0.5
-// Uoo)/Dt, in that operation order; f null is f = 0.
+// (ebpSolve.m:52-56); with rotate 0 only Uo = interior of Q (the new
+// hierarchy's Uo after a regrid, ebpRegrid.m:49).  k_prhs: FTrue of the step
+// on the cells of levels at or above the root (ebpRhs.m:25-47): BE f + Uo/Dt,
+// BDF2 f + (2 Uo - 0.5 Uoo)/Dt, in that operation order; f null is f = 0.
 __global__ void __launch_bounds__(kBlock) k_history(Decomp D, const PatchD *__restrict__ patches, const double *Q,
-                                                    double *Uo, double *Uoo) {
+                                                    double *Uo, double *Uoo, int rotate) {
   chain_in();
   const int g = blockIdx.x * kBlock + threadIdx.x;
   if (g >= D.n) return;
@@ -1388,8 +1389,45 @@ __global__ void __launch_bounds__(kBlock) k_history(Decomp D, const PatchD *__re
   const int s = g - __ldg(D.beg + p);
   const int lj = s / P.mx, lx = s - lj * P.mx;
   const int cc = P.c_off + s;
-  Uoo[cc] = Uo[cc];
+  if (rotate) Uoo[cc] = Uo[cc];
   Uo[cc] = Q[P.q_off + (lx + 1) + (lj + 1) * (P.mx + 2)];
+}
+
+// The BDF2 history Uoo of one level of a regridded hierarchy
+// (ebpRegrid.m:62-137, transferLevel): where a patch of the old hierarchy
+// on the same level covers the cell (src_old >= 0, an index into the old
+// hierarchy's cells) its old value is copied; elsewhere the value is the
+// conservative-linear prolongation of the new parent level's (already
+// transferred) history over the patch footprint (conslinInterior +
+// parentFootprint: central slopes inside the footprint, one-sided at its
+// edges, none along a footprint one coarse cell wide), in the reference's
+// operation order.  The footprint's parent cells come from the footprint
+// table (second entry per coarse cell); the root level copies every cell.
+__global__ void __launch_bounds__(kBlock) k_uoo_transfer(LevelD L, Decomp D, const int *__restrict__ fp,
+                                                         const int *__restrict__ src_old,
+                                                         const double *__restrict__ uoo_old, double *uoo) {
+  chain_in();
+  const int g = blockIdx.x * kBlock + threadIdx.x;
+  if (g >= D.n) return;
+  const int p = find_patch(D, blockIdx.x, g);
+  const PatchD &P = L.patches[p];
+  const int s = g - __ldg(D.beg + p);
+  const int c = P.c_off + s;
+  const int so = src_old[c];
+  if (so >= 0) {
+    uoo[c] = uoo_old[so];
+    return;
+  }
+  const int mx = P.mx, lj = s / mx, li = s - lj * mx;
+  const int cmx = mx >> 1, cmy = P.my >> 1, ci = li >> 1, cj = lj >> 1;
+  const int *pc = fp + 2 * P.fp_off + 1;      // parent cell of footprint cell t at pc[2 t]
+  auto at = [&](int a, int b) { return uoo[pc[2 * (a + b * cmx)]]; };
+  const double v = at(ci, cj);
+  double sx = 0, sy = 0;
+  if (cmx > 1) sx = ci == 0 ? at(1, cj) - v : (ci == cmx - 1 ? v - at(ci - 1, cj) : (at(ci + 1, cj) - at(ci - 1, cj)) / 2);
+  if (cmy > 1) sy = cj == 0 ? at(ci, 1) - v : (cj == cmy - 1 ? v - at(ci, cj - 1) : (at(ci, cj + 1) - at(ci, cj - 1)) / 2);
+  const double a = (li & 1) ? v + sx / 4 : v - sx / 4;
+  uoo[c] = (lj & 1) ? a + sy / 4 : a - sy / 4;
 }
 
 __global__ void __launch_bounds__(kBlock) k_prhs(Decomp D, const PatchD *__restrict__ patches, double *FTrue,

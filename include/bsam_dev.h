@@ -187,6 +187,20 @@ int bsam_batch_set_stop(bsam_hier h, int inst, int max_vcycles, double rel_tol);
 int bsam_parabolic_rhs(bsam_hier h, int scheme, double dt, const double *f, int64_t n);
 int bsam_history_push(bsam_hier h);
 
+/* The BDF2 history across a regrid, device to device (replaces the history
+ * part of ebpRegrid.m:16-59 and its transferLevel / conslinInterior /
+ * parentFootprint / interiors, :62-162): hn is the new hierarchy (uploaded,
+ * solution already transferred), hold the old one, both resident on the same
+ * device.  src_old[n = hn's cell count] gives for each cell of hn at or
+ * above its root the old hierarchy's cell holding the same cell of the same
+ * level, or -1 where the old hierarchy had no patch there (every root cell
+ * has one).  With has_uoo, level by level from the root up: Uoo(hn) = the old
+ * Uoo where src_old >= 0, else the conservative-linear prolongation of hn's
+ * parent-level Uoo over the patch footprint (one-sided slopes at its edges);
+ * then Uo(hn) = the interior of hn's Q on every level (ebpRegrid.m:49).  No
+ * history value passes through host memory.  Synchronous. */
+int bsam_history_transfer(bsam_hier hn, bsam_hier hold, const int32_t *src_old, int64_t n, int has_uoo);
+
 /* Tagging of the finest level on the device (ebTagCluster.m:50-59 'ulap',
  * indicator 0; ebRte.m:14-41 'rte', indicator 1), on the current solution:
  * tag where the indicator exceeds threshold, dilate by `buffer` cells

@@ -131,3 +131,51 @@ def test_regrid_skip_equals_rebuild_on_device(monkeypatch):
     from bsam.device import DeviceBackend
     hits = _skip_vs_rebuild(DeviceBackend.get(0), 128, 4, monkeypatch)
     assert all(hits)
+
+
+def rotating_source_problem():
+    """P3 of the reference's parabolic suite (ParabolicBSAM/tests/
+    runParabolicTests.m: a Gaussian source circling the centre, Dirichlet 0,
+    u0 = 0): the refinement follows the source, so every regrid rebuilds a
+    three-level hierarchy in a new place."""
+    om, Rc, ss = 2 * np.pi, 0.22, 0.03
+    cx = lambda t: 0.5 + Rc * np.cos(om * t)
+    cy = lambda t: 0.5 + Rc * np.sin(om * t)
+    src = lambda x, y, t: 25 * np.exp(-((x - cx(t)) ** 2 + (y - cy(t)) ** 2) / (2 * ss ** 2))
+    return ebpProblem([0, 1, 0, 1], 1, 0, src, ('dirichlet', 0), lambda x, y: 0 * x)
+
+
+ROTATING_SOURCE_OPTS = ('Scheme', 'bdf2', 'Dt', 5e-3, 'TFinal', 0.2, 'RegridEvery', 4, 'StepVerbose', 0,
+                        'BaseCells', [64, 64], 'MaxLevels', 3, 'Indicator', 'ulap',
+                        'TagThreshold', lambda L: 2e-3 / 4 ** (L - 1), 'TagBuffer', 3, 'RelTol', 1e-8)
+
+
+@pytest.mark.gpu
+def test_regrids_keep_history_on_device():
+    """The rotating-source run's first 40 steps (nine regrids, each onto a
+    moved three-level hierarchy): on the device the BDF2 history goes from
+    the old hierarchy to the new one without passing through host memory
+    (ebpRegrid.m:62-137 as kernels) -- one download of Uo / Uoo in the whole
+    run, for the result.  Per-step V-cycles and residuals, the final field
+    and history equal the oracle pipeline's bit for bit."""
+    import warnings
+    from bsam.device import DeviceBackend
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        a = ebpSolve(rotating_source_problem(), *ROTATING_SOURCE_OPTS, backend=OracleBackend())
+        before = DeviceBackend.history_downloads
+        b = ebpSolve(rotating_source_problem(), *ROTATING_SOURCE_OPTS, backend=DeviceBackend.get(0))
+    assert DeviceBackend.history_downloads - before == 1
+    assert a['nregrids'] == b['nregrids'] == 9
+    assert len(b['levels']) == 3
+    np.testing.assert_array_equal(a['cycles'], b['cycles'])
+    np.testing.assert_array_equal(a['relres'], b['relres'])
+    np.testing.assert_allclose(a['mass'], b['mass'], rtol=1e-13, atol=0)
+    Ha, Hb = a['H'], b['H']
+    assert Ha.nlev == Hb.nlev
+    for k in range(1, Ha.nlev + 1):
+        for qa, qb in zip(Ha.lev[k].Q, Hb.lev[k].Q):
+            np.testing.assert_array_equal(qa[1:-1, 1:-1], qb[1:-1, 1:-1])
+    for kp in Ha.par['Uo']:
+        np.testing.assert_array_equal(Ha.par['Uo'][kp], Hb.par['Uo'][kp])
+        np.testing.assert_array_equal(Ha.par['Uoo'][kp], Hb.par['Uoo'][kp])
