@@ -1168,12 +1168,17 @@ struct Builder {
       auto Q = [&](int i, int j) { return qo + (i - 1) + (j - 1) * (mx + 2); };
       pe_off[p] = (int)perim.size();
       auto add = [&](int side, int dst) -> bool {
-        if (r[PD_BCW + side] != 0) { perim.push_back(Rule{-1, 0, 0, 0, 0, 0}); return true; }
+        if (r[PD_BCW + side] != 0) { perim.push_back(Rule{-1, 0, 0, 0, 0, 0, 0, 0}); return true; }
         const int ri = rule_at(dst);
         if (ri < 0) return false;
         const G &g = tmp[ri];
         if (g.t != G_COPY && g.t != G_QIF && g.t != G_QIF_END && g.t != G_LIF) return false;
-        perim.push_back(Rule{g.t, g.a, g.b, g.c, g.dd, g.e});
+        // operand slots the rule does not read repeat its first operand (the
+        // smoother loads all five before it looks at the kind)
+        Rule R{g.t, g.a, g.b, g.c, g.dd, g.e, 0, 0};
+        if (g.t == G_COPY) R.b = R.c = g.a;
+        if (g.t != G_QIF_END) R.d = R.e = g.a;
+        perim.push_back(R);
         return true;
       };
       bool ok = true;
@@ -1423,7 +1428,7 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
   }
   for (int p = 0; p < d->npatch; ++p) pd[p].pe_off = B.pe_off[p];
   if ((rc = h->patches.upload(pd.data(), pd.size(), s))) return rc;
-  if (B.perim.empty()) B.perim.push_back(Rule{-1, 0, 0, 0, 0, 0});
+  if (B.perim.empty()) B.perim.push_back(Rule{-1, 0, 0, 0, 0, 0, 0, 0});
   std::vector<RelaxChunkD> dchunks(B.chunks.size());
   for (size_t i = 0; i < B.chunks.size(); ++i) {
     const RelaxChunk &c = B.chunks[i];

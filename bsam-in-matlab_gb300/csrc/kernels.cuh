@@ -139,6 +139,20 @@ struct GhostItems {
   const int *inst;             // instance per item (batches only, else null)
 };
 
+// the value of a COPY / QIF / QIF_END / LIF rule from its five operands
+template <class T>
+__device__ __forceinline__ T rule_value(int type, T qa, T qb, T qc, T qd, T qe) {
+  const T A1 = T(-1.0 / 5.0), A2 = T(2.0 / 3.0), A3 = T(8.0 / 15.0);
+  const T B1 = T(5.0 / 32.0), B2 = T(15.0 / 16.0), B3 = T(-3.0 / 32.0);
+  const T c23 = T(2.0 / 3.0), c13 = T(1.0 / 3.0);
+  switch (type) {
+    case G_COPY: return qa;
+    case G_QIF: return (A1 * qa + A2 * qb) + A3 * qc;
+    case G_QIF_END: return (A1 * qa + A2 * qb) + A3 * ((B1 * qc + B2 * qd) + B3 * qe);
+    default: return (c23 * qc + c23 * qa) - c13 * qb;   // G_LIF
+  }
+}
+
 template <class T, bool kCG = false>
 __device__ __forceinline__ T eval_rule(const GhostItems &G, int i, const T *Q, const T *bcg, T hx, T hy) {
   const T A1 = T(-1.0 / 5.0), A2 = T(2.0 / 3.0), A3 = T(8.0 / 15.0);
@@ -175,6 +189,58 @@ __device__ __forceinline__ void ghost_item(const GhostItems &G, int i, int8_t ty
   }
 }
 
+// A ghost item in two stages, so that every load it needs is in flight at
+// once: ghost_prep reads the item's static indices (before a kernel's
+// programmatic-launch wait), ghost_apply requests all of its solution
+// operands and its boundary value before it looks at the rule's kind, so
+// the lanes of a warp that fill different kinds of ghosts wait for one round
+// of loads together.  Operand slots a kind does not read repeat its first
+// operand.  A physical corner evaluates its two face rules as ghost_item does.
+struct GhostPrep {
+  int8_t ty;
+  int dst, a, b, c, d, e, g, nb;   // g: boundary-data index (-1: none); nb: Neumann side flag
+};
+
+__device__ __forceinline__ GhostPrep ghost_prep(const GhostItems &G, int i, int8_t ty, int dst) {
+  GhostPrep P;
+  P.ty = ty;
+  P.dst = dst;
+  const int a = __ldg(G.a + i);
+  P.a = a;
+  const bool ub = ty == G_QIF || ty == G_QIF_END || ty == G_LIF || ty == G_DIRICHLET;
+  const bool uc = ty == G_QIF || ty == G_QIF_END || ty == G_LIF || ty == G_LIF_CORNER;
+  const bool ue = ty == G_QIF_END;
+  P.b = ub ? __ldg(G.b + i) : a;
+  P.c = uc ? __ldg(G.c + i) : a;
+  P.d = ue ? __ldg(G.d + i) : a;
+  P.e = ue ? __ldg(G.e + i) : a;
+  P.g = (ty == G_DIRICHLET || ty == G_NEUMANN) ? __ldg(G.e + i) : -1;
+  P.nb = ty == G_NEUMANN ? __ldg(G.b + i) : 0;
+  return P;
+}
+
+template <class T, bool kCG = false>
+__device__ __forceinline__ void ghost_apply(const GhostItems &G, int i, const GhostPrep &P, T *Q, T *QC, const T *bcg,
+                                            T hx, T hy) {
+  if (P.ty == G_PHYS_CORNER) {
+    ghost_item<T, kCG>(G, i, P.ty, P.dst, Q, QC, bcg, hx, hy);
+    return;
+  }
+  const T qa = ld_sol<kCG>(Q + P.a), qb = ld_sol<kCG>(Q + P.b), qc = ld_sol<kCG>(Q + P.c);
+  const T qd = ld_sol<kCG>(Q + P.d), qe = ld_sol<kCG>(Q + P.e);
+  const T g = P.g >= 0 ? bcg[P.g] : T(0);
+  const T c23 = T(2.0 / 3.0), c13 = T(1.0 / 3.0), c83 = T(8.0 / 3.0);
+  T v;
+  switch (P.ty) {
+    case G_RING: QC[P.dst] = qa; return;
+    case G_LIF_CORNER: v = c23 * qc + c13 * qa; break;
+    case G_DIRICHLET: v = (c83 * g - 2 * qa) + c13 * qb; break;
+    case G_NEUMANN: v = qa + (P.nb ? hy : hx) * g; break;
+    default: v = rule_value<T>(P.ty, qa, qb, qc, qd, qe);   // COPY, QIF, QIF_END, LIF
+  }
+  Q[P.dst] = v;
+}
+
 // kT threads per block: kBlock, or 64 on a level whose kBlock grid leaves
 // SMs idle
 template <class T, int kT = kBlock>
@@ -190,11 +256,11 @@ __global__ void __launch_bounds__(kT) k_ghost(GhostItems G, int off, int n, T *_
   // (their own V-cycle starts below it)
   const int inst = (t < n && G.inst) ? G.inst[i] : -1;
   const bool skip = t >= n || (inst >= 0 && (!active[inst] || inst_nlev[inst] < need));
-  const int8_t ty = skip ? (int8_t)-1 : G.type[i];
-  const int dst = skip ? 0 : G.dst[i];
+  GhostPrep P;
+  if (!skip) P = ghost_prep(G, i, G.type[i], G.dst[i]);
   chain_wait();
   if (skip) return;
-  ghost_item<T>(G, i, ty, dst, Q, QC, bcg, T(hx_), T(hy_));
+  ghost_apply<T>(G, i, P, Q, QC, bcg, T(hx_), T(hy_));
 }
 
 // ---------------------------------------------------------------------------
@@ -239,22 +305,22 @@ enum { kActNone = 0, kActChunk = 1 };
 __device__ __forceinline__ int chunk_bc(int flags, int side) { return (flags >> (2 * side)) & 3; }
 __device__ __forceinline__ int chunk_par0(int flags) { return (flags >> 8) & 1; }
 
-struct Rule {                // one ghost rule, inline (perimeter table)
-  int type, a, b, c, d, e;
+// one ghost rule, inline (perimeter table): 32 bytes, two vector loads.  The
+// operand slots a rule does not use repeat its first operand (set at
+// upload), so all five can be read whatever the rule's kind.
+struct __align__(16) Rule {
+  int type, a, b, c, d, e, pad0, pad1;
 };
 
+// Every operand is requested before the rule's kind is looked at: the lanes
+// of a warp that evaluate different kinds of rules then wait for one round of
+// loads together, instead of one dependent round per kind in turn (the
+// divergent branches would otherwise serialise their load latencies).
 template <class T, bool kCG = false>
 __device__ __forceinline__ T eval_inline(const Rule &R, const T *Q) {
-  const T A1 = T(-1.0 / 5.0), A2 = T(2.0 / 3.0), A3 = T(8.0 / 15.0);
-  const T B1 = T(5.0 / 32.0), B2 = T(15.0 / 16.0), B3 = T(-3.0 / 32.0);
-  const T c23 = T(2.0 / 3.0), c13 = T(1.0 / 3.0);
-  auto q = [&](int j) { return ld_sol<kCG>(Q + j); };
-  switch (R.type) {
-    case G_COPY: return q(R.a);
-    case G_QIF: return (A1 * q(R.a) + A2 * q(R.b)) + A3 * q(R.c);
-    case G_QIF_END: return (A1 * q(R.a) + A2 * q(R.b)) + A3 * ((B1 * q(R.c) + B2 * q(R.d)) + B3 * q(R.e));
-    default: return (c23 * q(R.c) + c23 * q(R.a)) - c13 * q(R.b);   // G_LIF
-  }
+  const T qa = ld_sol<kCG>(Q + R.a), qb = ld_sol<kCG>(Q + R.b), qc = ld_sol<kCG>(Q + R.c);
+  const T qd = ld_sol<kCG>(Q + R.d), qe = ld_sol<kCG>(Q + R.e);
+  return rule_value<T>(R.type, qa, qb, qc, qd, qe);
 }
 
 // The smoother's operands per chunk and colour, packed at upload: for chunk
@@ -398,18 +464,35 @@ __device__ __forceinline__ void cell_update(const LevelD &L, const FieldsT<T> &f
   T *__restrict__ Q = f.Q + S.q_off;
   T qe = ld_sol<kCG>(Q + c + 1), qw = ld_sol<kCG>(Q + c - 1), qn = ld_sol<kCG>(Q + c + ldq), qs = ld_sol<kCG>(Q + c - ldq);
   T t = f.F[S.cc];
+  // the operands of the neighbour ghost's rule are requested with the
+  // solution loads, before any value is formed, so lanes with different kinds
+  // of ghosts wait for a single round of loads.  A lane holds one rule's
+  // operands: a patch-corner cell with rules on both sides (x and y) forms
+  // its y-side ghost in a second round.
+  const bool rx = kx == 3, ry = ky == 3;
+  T o0 = T(0), o1 = T(0), o2 = T(0), o3 = T(0), o4 = T(0);
+  int rt = 0;
+  if (rx || ry) {
+    const Rule R = perim[rx ? S.rx : S.ry];
+    rt = R.type;
+    o0 = ld_sol<kCG>(f.Q + R.a); o1 = ld_sol<kCG>(f.Q + R.b); o2 = ld_sol<kCG>(f.Q + R.c);
+    o3 = ld_sol<kCG>(f.Q + R.d); o4 = ld_sol<kCG>(f.Q + R.e);
+  }
+  // a partial Dirichlet ghost reads the interior neighbour across the cell,
+  // which is the opposite neighbour already loaded
   if (kx > 0) {
     T v;
-    if (kx == 1) v = c83 * S.gx + c13 * ld_sol<kCG>(Q + (sx ? c - 1 : c + 1));
+    if (kx == 1) v = c83 * S.gx + c13 * (sx ? qw : qe);
     else if (kx == 2) v = H.hx * S.gx;
-    else v = eval_inline<T, kCG>(perim[S.rx], f.Q);
+    else v = rule_value<T>(rt, o0, o1, o2, o3, o4);
     if (sx) qe = v; else qw = v;
   }
   if (ky > 0) {
     T v;
-    if (ky == 1) v = c83 * S.gy + c13 * ld_sol<kCG>(Q + (sy ? c - ldq : c + ldq));
+    if (ky == 1) v = c83 * S.gy + c13 * (sy ? qs : qn);
     else if (ky == 2) v = H.hy * S.gy;
-    else v = eval_inline<T, kCG>(perim[S.ry], f.Q);
+    else if (rx) v = eval_inline<T, kCG>(perim[S.ry], f.Q);
+    else v = rule_value<T>(rt, o0, o1, o2, o3, o4);
     if (sy) qn = v; else qs = v;
   }
   // kPow2: the coefficients arrive pre-scaled by the exact 1/h^2 (a power of
@@ -623,7 +706,7 @@ __global__ void __launch_bounds__(kT, (sizeof(T) == 4 ? 8 : 5) * (kBlock / kT))
 // (cluster-strided), with a cluster barrier (release / acquire) between
 // passes, then the level's ghost fill (launch_fill's items).  Each pass and
 // the fill compute exactly what the separate launches compute -- the same
-// relax_cell and ghost_item code -- with the solution read from L2.  One
+// relax_cell and ghost_apply code -- with the solution read from L2.  One
 // cluster holds every block, so the barrier orders the whole level; no
 // thread leaves the loop early, so every barrier is reached by all.
 constexpr int kClusterBlock = 1024;
@@ -653,7 +736,7 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
     const int i = g_off + t;
     const int inst = G.inst ? G.inst[i] : -1;
     if (inst >= 0 && !f.active[inst]) continue;
-    ghost_item<T, true>(G, i, G.type[i], G.dst[i], f.Q, f.QC, f.bcg, T(hx_), T(hy_));
+    ghost_apply<T, true>(G, i, ghost_prep(G, i, G.type[i], G.dst[i]), f.Q, f.QC, f.bcg, T(hx_), T(hy_));
   }
 }
 
