@@ -22,7 +22,9 @@ DEV_LIB = os.path.join(LIBDIR, 'libbsam_dev.so')
 
 DEV_SOURCES = ['bsam_dev.cu', 'bsam_noalloc.cu', 'bsam_geom.cu']
 NVCC_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a', '-O3', '-lineinfo', '-std=c++17',
-              '--fmad=false', '-Xcompiler', '-fPIC,-ffp-contract=off', '-shared']
+              '--fmad=false', '-Xcompiler', '-fPIC,-ffp-contract=off']
+# per-source extra flags (none at present)
+SOURCE_FLAGS = {}
 
 
 def _stale(lib, srcs):
@@ -42,15 +44,27 @@ def build_host(force=False):
 
 
 def build_dev(force=False, verbose=False):
+    """Compiles every CUDA source to an object (in parallel, each with its own
+    flags) and links the shared library."""
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = [os.path.join(CSRC, s) for s in DEV_SOURCES]
     deps = srcs + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(('.cuh', '.h'))] + \
         [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
     if force or _stale(DEV_LIB, deps):
-        cmd = ['nvcc'] + NVCC_FLAGS + ['-I', INCLUDE, '-o', DEV_LIB] + srcs
-        if verbose:
-            cmd.insert(1, '-Xptxas=-v')
-        subprocess.check_call(cmd)
+        objdir = os.path.join(LIBDIR, 'obj')
+        os.makedirs(objdir, exist_ok=True)
+        procs, objs = [], []
+        for name, src in zip(DEV_SOURCES, srcs):
+            obj = os.path.join(objdir, name.replace('.cu', '.o'))
+            cmd = ['nvcc'] + NVCC_FLAGS + SOURCE_FLAGS.get(name, []) + ['-I', INCLUDE, '-c', '-o', obj, src]
+            if verbose:
+                cmd.insert(1, '-Xptxas=-v')
+            procs.append((cmd, subprocess.Popen(cmd)))
+            objs.append(obj)
+        for cmd, p in procs:
+            if p.wait() != 0:
+                raise subprocess.CalledProcessError(p.returncode, cmd)
+        subprocess.check_call(['nvcc', '-gencode', 'arch=compute_103a,code=sm_103a', '-shared', '-o', DEV_LIB] + objs)
     return DEV_LIB
 
 

@@ -751,30 +751,38 @@ __device__ __forceinline__ T restrict_cell(const T *Q, int ldq, int ci, int cj) 
   return T(0.25) * (((Q[c] + Q[c + 1]) + Q[c + ldq]) + Q[c + ldq + 1]);
 }
 
-// kT threads per block: kBlock, or 64 on a level whose kBlock grid leaves
-// SMs idle
-template <class T, int kT = kBlock>
-__global__ void __launch_bounds__(kT) k_restrict(LevelD L, Decomp D, FieldsT<T> f, int to_parent) {
-  chain_trigger();
-  const int g = blockIdx.x * kT + threadIdx.x;
+// one coarse cell of the restriction; kChain: the grid kernel's
+// programmatic-launch wait sits between the static loads and the solution
+// (every early exit executes it too)
+template <class T, bool kChain>
+__device__ __forceinline__ void restrict_item(const LevelD &L, const Decomp &D, const FieldsT<T> &f, int to_parent,
+                                              int g) {
   if (g >= D.n) {
-    chain_wait();
+    if (kChain) chain_wait();
     return;
   }
   const int p = find_patch(D, g / kBlock, g);
   const PatchD &P = L.patches[p];
   if (!f.active[P.inst]) {
-    chain_wait();
+    if (kChain) chain_wait();
     return;
   }
   const int cmx = P.mx >> 1, q_off = P.q_off, ldq = P.mx + 2, qc_off = P.qc_off;
   const int s = g - __ldg(D.beg + p);
   const int cj = s / cmx, ci = s - cj * cmx;
   const int dst = to_parent ? __ldg(f.fp + 2 * (P.fp_off + s)) : 0;
-  chain_wait();
+  if (kChain) chain_wait();
   const T R = restrict_cell<T>(f.Q + q_off, ldq, ci, cj);
   f.QC[qc_off + (ci + 1) + (cj + 1) * (cmx + 2)] = R;
   if (to_parent) f.Q[dst] = R;
+}
+
+// kT threads per block: kBlock, or 64 on a level whose kBlock grid leaves
+// SMs idle
+template <class T, int kT = kBlock>
+__global__ void __launch_bounds__(kT) k_restrict(LevelD L, Decomp D, FieldsT<T> f, int to_parent) {
+  chain_trigger();
+  restrict_item<T, true>(L, D, f, to_parent, blockIdx.x * kT + threadIdx.x);
 }
 // ---------------------------------------------------------------------------
 // ebFaceCorrections (ebFaceCorrections.m:18-61): correction of coarse face j
@@ -872,6 +880,97 @@ __device__ __forceinline__ double op_pre(double q, double qe, double qw, double 
   return (divr(-(feE - feW), L.hx2, L.ihx2, L.pow2) - divr(fnN - fnS, L.hy2, L.ihy2, L.pow2)) + cc * q;
 }
 
+// the three item kinds of the coarse load (kChain as restrict_item)
+template <class T, bool kChain>
+__device__ __forceinline__ void load_ring_item(const FieldsT<T> &f, const int *__restrict__ ring,
+                                               const int *__restrict__ ring_inst, int ring_off, int n_ring, int t) {
+  int src = 0, dst = 0;
+  bool on = t < n_ring && (!ring_inst || f.active[__ldg(ring_inst + ring_off + t)]);
+  if (on) {
+    src = __ldg(ring + 2 * (ring_off + t));
+    dst = __ldg(ring + 2 * (ring_off + t) + 1);
+  }
+  if (kChain) chain_wait();
+  if (on) f.QC[dst] = f.Q[src];
+}
+
+template <class T, bool kChain>
+__device__ __forceinline__ void load_fp_item(const LevelD &L, const LevelD &Lc, const Decomp &D, const FieldsT<T> &f,
+                                             int g) {
+  if (g >= D.n) {
+    if (kChain) chain_wait();
+    return;
+  }
+  const int p = find_patch(D, g / kBlock, g);
+  const PatchD &P = L.patches[p];
+  if (!f.active[P.inst]) {
+    if (kChain) chain_wait();
+    return;
+  }
+  const int mx = P.mx, cmx = mx >> 1, cmy = P.my >> 1, ldq = mx + 2;
+  const int s = g - __ldg(D.beg + p);
+  const int cj = s / cmx, ci = s - cj * cmx;
+  const int q_off = P.q_off, c_off = P.c_off, qc_off = P.qc_off;
+  // static operands of the four fine cells (restrict2 order) and of the
+  // coarse operator
+  const T *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off, *CC = f.CC + c_off;
+  double dE[4], dW[4], dN[4], dS[4], cf[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int li = 2 * ci + (t & 1), lj = 2 * cj + (t >> 1);
+    dE[t] = dbl(__ldg(DeW + (li + 1) + lj * (mx + 1)));
+    dW[t] = dbl(__ldg(DeW + li + lj * (mx + 1)));
+    dN[t] = dbl(__ldg(DnS + li + (lj + 1) * mx));
+    dS[t] = dbl(__ldg(DnS + li + lj * mx));
+    cf[t] = dbl(__ldg(CC + li + lj * mx));
+  }
+  const int ldc = cmx + 2;
+  const int *win = f.win + P.win_off;
+  const int w = (ci + 1) + (cj + 1) * ldc;
+  // ring neighbours of the coarse operator come from the parent's Q
+  const int se = (ci == cmx - 1) ? __ldg(win + w + 1) : -1;
+  const int sw = (ci == 0) ? __ldg(win + w - 1) : -1;
+  const int sn = (cj == cmy - 1) ? __ldg(win + w + ldc) : -1;
+  const int ss = (cj == 0) ? __ldg(win + w - ldc) : -1;
+  const T *PDeW = f.pcoef + P.pc_off;
+  const T *PDnS = PDeW + (cmx + 1) * cmy;
+  const T *PCC = PDnS + cmx * (cmy + 1);
+  const double pE = dbl(__ldg(PDeW + (ci + 1) + cj * (cmx + 1))), pW = dbl(__ldg(PDeW + ci + cj * (cmx + 1)));
+  const double pN = dbl(__ldg(PDnS + ci + (cj + 1) * cmx)), pS = dbl(__ldg(PDnS + ci + cj * cmx));
+  const double pC = dbl(__ldg(PCC + s));
+  const int dst = __ldg(f.fp + 2 * (P.fp_off + s) + 1);
+  if (kChain) chain_wait();
+  const T *Qp = f.Q + q_off;
+  const T *Fp = f.F + c_off;
+  double rf[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int li = 2 * ci + (t & 1), lj = 2 * cj + (t >> 1);
+    const int c = (li + 1) + (lj + 1) * ldq;
+    rf[t] = dbl(Fp[li + lj * mx]) - op_pre(dbl(Qp[c]), dbl(Qp[c + 1]), dbl(Qp[c - 1]), dbl(Qp[c + ldq]),
+                                           dbl(Qp[c - ldq]), dE[t], dW[t], dN[t], dS[t], cf[t], L);
+  }
+  const double rr = 0.25 * (((rf[0] + rf[1]) + rf[2]) + rf[3]);
+  const T *QC = f.QC + qc_off;
+  const double q = dbl(QC[w]);
+  const double qe = dbl(se >= 0 ? f.Q[se] : QC[w + 1]);
+  const double qw = dbl(sw >= 0 ? f.Q[sw] : QC[w - 1]);
+  const double qn = dbl(sn >= 0 ? f.Q[sn] : QC[w + ldc]);
+  const double qs = dbl(ss >= 0 ? f.Q[ss] : QC[w - ldc]);
+  const double lc = op_pre(q, qe, qw, qn, qs, pE, pW, pN, pS, pC, Lc);
+  f.F[dst] = T(rr + lc);
+}
+
+template <class T, bool kChain>
+__device__ __forceinline__ void load_corr_item(const LevelD &L, const LevelD &Lc, const FieldsT<T> &f, const CorrCSR &C,
+                                               int n_tgt, int t) {
+  const bool on = t < n_tgt && f.active[Lc.patches[C.patch[t]].inst];
+  const int cell = on ? C.cell[t] : 0;
+  if (kChain) chain_wait();
+  if (!on) return;
+  f.F[cell] = T(add_corrections<T>(dbl(f.F[cell]), C, t, L, Lc, f, false));
+}
+
 // kT threads per block (kBlock, or 64 on a level whose kBlock grid leaves
 // SMs idle: a footprint cell is ~84 FP64 operations, and an SM issues about
 // two per clock); the decomposition's per-block patch table is kBlock-based
@@ -884,91 +983,16 @@ __global__ void __launch_bounds__(kT) k_load(LevelD L, LevelD Lc, Decomp D, Fiel
   const int nb_fp = (D.n + kT - 1) / kT;
   int b = blockIdx.x;
   if (b < nb_ring) {
-    const int t = b * kT + threadIdx.x;
-    int src = 0, dst = 0;
-    bool on = t < n_ring && (!ring_inst || f.active[__ldg(ring_inst + ring_off + t)]);
-    if (on) {
-      src = __ldg(ring + 2 * (ring_off + t));
-      dst = __ldg(ring + 2 * (ring_off + t) + 1);
-    }
-    chain_wait();
-    if (on) f.QC[dst] = f.Q[src];
+    load_ring_item<T, true>(f, ring, ring_inst, ring_off, n_ring, b * kT + threadIdx.x);
     return;
   }
   b -= nb_ring;
   if (b < nb_fp) {
-    const int g = b * kT + threadIdx.x;
-    if (g >= D.n) {
-      chain_wait();
-      return;
-    }
-    const int p = find_patch(D, g / kBlock, g);
-    const PatchD &P = L.patches[p];
-    if (!f.active[P.inst]) {
-      chain_wait();
-      return;
-    }
-    const int mx = P.mx, cmx = mx >> 1, cmy = P.my >> 1, ldq = mx + 2;
-    const int s = g - __ldg(D.beg + p);
-    const int cj = s / cmx, ci = s - cj * cmx;
-    const int q_off = P.q_off, c_off = P.c_off, qc_off = P.qc_off;
-    // static operands of the four fine cells (restrict2 order) and of the
-    // coarse operator
-    const T *DeW = f.DeW + P.dew_off, *DnS = f.DnS + P.dns_off, *CC = f.CC + c_off;
-    double dE[4], dW[4], dN[4], dS[4], cf[4];
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      const int li = 2 * ci + (t & 1), lj = 2 * cj + (t >> 1);
-      dE[t] = dbl(__ldg(DeW + (li + 1) + lj * (mx + 1)));
-      dW[t] = dbl(__ldg(DeW + li + lj * (mx + 1)));
-      dN[t] = dbl(__ldg(DnS + li + (lj + 1) * mx));
-      dS[t] = dbl(__ldg(DnS + li + lj * mx));
-      cf[t] = dbl(__ldg(CC + li + lj * mx));
-    }
-    const int ldc = cmx + 2;
-    const int *win = f.win + P.win_off;
-    const int w = (ci + 1) + (cj + 1) * ldc;
-    // ring neighbours of the coarse operator come from the parent's Q
-    const int se = (ci == cmx - 1) ? __ldg(win + w + 1) : -1;
-    const int sw = (ci == 0) ? __ldg(win + w - 1) : -1;
-    const int sn = (cj == cmy - 1) ? __ldg(win + w + ldc) : -1;
-    const int ss = (cj == 0) ? __ldg(win + w - ldc) : -1;
-    const T *PDeW = f.pcoef + P.pc_off;
-    const T *PDnS = PDeW + (cmx + 1) * cmy;
-    const T *PCC = PDnS + cmx * (cmy + 1);
-    const double pE = dbl(__ldg(PDeW + (ci + 1) + cj * (cmx + 1))), pW = dbl(__ldg(PDeW + ci + cj * (cmx + 1)));
-    const double pN = dbl(__ldg(PDnS + ci + (cj + 1) * cmx)), pS = dbl(__ldg(PDnS + ci + cj * cmx));
-    const double pC = dbl(__ldg(PCC + s));
-    const int dst = __ldg(f.fp + 2 * (P.fp_off + s) + 1);
-    chain_wait();
-    const T *Qp = f.Q + q_off;
-    const T *Fp = f.F + c_off;
-    double rf[4];
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      const int li = 2 * ci + (t & 1), lj = 2 * cj + (t >> 1);
-      const int c = (li + 1) + (lj + 1) * ldq;
-      rf[t] = dbl(Fp[li + lj * mx]) - op_pre(dbl(Qp[c]), dbl(Qp[c + 1]), dbl(Qp[c - 1]), dbl(Qp[c + ldq]),
-                                             dbl(Qp[c - ldq]), dE[t], dW[t], dN[t], dS[t], cf[t], L);
-    }
-    const double rr = 0.25 * (((rf[0] + rf[1]) + rf[2]) + rf[3]);
-    const T *QC = f.QC + qc_off;
-    const double q = dbl(QC[w]);
-    const double qe = dbl(se >= 0 ? f.Q[se] : QC[w + 1]);
-    const double qw = dbl(sw >= 0 ? f.Q[sw] : QC[w - 1]);
-    const double qn = dbl(sn >= 0 ? f.Q[sn] : QC[w + ldc]);
-    const double qs = dbl(ss >= 0 ? f.Q[ss] : QC[w - ldc]);
-    const double lc = op_pre(q, qe, qw, qn, qs, pE, pW, pN, pS, pC, Lc);
-    f.F[dst] = T(rr + lc);
+    load_fp_item<T, true>(L, Lc, D, f, b * kT + threadIdx.x);
     return;
   }
   b -= nb_fp;
-  const int t = b * kT + threadIdx.x;
-  const bool on = t < n_tgt && f.active[Lc.patches[C.patch[t]].inst];
-  const int cell = on ? C.cell[t] : 0;
-  chain_wait();
-  if (!on) return;
-  f.F[cell] = T(add_corrections<T>(dbl(f.F[cell]), C, t, L, Lc, f, false));
+  load_corr_item<T, true>(L, Lc, f, C, n_tgt, b * kT + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -978,18 +1002,17 @@ __global__ void __launch_bounds__(kT) k_load(LevelD L, LevelD Lc, Decomp D, Fiel
 // writes its four fine cells.
 // kT threads per block: kBlock, or 64 on a level whose kBlock grid leaves
 // SMs idle (about 37 FP64 operations per coarse cell, two per clock per SM)
-template <class T, int kT = kBlock>
-__global__ void __launch_bounds__(kT) k_prolong(LevelD L, Decomp D, FieldsT<T> f, int correct) {
-  chain_trigger();
-  const int g = blockIdx.x * kT + threadIdx.x;
+template <class T, bool kChain>
+__device__ __forceinline__ void prolong_item(const LevelD &L, const Decomp &D, const FieldsT<T> &f, int correct,
+                                             int g) {
   if (g >= D.n) {
-    chain_wait();
+    if (kChain) chain_wait();
     return;
   }
   const int p = find_patch(D, g / kBlock, g);
   const PatchD &P = L.patches[p];
   if (!f.active[P.inst]) {   // frozen instance, or an instance whose level k is not new
-    chain_wait();
+    if (kChain) chain_wait();
     return;
   }
   const int cm = P.mx >> 1;
@@ -1003,7 +1026,7 @@ __global__ void __launch_bounds__(kT) k_prolong(LevelD L, Decomp D, FieldsT<T> f
 #pragma unroll
     for (int di = 0; di < 3; ++di) src[dj][di] = __ldg(win + (a + di) + (b + dj) * ldw);
   const int qc_off = P.qc_off, q_off = P.q_off, ldq = P.mx + 2;
-  chain_wait();
+  if (kChain) chain_wait();
   const T *QC = f.QC + qc_off;
   T E[3][3];
 #pragma unroll
@@ -1034,6 +1057,12 @@ __global__ void __launch_bounds__(kT) k_prolong(LevelD L, Decomp D, FieldsT<T> f
   }
 }
 
+template <class T, int kT = kBlock>
+__global__ void __launch_bounds__(kT) k_prolong(LevelD L, Decomp D, FieldsT<T> f, int correct) {
+  chain_trigger();
+  prolong_item<T, true>(L, D, f, correct, blockIdx.x * kT + threadIdx.x);
+}
+
 // ---------------------------------------------------------------------------
 // Coarsest solve (ebCoarsest.m:79-91): u = Ainv (F + bcRhs), one warp per
 // row; lane l sums columns l, l+32, ... in order, then a halving tree.
@@ -1048,17 +1077,13 @@ struct CoarsestD {
 // hierarchy's rows' FP64 work over as many SMs as there are rows; a batch
 // keeps eight, since most of its instances' blocks exit at once in its last
 // V-cycles
-template <class T, int kRows = 1>
-__global__ void __launch_bounds__(32 * kRows) k_coarsest(const double *__restrict__ Ainv,
-                                                         const double *__restrict__ bcRhs,
-                                                         const CoarsestD *__restrict__ cd, FieldsT<T> f) {
-  chain_trigger();
-  const CoarsestD D = cd[blockIdx.y];
+// one row of the coarsest solve, computed by one warp (lane = lane index)
+template <class T, bool kChain>
+__device__ __forceinline__ void coarsest_row(const double *__restrict__ Ainv, const double *__restrict__ bcRhs,
+                                             const CoarsestD &D, const FieldsT<T> &f, int row, int lane) {
   const int N = D.N;
-  const int row = blockIdx.x * kRows + (int)(threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
   if (row >= N || !f.active[D.inst]) {
-    chain_wait();
+    if (kChain) chain_wait();
     return;
   }
   const double *a = Ainv + D.ainv_off + (size_t)row * N;
@@ -1071,7 +1096,7 @@ __global__ void __launch_bounds__(32 * kRows) k_coarsest(const double *__restric
     av[i] = c < N ? __ldg(a + c) : 0.0;
     bv[i] = (c < N && rhs) ? __ldg(rhs + c) : 0.0;
   }
-  chain_wait();
+  if (kChain) chain_wait();
   const T *F = f.F + D.c_off;
   double s = 0.0;
 #pragma unroll
@@ -1089,6 +1114,15 @@ __global__ void __launch_bounds__(32 * kRows) k_coarsest(const double *__restric
     const int i = row % D.n1, j = row / D.n1;
     f.Q[D.q_off + (i + 1) + (j + 1) * (D.n1 + 2)] = T(s);
   }
+}
+
+template <class T, int kRows = 1>
+__global__ void __launch_bounds__(32 * kRows) k_coarsest(const double *__restrict__ Ainv,
+                                                         const double *__restrict__ bcRhs,
+                                                         const CoarsestD *__restrict__ cd, FieldsT<T> f) {
+  chain_trigger();
+  const CoarsestD D = cd[blockIdx.y];
+  coarsest_row<T, true>(Ainv, bcRhs, D, f, blockIdx.x * kRows + (int)(threadIdx.x >> 5), threadIdx.x & 31);
 }
 
 // ---------------------------------------------------------------------------
