@@ -648,11 +648,28 @@ void launch_consistent(bsam_hier h) {
   for (int k = 1; k <= h->nlev; ++k) launch_fill(h, k);
 }
 
+// F = FTrue (ebSolveCycles.m:30-34), once before a run of FP64 V-cycles
+// instead of at the start of each: within a solve F is written only by the
+// coarse loads, over the parent footprint (recomputed every V-cycle before
+// any read) and at the flux-correction targets, whose value the load forms
+// from FTrue itself (load_corr_item); every other cell keeps FTrue.  So the
+// F each V-cycle reads is the one the reference's per-cycle reset gives.
+void reset_force(bsam_hier h) {
+  if (h->ninst == 1) {
+    cudaMemcpyAsync(h->F.p, h->FTrue.p, sizeof(double) * h->n_cells, cudaMemcpyDeviceToDevice, h->stream);
+  } else {
+    Decomp D = decomp(h, h->all_cells);
+    Launch l(h, K_LOAD, 16.0 * (double)h->n_cells);
+    launch_k(h, k_freset, D.nblocks, kBlock, D, (const PatchD *)h->patches.p, fields(h));
+  }
+}
+
 // one ebSolveCycles iteration body (mode 1 inside ebSolveCycles, 2 for an
 // eager V-cycle).  FP64: F = FTrue, V-cycle, fill-down, residual.  Mixed:
 // the FP32 correction E = 0, one FP32 FAS V-cycle of E against the stored
 // residual, Q += E in FP64, restriction and ghost fill in FP64, FP64
-// residual.
+// residual.  The FP64 body expects F = FTrue off the footprints
+// (reset_force before the first iteration).
 int launch_iteration(bsam_hier h, int mode) {
   if (mixed(h)) {
     CK(cudaMemsetAsync(h->E.p, 0, sizeof(float) * h->E.n, h->stream));
@@ -667,13 +684,6 @@ int launch_iteration(bsam_hier h, int mode) {
     launch_residual(h, mode);
     CK(cudaGetLastError());
     return BSAM_OK;
-  }
-  if (h->ninst == 1) {
-    CK(cudaMemcpyAsync(h->F.p, h->FTrue.p, sizeof(double) * h->n_cells, cudaMemcpyDeviceToDevice, h->stream));
-  } else {
-    Decomp D = decomp(h, h->all_cells);
-    Launch l(h, K_LOAD, 16.0 * (double)h->n_cells);
-    launch_k(h, k_freset, D.nblocks, kBlock, D, (const PatchD *)h->patches.p, fields(h));
   }
   launch_vcycle(h, h->nlev);
   launch_filldown(h);
@@ -2024,6 +2034,8 @@ int bsam_vcycle(bsam_hier h) {
   if (mixed(h)) {   // the correction cycle's right-hand side
     launch_consistent(h);
     launch_residual(h, 2);
+  } else {
+    reset_force(h);
   }
   if ((rc = launch_iteration(h, 2))) return rc;
   CK(cudaStreamSynchronize(h->stream));
@@ -2036,6 +2048,7 @@ int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles,
   int rc = set_device(h);
   if (rc) return rc;
   if ((rc = ensure_f32(h))) return rc;
+  if (!mixed(h)) reset_force(h);
   for (int k = 1; k <= h->nlev; ++k) launch_fill(h, k);
   launch_residual(h, 0);
   CK(cudaGetLastError());
@@ -2263,6 +2276,8 @@ int bsam_profile_vcycles(bsam_hier h, int ncycles, int level, double ms[BSAM_NKI
   if (mixed(h)) {
     launch_consistent(h);
     launch_residual(h, 2);
+  } else {
+    reset_force(h);
   }
   if ((rc = autotune(h))) return rc;
   h->profiling = true;

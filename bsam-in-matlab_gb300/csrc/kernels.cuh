@@ -968,7 +968,12 @@ __device__ __forceinline__ void load_corr_item(const LevelD &L, const LevelD &Lc
   const int cell = on ? C.cell[t] : 0;
   if (kChain) chain_wait();
   if (!on) return;
-  f.F[cell] = T(add_corrections<T>(dbl(f.F[cell]), C, t, L, Lc, f, false));
+  // FP64: the target's F before its corrections is FTrue (the value the
+  // reference's per-cycle reset F = FTrue leaves there), so the V-cycle does
+  // not depend on a reset of F before it; the correction cycle of the mixed
+  // form adds to its own right-hand side
+  const double base = sizeof(T) == sizeof(double) ? f.FTrue[cell] : dbl(f.F[cell]);
+  f.F[cell] = T(add_corrections<T>(base, C, t, L, Lc, f, false));
 }
 
 // kT threads per block (kBlock, or 64 on a level whose kBlock grid leaves
