@@ -441,6 +441,10 @@ def main():
     ap.add_argument('--batch', type=int, default=256, help='instances of the batching form (0: skip)')
     ap.add_argument('--no-forms', action='store_true', help='skip the mixed, batching and serving forms')
     ap.add_argument('--serve-rates', default='5,10,20', help='offered request rates of the serving form')
+    ap.add_argument('--eager-vcycle', action='store_true',
+                    help='profiling aid: upload the starfish hierarchy, run one eager FP64 V-cycle (every kernel of '
+                         'the V-cycle, fill-down and residual launched once, in order, between cudaProfilerStart and '
+                         'cudaProfilerStop) and exit; for ncu --profile-from-start off')
     args = ap.parse_args()
     if 'WORLD_SIZE' not in os.environ and args.gpus > 1 and args.impl == 'native':
         # one process per GPU: start the ranks under torch.distributed.run
@@ -476,6 +480,14 @@ def main():
     t_build = time.perf_counter()
     fl = flatten(H)
     dh = DevHier(backend.ctx, fl, opts)
+    if args.eager_vcycle:
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        dh.vcycle()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        print(json.dumps({'eager_vcycle': 'done', 'levels': H.nlev, 'kernels': dh.kernels_per_vcycle()}), flush=True)
+        return
     dh.save_state()
     t_upload = time.perf_counter()
     stream = torch.cuda.ExternalStream(dh.stream(), device=torch.device('cuda', local))
@@ -552,7 +564,15 @@ def main():
     from bsam.device import fp64_rate
     fp64_peak = fp64_rate(backend.ctx)
     fp64_ach = rl['bytes'] * 9 / 48 / (rl['ms'] / 1e3) / 1e9
-    per_kind = {k: {'ms_per_cycle': v['ms'] / 3, 'launches_per_cycle': v['launches'] / 3} for k, v in prof.items()}
+    # per kernel kind over all levels: time, launches and the algorithmic
+    # bytes of each kind (smoother 24 B per cell and colour pass, coarse load
+    # 50, prolongation 20, restriction 12, residual 41; ghost fills and the
+    # coarsest solve have none) against the copy peak
+    per_kind = {k: {'ms_per_cycle': v['ms'] / 3, 'launches_per_cycle': v['launches'] / 3,
+                    'bytes_per_cycle': v['bytes'] / 3,
+                    'achieved_gbs': (v['bytes'] / (v['ms'] / 1e3) / 1e9) if v['ms'] > 0 and v['bytes'] > 0 else None,
+                    'frac': (v['bytes'] / (v['ms'] / 1e3) / 1e9 / peak) if v['ms'] > 0 and v['bytes'] > 0 else None}
+                for k, v in prof.items() if v['launches']}
 
     # ---- forms beside the plain FP64 path -----------------------------------
     forms = None

@@ -53,3 +53,16 @@ def test_native_line():
     assert {'sm_mhz', 'sm_max_mhz', 'reasons'} <= set(d['clocks'])
     s = d['setup']
     assert 0 < s['host_build_s'] < s['setup_and_solve_s'] and s['first_solve_s'] > 0
+    pk = d['config']['per_kernel']
+    assert pk['relax']['launches_per_cycle'] > 0 and pk['relax']['achieved_gbs'] > 0
+    assert 0 < pk['coarse_load']['frac'] < 1.5 and pk['ghost']['achieved_gbs'] is None
+
+
+@pytest.mark.gpu
+def test_eager_vcycle_mode():
+    """The profiling aid: one eager V-cycle between cudaProfilerStart/Stop."""
+    out = subprocess.run([sys.executable, os.path.join(ROOT, 'bench.py'), '--eager-vcycle'], cwd=ROOT,
+                         capture_output=True, text=True, timeout=900)
+    assert out.returncode == 0, out.stderr[-2000:]
+    d = json.loads([l for l in out.stdout.splitlines() if l.startswith('{')][0])
+    assert d['eager_vcycle'] == 'done' and d['levels'] == 7 and d['kernels'] > 50
