@@ -353,9 +353,12 @@ def serving_form(rates, per_rate):
     warm, _ = run_stream(srv, [star_request(90000 + i) for i in range(srv.nbuild)], rate=100.0, seed=9)
     out = {'workload': 'served diffuse-domain star requests (Poisson arrivals), base 64^2, MaxLevels U{3,4,5}, '
                        'mixed precision, RelTol 1e-10',
-           'builders': srv.nbuild, 'wave_slots': len(srv.ctxs), 'server_start_s': start_s, 'rates': []}
+           'builders': srv.nbuild, 'wave_slots': len(srv.ctxs), 'server_start_s': start_s, 'rates': [],
+           'gpu_distance': srv.distance is not None}
     for rate in rates:
-        n = int(max(per_rate, round(rate * 6)))
+        # about four seconds of arrivals, 30 to 120 requests: enough to see
+        # where the delivered rate stops following the offered one
+        n = int(min(max(per_rate, round(rate * 4)), 120))
         specs = [star_request(int(rate * 1000) + i) for i in range(n)]
         w0 = len(srv.waves_run)
         res, wall = run_stream(srv, specs, rate=rate, seed=int(rate))
@@ -378,6 +381,14 @@ def serving_form(rates, per_rate):
     d['parabolic_p50_ms'] = float(np.percentile([r.latency_s * 1e3 for r in par], 50))
     out['mixed_stream'] = d
     srv.close()
+    if srv.distance is not None:
+        out['distance_service'] = {'calls': srv.distance.calls, 'points': srv.distance.points,
+                                   'busy_s': srv.distance.busy_s}
+    ok = [r for r in out['rates']]
+    if ok:
+        best = max(ok, key=lambda r: r['solves_per_s'])
+        out['saturation'] = {'offered_rate': best['offered_rate'], 'solves_per_s': best['solves_per_s'],
+                             'mean_wave_size': best['mean_wave_size']}
     return out
 
 
@@ -440,7 +451,7 @@ def main():
     ap.add_argument('--cpu-budget', type=float, default=15.0)
     ap.add_argument('--batch', type=int, default=256, help='instances of the batching form (0: skip)')
     ap.add_argument('--no-forms', action='store_true', help='skip the mixed, batching and serving forms')
-    ap.add_argument('--serve-rates', default='5,10,20', help='offered request rates of the serving form')
+    ap.add_argument('--serve-rates', default='5,10,20,50,100,200', help='offered request rates of the serving form')
     ap.add_argument('--eager-vcycle', action='store_true',
                     help='profiling aid: upload the starfish hierarchy, run one eager FP64 V-cycle (every kernel of '
                          'the V-cycle, fill-down and residual launched once, in order, between cudaProfilerStart and '

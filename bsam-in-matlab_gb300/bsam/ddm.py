@@ -35,7 +35,9 @@ class StarGeometry:
         self.params = (s0, s1, s2, k, th0)
         self._h = hostlib.lib().bsam_starfish_new(int(n), float(s0), float(s1), float(s2), float(k), float(th0))
         self.name = name or f'star: r = {s0}({s1} + {s2} sin({k} theta + {th0}))'
-        self.device = device          # a bsam.device.Context: the segment minimum runs on the GPU
+        # a bsam.device.Context, or a serving builder's RemoteDistance: the
+        # segment minimum runs on the GPU
+        self.device = device
         self._cache = []              # recent (key, d): phi, delta, D, C, F sample the same points
         self._pref = {}               # key -> (x, y, d) of the point sets handed to prefetch()
 
@@ -78,12 +80,15 @@ class StarGeometry:
             hostlib.lib().bsam_starfish_distance_mt(self._h, x.ctypes.data, y.ctypes.data, d.ctypes.data, x.size,
                                                     hostlib.host_threads())
             return d
-        from .device import polygon_dist2
         best = np.empty_like(x)
         sign = np.empty_like(x)
         hostlib.lib().bsam_starfish_init_sign(self._h, x.ctypes.data, y.ctypes.data, best.ctypes.data,
                                               sign.ctypes.data, x.size)
-        polygon_dist2(self.device, self.vertices, x, y, best)
+        if hasattr(self.device, 'dist2'):     # a builder process: the server's GPU distance service
+            self.device.dist2(self.vertices, x, y, best)
+        else:
+            from .device import polygon_dist2
+            polygon_dist2(self.device, self.vertices, x, y, best)
         return sign * np.sqrt(best)
 
     def prefetch(self, sets):

@@ -6,7 +6,9 @@ builder spec) arrive at any time.  Each one goes through two stages:
   build  host set-up in a pool of worker processes (spawned, without a CUDA
          context: geometry, coefficients, tagging and clustering, the
          hierarchy and its flat upload tables -- the reference's ebSetup /
-         ebAddLevel / ddTransmissionProblem path); the set-up's device steps
+         ebAddLevel / ddTransmissionProblem path; the polygon distances of
+         their sample points go to the server's DistanceService, which runs
+         them on the GPU); the set-up's device steps
          (ghost fills, new-level prolongations) are deferred to the wave,
          which runs them on the merged upload (bsam_setup_levels) -- many
          processes issuing small synchronous GPU calls would time-slice one
@@ -86,10 +88,122 @@ def run_parabolic(spec, backend):
                     'StepVerbose', 0, 'Precision', spec.get('Precision', 'fp64'), backend=backend)
 
 
-def _worker_init():
+class DistanceService:
+    """The polygon distances of the builder processes, computed on the GPU.
+
+    A builder has no CUDA context (many contexts would time-slice the GPU),
+    but most of a diffuse-domain request's host set-up is the signed distance
+    of every sample point to its 3000-point interface (the segment minimum of
+    ddStarfishGeometry.m:140-177).  The builder keeps the O(n) host part
+    (polar-angle segment, starting candidate, radial sign) and hands the
+    segment minimum to this service: the points go through a shared-memory
+    block, one thread of the server process runs ``bsam_polygon_dist2`` on a
+    context and stream of its own, and writes the minima back in place.  The
+    minimum over all segments is the same whichever search finds it, so a
+    hierarchy built this way equals the host-built one bit for bit.
+    """
+
+    def __init__(self, mpctx, nworkers, device=0, dist2=None, threads=2):
+        self.req = mpctx.Queue()
+        self.resp = [mpctx.Queue() for _ in range(nworkers)]
+        self.slot = mpctx.Value('i', 0)
+        self.calls = 0
+        self.points = 0
+        self.busy_s = 0.0
+        self.stat = threading.Lock()
+        # several serving threads, each with its own context and stream, so
+        # one builder's copies overlap another's kernel
+        self.threads = []
+        for i in range(max(1, int(threads))):
+            fn = dist2
+            if fn is None:     # the device's segment minimum on a context of its own
+                from .device import Context, polygon_dist2
+                ctx = Context(device)
+                fn = lambda verts, x, y, best, ctx=ctx: polygon_dist2(ctx, verts, x, y, best)
+            t = threading.Thread(target=self._serve, args=(fn,), name=f'bsam-distance-{i}', daemon=True)
+            t.start()
+            self.threads.append(t)
+
+    def initargs(self):
+        return (self.req, self.resp, self.slot)
+
+    def _serve(self, dist2):
+        from multiprocessing import shared_memory
+        while True:
+            msg = self.req.get()
+            if msg is None:
+                return
+            wid, name, nv, n = msg
+            err = None
+            t0 = time.perf_counter()
+            try:
+                # the builder owns the block and unlinks it (the builders share
+                # this process's resource tracker, so attaching adds nothing
+                # it has to forget)
+                shm = shared_memory.SharedMemory(name=name)
+                buf = np.ndarray((2 * nv + 3 * n,), dtype=np.float64, buffer=shm.buf)
+                verts = buf[:2 * nv].reshape(nv, 2)
+                x, y, best = buf[2 * nv:2 * nv + n], buf[2 * nv + n:2 * nv + 2 * n], buf[2 * nv + 2 * n:]
+                dist2(verts, x, y, best)
+                del buf, verts, x, y, best
+                shm.close()
+                with self.stat:
+                    self.calls += 1
+                    self.points += n
+            except Exception as e:  # noqa: BLE001 -- reported to the builder
+                err = repr(e)
+            with self.stat:
+                self.busy_s += time.perf_counter() - t0
+            self.resp[wid].put(err)
+
+    def close(self):
+        for _ in self.threads:
+            self.req.put(None)
+        for t in self.threads:
+            t.join()
+
+
+class RemoteDistance:
+    """A builder's handle on the DistanceService (``StarGeometry(device=...)``)."""
+
+    def __init__(self, req, resp, wid):
+        self.req, self.resp, self.wid = req, resp, wid
+
+    def dist2(self, verts, x, y, best):
+        from multiprocessing import shared_memory
+        nv, n = int(verts.shape[0]), int(x.size)
+        shm = shared_memory.SharedMemory(create=True, size=8 * (2 * nv + 3 * n))
+        try:
+            buf = np.ndarray((2 * nv + 3 * n,), dtype=np.float64, buffer=shm.buf)
+            buf[:2 * nv] = np.ascontiguousarray(verts, dtype=np.float64).ravel()
+            buf[2 * nv:2 * nv + n] = x
+            buf[2 * nv + n:2 * nv + 2 * n] = y
+            buf[2 * nv + 2 * n:] = best
+            self.req.put((self.wid, shm.name, nv, n))
+            err = self.resp.get(timeout=300)
+            if err is not None:
+                raise RuntimeError(f'bsam_serve:distance: {err}')
+            best[:] = buf[2 * nv + 2 * n:]
+            del buf
+        finally:
+            shm.close()
+            shm.unlink()
+        return best
+
+
+_REMOTE = None        # this builder's RemoteDistance (set by _worker_init)
+
+
+def _worker_init(req=None, resp=None, slot=None):
+    global _REMOTE
     os.environ['OMP_NUM_THREADS'] = '1'
     os.environ['OPENBLAS_NUM_THREADS'] = '1'
     os.environ['BSAM_HOST_THREADS'] = '1'       # the pool already uses every core
+    if req is not None:
+        with slot.get_lock():
+            wid = slot.value
+            slot.value += 1
+        _REMOTE = RemoteDistance(req, resp[wid], wid)
 
 
 def _warm(_):
@@ -128,7 +242,7 @@ def build_spec(spec):
     be = DeferredBackend()
     if spec['kind'] == 'dd_star':
         from .ddm import StarGeometry, ddTransmissionProblem, starfish_q, starfish_h, starfish_tag
-        g = StarGeometry(3000, spec['a0'], 1.0, spec['b'], float(spec['k']), spec['th0'])
+        g = StarGeometry(3000, spec['a0'], 1.0, spec['b'], float(spec['k']), spec['th0'], device=_REMOTE)
         data = dict(STAR_DATA, q=starfish_q, h=starfish_h)
         prob, _ = ddTransmissionProblem(g, spec['eps'], STAR_BOX, data)
         opts = ebOptions('BaseCells', 64, 'MaxLevels', int(spec['MaxLevels']), 'Indicator', 'fun',
@@ -180,19 +294,24 @@ class Server:
                    of the free device memory at start)
     """
 
-    def __init__(self, builders=None, waves=3, wave_size=64, budget_bytes=None, device=0, build_fn=None):
+    def __init__(self, builders=None, waves=3, wave_size=64, budget_bytes=None, device=0, build_fn=None,
+                 gpu_distance=True):
         from .device import Context
         self.device = device
         self.nbuild = builders or max(1, min(16, (os.cpu_count() or 2) - 1))
         self.pool = None
+        self.distance = None
         if build_fn is None:
             # builder processes inherit a one-thread BLAS / OpenMP setting
             # (several of them share the host's cores)
             saved = {k: os.environ.get(k) for k in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS')}
             os.environ.update(OMP_NUM_THREADS='1', OPENBLAS_NUM_THREADS='1')
             try:
-                self.pool = cf.ProcessPoolExecutor(self.nbuild, mp_context=mp.get_context('spawn'),
-                                                   initializer=_worker_init)
+                spawn = mp.get_context('spawn')
+                if gpu_distance and device is not None:
+                    self.distance = DistanceService(spawn, self.nbuild, device)
+                self.pool = cf.ProcessPoolExecutor(self.nbuild, mp_context=spawn, initializer=_worker_init,
+                                                   initargs=self.distance.initargs() if self.distance else ())
                 list(self.pool.map(_warm, range(self.nbuild)))
             finally:
                 for k, v in saved.items():
@@ -259,6 +378,8 @@ class Server:
         self.workers.shutdown()
         if self.pool is not None:
             self.pool.shutdown()
+        if self.distance is not None:
+            self.distance.close()
 
     # ---- stages -----------------------------------------------------------------
     def _built(self, rid, spec, f, times):

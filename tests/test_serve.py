@@ -193,3 +193,93 @@ def test_parabolic_request_same_alone_and_beside_waves():
             for qa, qb in zip(direct['H'].lev[k].Q, r.solution['H'].lev[k].Q):
                 np.testing.assert_array_equal(qa[1:-1, 1:-1], qb[1:-1, 1:-1])
     assert all(r.final_rel <= 1e-10 for r in rm[1:])
+
+
+def _brute_dist2(verts, x, y, best):
+    """Squared distance to the closed polygon by brute force (a stand-in for
+    the device minimum in a CPU test of the service's plumbing)."""
+    a, b = verts[:-1], verts[1:]
+    for i in range(x.size):
+        px, py = x[i], y[i]
+        dx, dy = b[:, 0] - a[:, 0], b[:, 1] - a[:, 1]
+        t = np.clip(((px - a[:, 0]) * dx + (py - a[:, 1]) * dy) / (dx * dx + dy * dy), 0, 1)
+        ex, ey = a[:, 0] + t * dx - px, a[:, 1] + t * dy - py
+        best[i] = min(best[i], float(np.min(ex * ex + ey * ey)))
+    return best
+
+
+def _remote_distances(n):
+    from bsam import serve
+    from bsam.ddm import StarGeometry
+    g = StarGeometry(200, 0.9, 1.2, 0.5, 4.0, 0.3, device=serve._REMOTE)
+    rng = np.random.Generator(np.random.PCG64(n))
+    X, Y = rng.uniform(-2, 2, (2, 50))
+    return X, Y, g.signedDistance(X, Y), serve._REMOTE is not None
+
+
+def test_distance_service_plumbing():
+    """Builder processes hand their polygon distances to the server's
+    service through shared memory and get the minima back in place."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    from bsam import serve
+    from bsam.ddm import StarGeometry
+    spawn = mp.get_context('spawn')
+    svc = serve.DistanceService(spawn, 2, dist2=_brute_dist2)
+    with cf.ProcessPoolExecutor(2, mp_context=spawn, initializer=serve._worker_init,
+                                initargs=svc.initargs()) as pool:
+        out = list(pool.map(_remote_distances, [1, 2, 3]))
+    svc.close()
+    host = StarGeometry(200, 0.9, 1.2, 0.5, 4.0, 0.3)
+    for X, Y, d, remote in out:
+        assert remote
+        np.testing.assert_allclose(d, host.signedDistance(X, Y), rtol=0, atol=1e-13)
+    assert svc.calls == 3 and svc.points == 150
+
+
+@pytest.mark.gpu
+def test_gpu_distance_builds_equal_host_builds():
+    """Requests built by builder processes whose polygon distances run on
+    the GPU (the server's DistanceService) solve to the same bits as
+    requests built with the host distance."""
+    specs = [dict(star_request(s), MaxLevels=3) for s in (21, 22)]
+    out = {}
+    for gpu in (True, False):
+        srv = Server(builders=2, waves=1, wave_size=1, gpu_distance=gpu)
+        futs = [srv.submit(s) for s in specs]
+        out[gpu] = [f.result(timeout=600) for f in futs]
+        if gpu:
+            assert srv.distance is not None and srv.distance.calls > 0
+        else:
+            assert srv.distance is None
+        srv.close()
+    for a, b in zip(out[True], out[False]):
+        for name in ('FTrue', 'DeW', 'DnS', 'CC', 'InvDiagS'):
+            np.testing.assert_array_equal(getattr(a.flat, name), getattr(b.flat, name))
+        np.testing.assert_array_equal(a.Q, b.Q)
+        assert a.vcycles == b.vcycles and a.final_rel <= 1e-10
+
+
+@pytest.mark.gpu
+def test_elliptic_request_same_alone_and_beside_another_wave():
+    """An elliptic request solved on one wave slot while a wave of another
+    hierarchy runs on a second slot gives the same bits as when it runs
+    alone."""
+    from bsam.serve import build_spec
+    a = dict(star_request(31), MaxLevels=3)
+    b = dict(star_request(32), MaxLevels=5)
+    alone = Server(waves=1, wave_size=1, build_fn=build_spec)
+    ra = alone.submit(a).result(timeout=600)
+    alone.close()
+    mix = Server(waves=2, wave_size=1, build_fn=build_spec)
+    with mix.lock:          # both ready before the dispatcher takes either
+        fb = mix.submit(b)
+        fa = mix.submit(a)
+    rb, rm = fb.result(timeout=600), fa.result(timeout=600)
+    mix.close()
+    w = mix.waves_run
+    assert len(w) == 2 and max(x['start'] for x in w) < min(x['end'] for x in w), w   # the waves overlapped
+    assert rb.final_rel <= 1e-10 and rm.final_rel <= 1e-10
+    assert rm.vcycles == ra.vcycles
+    np.testing.assert_array_equal(rm.hist, ra.hist)
+    np.testing.assert_array_equal(rm.Q, ra.Q)
