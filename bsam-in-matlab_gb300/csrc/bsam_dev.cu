@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <unordered_map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -157,6 +158,11 @@ struct bsam_hier_s {
   std::vector<ResAcc> res_acc;
   DBuf<int8_t> g_type;
   DBuf<int> g_dst, g_a, g_b, g_c, g_d, g_e;
+  // the fill that follows a restriction into the level (k_restrict_fill):
+  // operands a, b, c of every ghost item, a cell under the finer level's
+  // footprint coded -1 - (entry of ga_rt)
+  DBuf<int> ga_a, ga_b, ga_c;
+  DBuf<int2> ga_rt;
   DBuf<PatchD> patches;
   DBuf<ResAcc> acc;
   DBuf<Rule> perim;                // per-patch perimeter ghost rules (inline)
@@ -522,6 +528,30 @@ void launch_restrict(bsam_hier h, int k, int to_parent) {
     launch_k(h, k_restrict<T>, D.nblocks, kBlock, leveld(h, k), D, fields_t<T>(h), to_parent);
 }
 
+// restriction of level k into QC and level k-1, then the ghost fill of
+// level k-1 (launch_restrict + launch_fill(k - 1, k)) in one launch
+template <class T = double>
+void launch_restrict_fill(bsam_hier h, int k) {
+  const LevelPlan &L = h->lev[k], &Lc = h->lev[k - 1];
+  if (!Lc.g1_n) {
+    launch_restrict<T>(h, k, 1);
+    return;
+  }
+  Decomp D = decomp(h, L.coarse);
+  FieldsT<T> f = fields_t<T>(h);
+  Launch l(h, K_RESTRICT, 12.0 * tscale<T>() * (double)L.ncells, k);
+  const GhostAlt A{h->ga_a.p, h->ga_b.p, h->ga_c.p, h->ga_rt.p};
+  if (nblk(D.n) + nblk(Lc.g1_n) < spread_limit(h)) {
+    const int nb = (D.n + 63) / 64;
+    launch_k(h, k_restrict_fill<T, 64>, nb + (Lc.g1_n + 63) / 64, 64, leveld(h, k), D, f, 1, nb, ghost_items(h),
+             A, Lc.g1_off, Lc.g1_n, Lc.hx, Lc.hy, (const int *)h->active.p, (const int *)h->inst_nlev.p, k);
+  } else {
+    const int nb = nblk(D.n);
+    launch_k(h, k_restrict_fill<T>, nb + nblk(Lc.g1_n), kBlock, leveld(h, k), D, f, 1, nb, ghost_items(h), A,
+             Lc.g1_off, Lc.g1_n, Lc.hx, Lc.hy, (const int *)h->active.p, (const int *)h->inst_nlev.p, k);
+  }
+}
+
 CorrCSR corr_csr(bsam_hier h, const LevelPlan &L) {
   return CorrCSR{h->ct_cell.p + L.ct_off, h->ct_patch.p + L.ct_off, h->ct_beg.p + L.ct_off, h->ct_item.p, h->ct_j.p};
 }
@@ -588,8 +618,7 @@ void launch_vcycle(bsam_hier h, int k) {
     return;
   }
   launch_relax<T>(h, k, h->opts.npre);
-  launch_restrict<T>(h, k, 1);
-  launch_fill<T>(h, k - 1, k);
+  launch_restrict_fill<T>(h, k);
   launch_coarse_load<T>(h, k);
   launch_vcycle<T>(h, k - 1);
   launch_prolong<T>(h, k, 1);
@@ -605,10 +634,7 @@ void launch_vcycle(bsam_hier h, int k) {
 }
 
 void launch_filldown(bsam_hier h) {
-  for (int kk = h->nlev; kk >= 2; --kk) {
-    launch_restrict(h, kk, 1);
-    launch_fill(h, kk - 1, kk);
-  }
+  for (int kk = h->nlev; kk >= 2; --kk) launch_restrict_fill(h, kk);
 }
 
 bool mixed(bsam_hier h) { return h->opts.precision == 1; }
@@ -1574,6 +1600,44 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
   h->hist_stride = h->opts.max_vcycles + 1;
   std::vector<int> inlev(h->ninst, 0);
   for (int p = 0; p < d->npatch; ++p) inlev[pinst[p]] = std::max(inlev[pinst[p]], (int)B.P(p)[PD_LEVEL]);
+  // fused-fill operands: for the ghost items of each level k-1 (k >= 2),
+  // the cells of level k-1 that the restriction from level k overwrites,
+  // with the four fine cells they are restricted from (ebTransfer.m:10-33)
+  {
+    std::vector<int> aa(B.ga), ab(B.gb), ac(B.gc);
+    std::vector<int2> rt;
+    for (int k = 2; k <= d->nlev; ++k) {
+      const LevelPlan &L = h->lev[k], &Lc = h->lev[k - 1];
+      if (!Lc.g1_n) continue;
+      std::unordered_map<int, int> cov;   // parent Q index -> entry of rt
+      for (int p = L.p0; p < L.p1; ++p) {
+        const int32_t *r = B.P(p);
+        const int mx = r[PD_MX], cmx = mx / 2, cmy = r[PD_MY] / 2, ldq = mx + 2;
+        for (int sidx = 0; sidx < cmx * cmy; ++sidx) {
+          const int cj = sidx / cmx, ci = sidx - cj * cmx;
+          const int dst = d->fp[2 * (r[PD_FP0] + sidx)];
+          cov[dst] = (int)rt.size();
+          rt.push_back(make_int2(r[PD_QOFF] + (2 * ci + 1) + (2 * cj + 1) * ldq, ldq));
+        }
+      }
+      auto code = [&](int q) {
+        auto it = cov.find(q);
+        return it == cov.end() ? q : -1 - it->second;
+      };
+      for (int i = Lc.g1_off; i < Lc.g1_off + Lc.g1_n; ++i) {
+        const int8_t t = B.gt[i];
+        if (t == G_RING) continue;               // source in the level below: never restricted
+        if (t == G_PHYS_CORNER) { ac[i] = code(B.gc[i]); continue; }   // a, b: rule indices
+        aa[i] = code(B.ga[i]);
+        if (t == G_QIF || t == G_QIF_END || t == G_LIF || t == G_DIRICHLET) ab[i] = code(B.gb[i]);
+        if (t == G_QIF || t == G_QIF_END || t == G_LIF || t == G_LIF_CORNER) ac[i] = code(B.gc[i]);
+      }
+    }
+    if (rt.empty()) rt.push_back(make_int2(0, 0));
+    if ((rc = h->ga_a.upload(aa.data(), aa.size(), s)) || (rc = h->ga_b.upload(ab.data(), ab.size(), s)) ||
+        (rc = h->ga_c.upload(ac.data(), ac.size(), s)) || (rc = h->ga_rt.upload(rt.data(), rt.size(), s)))
+      return rc;
+  }
   if ((rc = h->g_inst.upload(B.gi.data(), B.gi.size(), s)) || (rc = h->ring_inst.upload(rinst.data(), rinst.size(), s)) ||
       (rc = h->inst_nlev.upload(inlev.data(), inlev.size(), s)))
     return rc;
@@ -1634,11 +1698,13 @@ void release(bsam_hier h) {
                          &h->bcg32, &h->rpack32})
     b->release();
   for (DBuf<int> *b : {&h->win, &h->fp, &h->ring, &h->ints, &h->ct_cell, &h->ct_patch, &h->ct_beg, &h->ct_item,
-                       &h->ct_j, &h->active, &h->iters, &h->ones, &h->g_inst, &h->ring_inst, &h->inst_nlev, &h->g_dst, &h->g_a, &h->g_b, &h->g_c, &h->g_d, &h->g_e})
+                       &h->ct_j, &h->active, &h->iters, &h->ones, &h->g_inst, &h->ring_inst, &h->inst_nlev, &h->g_dst, &h->g_a, &h->g_b, &h->g_c, &h->g_d, &h->g_e,
+                       &h->ga_a, &h->ga_b, &h->ga_c})
     b->release();
   h->flags.release(); h->g_type.release(); h->patches.release(); h->acc.release(); h->perim.release();
   h->rchunks.release(); h->pchunks.release(); h->cact.release(); h->crange.release(); h->levelx.release(); h->rtasks.release(); h->instres.release(); h->sranges.release();
   h->coarsest.release();
+  h->ga_rt.release();
   delete[] h->acc_host;
   delete[] h->active_host;
   h->acc_host = nullptr;

@@ -196,49 +196,98 @@ __device__ __forceinline__ void ghost_item(const GhostItems &G, int i, int8_t ty
 // the lanes of a warp that fill different kinds of ghosts wait for one round
 // of loads together.  Operand slots a kind does not read repeat its first
 // operand.  A physical corner evaluates its two face rules as ghost_item does.
+//
+// GhostAlt: the operands of a level's ghost items for the fill that follows
+// the restriction of the level above into it, fused into one launch with
+// that restriction (k_restrict_fill).  A solution operand that the
+// restriction overwrites (a cell under the finer level's footprint) is coded
+// -1 - j, and the item forms its value itself from the four fine cells of
+// entry j of `rt` with restrict_cell's arithmetic -- the value the
+// restriction stores -- so the fill reads nothing the same launch writes.
+struct GhostAlt {
+  const int *a, *b, *c;        // operand slots (d and e are parent cells: never restricted)
+  const int2 *rt;              // (first fine cell in Q, fine row stride)
+};
+
 struct GhostPrep {
   int8_t ty;
   int dst, a, b, c, d, e, g, nb;   // g: boundary-data index (-1: none); nb: Neumann side flag
 };
 
-__device__ __forceinline__ GhostPrep ghost_prep(const GhostItems &G, int i, int8_t ty, int dst) {
+template <bool kAlt = false>
+__device__ __forceinline__ GhostPrep ghost_prep(const GhostItems &G, int i, int8_t ty, int dst,
+                                                const GhostAlt *A = nullptr) {
   GhostPrep P;
   P.ty = ty;
   P.dst = dst;
-  const int a = __ldg(G.a + i);
+  const int a = kAlt ? __ldg(A->a + i) : __ldg(G.a + i);
   P.a = a;
   const bool ub = ty == G_QIF || ty == G_QIF_END || ty == G_LIF || ty == G_DIRICHLET;
   const bool uc = ty == G_QIF || ty == G_QIF_END || ty == G_LIF || ty == G_LIF_CORNER;
   const bool ue = ty == G_QIF_END;
-  P.b = ub ? __ldg(G.b + i) : a;
-  P.c = uc ? __ldg(G.c + i) : a;
-  P.d = ue ? __ldg(G.d + i) : a;
-  P.e = ue ? __ldg(G.e + i) : a;
+  P.b = ub ? (kAlt ? __ldg(A->b + i) : __ldg(G.b + i)) : a;
+  P.c = uc ? (kAlt ? __ldg(A->c + i) : __ldg(G.c + i)) : a;
+  // d and e (parent cells of QIF_END) are read directly: unused, they
+  // repeat the item's plain first operand (a cell of Q in every kind that
+  // reaches ghost_value)
+  const int pa = kAlt ? __ldg(G.a + i) : a;
+  P.d = ue ? __ldg(G.d + i) : pa;
+  P.e = ue ? __ldg(G.e + i) : pa;
   P.g = (ty == G_DIRICHLET || ty == G_NEUMANN) ? __ldg(G.e + i) : -1;
   P.nb = ty == G_NEUMANN ? __ldg(G.b + i) : 0;
   return P;
 }
 
-template <class T, bool kCG = false>
-__device__ __forceinline__ void ghost_apply(const GhostItems &G, int i, const GhostPrep &P, T *Q, T *QC, const T *bcg,
-                                            T hx, T hy) {
-  if (P.ty == G_PHYS_CORNER) {
-    ghost_item<T, kCG>(G, i, P.ty, P.dst, Q, QC, bcg, hx, hy);
-    return;
+// a solution operand: a cell of Q, or (code < 0, fused fills only) the
+// restriction of its four fine cells
+template <class T, bool kCG, bool kAlt>
+__device__ __forceinline__ T ghost_operand(const T *Q, int code, const GhostAlt *A) {
+  if (kAlt && code < 0) {
+    const int2 r = __ldg(A->rt + (-1 - code));
+    const T *q = Q + r.x;
+    return T(0.25) * (((ld_sol<kCG>(q) + ld_sol<kCG>(q + 1)) + ld_sol<kCG>(q + r.y)) + ld_sol<kCG>(q + r.y + 1));
   }
-  const T qa = ld_sol<kCG>(Q + P.a), qb = ld_sol<kCG>(Q + P.b), qc = ld_sol<kCG>(Q + P.c);
+  return ld_sol<kCG>(Q + code);
+}
+
+// the value of a prepared item that is not a ring refresh or a corner
+template <class T, bool kCG, bool kAlt>
+__device__ __forceinline__ T ghost_value(const GhostPrep &P, const T *Q, const T *bcg, T hx, T hy,
+                                         const GhostAlt *A) {
+  const T qa = ghost_operand<T, kCG, kAlt>(Q, P.a, A), qb = ghost_operand<T, kCG, kAlt>(Q, P.b, A);
+  const T qc = ghost_operand<T, kCG, kAlt>(Q, P.c, A);
   const T qd = ld_sol<kCG>(Q + P.d), qe = ld_sol<kCG>(Q + P.e);
   const T g = P.g >= 0 ? bcg[P.g] : T(0);
   const T c23 = T(2.0 / 3.0), c13 = T(1.0 / 3.0), c83 = T(8.0 / 3.0);
-  T v;
   switch (P.ty) {
-    case G_RING: QC[P.dst] = qa; return;
-    case G_LIF_CORNER: v = c23 * qc + c13 * qa; break;
-    case G_DIRICHLET: v = (c83 * g - 2 * qa) + c13 * qb; break;
-    case G_NEUMANN: v = qa + (P.nb ? hy : hx) * g; break;
-    default: v = rule_value<T>(P.ty, qa, qb, qc, qd, qe);   // COPY, QIF, QIF_END, LIF
+    case G_LIF_CORNER: return c23 * qc + c13 * qa;
+    case G_DIRICHLET: return (c83 * g - 2 * qa) + c13 * qb;
+    case G_NEUMANN: return qa + (P.nb ? hy : hx) * g;
+    default: return rule_value<T>(P.ty, qa, qb, qc, qd, qe);   // COPY, QIF, QIF_END, LIF
   }
-  Q[P.dst] = v;
+}
+
+template <class T, bool kCG = false, bool kAlt = false>
+__device__ __forceinline__ void ghost_apply(const GhostItems &G, int i, const GhostPrep &P, T *Q, T *QC, const T *bcg,
+                                            T hx, T hy, const GhostAlt *A = nullptr) {
+  if (P.ty == G_PHYS_CORNER) {
+    if (!kAlt) {
+      ghost_item<T, kCG>(G, i, P.ty, P.dst, Q, QC, bcg, hx, hy);
+      return;
+    }
+    // (face ghost 1 + face ghost 2) - interior, each face ghost by its own
+    // rule with the fused fill's operands
+    const int r1 = G.a[i], r2 = G.b[i];
+    const T v1 = ghost_value<T, kCG, true>(ghost_prep<true>(G, r1, G.type[r1], 0, A), Q, bcg, hx, hy, A);
+    const T v2 = ghost_value<T, kCG, true>(ghost_prep<true>(G, r2, G.type[r2], 0, A), Q, bcg, hx, hy, A);
+    Q[P.dst] = (v1 + v2) - ghost_operand<T, kCG, true>(Q, __ldg(A->c + i), A);
+    return;
+  }
+  if (P.ty == G_RING) {
+    QC[P.dst] = ld_sol<kCG>(Q + P.a);
+    return;
+  }
+  Q[P.dst] = ghost_value<T, kCG, kAlt>(P, Q, bcg, hx, hy, A);
 }
 
 // kT threads per block: kBlock, or 64 on a level whose kBlock grid leaves
@@ -783,6 +832,33 @@ template <class T, int kT = kBlock>
 __global__ void __launch_bounds__(kT) k_restrict(LevelD L, Decomp D, FieldsT<T> f, int to_parent) {
   chain_trigger();
   restrict_item<T, true>(L, D, f, to_parent, blockIdx.x * kT + threadIdx.x);
+}
+
+// The restriction of level k into QC and the parent (ebTransfer.m:10-33)
+// and the ghost fill of the parent level that follows it (ebVcycle.m:27,
+// ebTransfer.m:73-79) in one launch: blocks [0, nb_r) restrict, the rest
+// fill level k-1 with the fused operands of GhostAlt (a fill operand under
+// level k's footprint is restricted by the item itself), so no item reads a
+// value another item of the launch writes.
+template <class T, int kT = kBlock>
+__global__ void __launch_bounds__(kT) k_restrict_fill(LevelD L, Decomp D, FieldsT<T> f, int to_parent, int nb_r,
+                                                     GhostItems G, GhostAlt A, int g_off, int g_n, double hx_,
+                                                     double hy_, const int *__restrict__ active,
+                                                     const int *__restrict__ inst_nlev, int need) {
+  chain_trigger();
+  if ((int)blockIdx.x < nb_r) {
+    restrict_item<T, true>(L, D, f, to_parent, blockIdx.x * kT + threadIdx.x);
+    return;
+  }
+  const int t = ((int)blockIdx.x - nb_r) * kT + threadIdx.x;
+  const int i = g_off + t;
+  const int inst = (t < g_n && G.inst) ? G.inst[i] : -1;
+  const bool skip = t >= g_n || (inst >= 0 && (!active[inst] || inst_nlev[inst] < need));
+  GhostPrep P;
+  if (!skip) P = ghost_prep<true>(G, i, G.type[i], G.dst[i], &A);
+  chain_wait();
+  if (skip) return;
+  ghost_apply<T, false, true>(G, i, P, f.Q, f.QC, f.bcg, T(hx_), T(hy_), &A);
 }
 // ---------------------------------------------------------------------------
 // ebFaceCorrections (ebFaceCorrections.m:18-61): correction of coarse face j
