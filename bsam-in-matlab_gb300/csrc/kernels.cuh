@@ -1375,27 +1375,50 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__rest
   chain_in();
   const int inst = blockIdx.x;
   const InstRes R = ir[inst];
-  __shared__ double s_a[kFinal], s_b[kFinal];
   __shared__ int s_write;
   const int t = threadIdx.x;
-  // four independent loads in flight per thread (max is order-free)
+  // one pass over the slots: the max-norms (order-free) and, per level
+  // (range), a fixed-order tree over the threads' partial sums -- four
+  // strided partial sums per thread, then their sum; the levels of a group
+  // are reduced in the same barrier steps (each level's pairings unchanged)
+  // and summed in level order with their areas
   double li = 0, fn = 0;
-  for (int r = R.range0; r < R.range1; ++r) {
-    const int s0 = ranges[r].s0, s1 = ranges[r].s1;
-    int i = s0 + t;
-    for (; i + 3 * kFinal < s1; i += 4 * kFinal) {
-      const double a0 = slots[i], a1 = slots[i + kFinal], a2 = slots[i + 2 * kFinal], a3 = slots[i + 3 * kFinal];
-      const double b0 = slots[2 * nslots + i], b1 = slots[2 * nslots + i + kFinal];
-      const double b2 = slots[2 * nslots + i + 2 * kFinal], b3 = slots[2 * nslots + i + 3 * kFinal];
-      li = pmax(li, pmax(pmax(a0, a1), pmax(a2, a3)));
-      fn = pmax(fn, pmax(pmax(b0, b1), pmax(b2, b3)));
+  __shared__ double s_p[kFinalGroup][kFinal];
+  __shared__ double s_a[kFinal / 32 + 1], s_b[kFinal / 32 + 1];
+  double l2sq = 0;
+  for (int r0 = R.range0; r0 < R.range1; r0 += kFinalGroup) {
+    const int nr = min(kFinalGroup, R.range1 - r0);
+    for (int q = 0; q < nr; ++q) {
+      const int s0 = ranges[r0 + q].s0, s1 = ranges[r0 + q].s1;
+      double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+      int i = s0 + t;
+      for (; i + 3 * kFinal < s1; i += 4 * kFinal) {
+        const double a0 = slots[i], a1 = slots[i + kFinal], a2 = slots[i + 2 * kFinal], a3 = slots[i + 3 * kFinal];
+        const double b0 = slots[2 * nslots + i], b1 = slots[2 * nslots + i + kFinal];
+        const double b2 = slots[2 * nslots + i + 2 * kFinal], b3 = slots[2 * nslots + i + 3 * kFinal];
+        p0 = p0 + slots[nslots + i];
+        p1 = p1 + slots[nslots + i + kFinal];
+        p2 = p2 + slots[nslots + i + 2 * kFinal];
+        p3 = p3 + slots[nslots + i + 3 * kFinal];
+        li = pmax(li, pmax(pmax(a0, a1), pmax(a2, a3)));
+        fn = pmax(fn, pmax(pmax(b0, b1), pmax(b2, b3)));
+      }
+      for (; i < s1; i += kFinal) {
+        p0 = p0 + slots[nslots + i];
+        li = pmax(li, slots[i]);
+        fn = pmax(fn, slots[2 * nslots + i]);
+      }
+      s_p[q][t] = (p0 + p1) + (p2 + p3);
     }
-    for (; i < s1; i += kFinal) {
-      li = pmax(li, slots[i]);
-      fn = pmax(fn, slots[2 * nslots + i]);
+    __syncthreads();
+    for (int off = kFinal / 2; off >= 1; off >>= 1) {
+      if (t < off)
+        for (int q = 0; q < nr; ++q) s_p[q][t] = s_p[q][t] + s_p[q][t + off];
+      __syncthreads();
     }
+    for (int q = 0; q < nr; ++q) l2sq = l2sq + s_p[q][0] * ranges[r0 + q].area;
+    __syncthreads();
   }
-  // a max is order-free: warp shuffles, then one shared stage
 #pragma unroll
   for (int off = 16; off >= 1; off >>= 1) {
     li = pmax(li, __shfl_xor_sync(0xffffffffu, li, off));
@@ -1422,37 +1445,6 @@ __global__ void __launch_bounds__(kFinal) k_residual_final(const InstRes *__rest
   __syncthreads();
   const double linf = s_a[kFinal / 32];
   double fnorm = s_b[kFinal / 32];
-  // L2: per level (range) a fixed-order tree over the threads' partial
-  // sums; the levels of a group are loaded together and reduced in the same
-  // barrier steps (each level's pairings unchanged), then summed in level
-  // order with their areas
-  __shared__ double s_p[kFinalGroup][kFinal];
-  double l2sq = 0;
-  for (int r0 = R.range0; r0 < R.range1; r0 += kFinalGroup) {
-    const int nr = min(kFinalGroup, R.range1 - r0);
-    for (int q = 0; q < nr; ++q) {
-      // fixed order: four strided partial sums per thread, then their sum
-      const int s0 = ranges[r0 + q].s0, s1 = ranges[r0 + q].s1;
-      double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
-      int i = s0 + t;
-      for (; i + 3 * kFinal < s1; i += 4 * kFinal) {
-        p0 = p0 + slots[nslots + i];
-        p1 = p1 + slots[nslots + i + kFinal];
-        p2 = p2 + slots[nslots + i + 2 * kFinal];
-        p3 = p3 + slots[nslots + i + 3 * kFinal];
-      }
-      for (; i < s1; i += kFinal) p0 = p0 + slots[nslots + i];
-      s_p[q][t] = (p0 + p1) + (p2 + p3);
-    }
-    __syncthreads();
-    for (int off = kFinal / 2; off >= 1; off >>= 1) {
-      if (t < off)
-        for (int q = 0; q < nr; ++q) s_p[q][t] = s_p[q][t] + s_p[q][t + off];
-      __syncthreads();
-    }
-    for (int q = 0; q < nr; ++q) l2sq = l2sq + s_p[q][0] * ranges[r0 + q].area;
-    __syncthreads();
-  }
   if (t == 0) {
     int wr = -1;
     fnorm = fnorm > 2.2250738585072014e-308 ? fnorm : 2.2250738585072014e-308;
