@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <unordered_map>
 #include <mutex>
@@ -185,6 +186,10 @@ struct bsam_hier_s {
   cudaGraph_t wgraph = nullptr;
   cudaGraphExec_t wexec = nullptr;
   bool while_tried = false;
+  // the whole solve -- preamble and device-side loop -- as one graph
+  cudaGraph_t sgraph = nullptr;
+  cudaGraphExec_t sexec = nullptr;
+  bool solve_tried = false;
   int64_t kernels_per_cycle = 0;
   // profiling
   bool profiling = false;
@@ -194,6 +199,8 @@ struct bsam_hier_s {
   int64_t launch_count = 0;
   int64_t graph_launches = 0;
   int64_t while_bodies = 0;        // iterations run inside WHILE graphs
+  int64_t solve_graphs = 0;        // solves run as one graph launch
+  int64_t preamble_kernels = 0;    // kernels of such a solve before its loop
   // per precision and level: colour cells per smoother thread (1, 2, 4),
   // picked by the autotuner at the first solve (result-neutral)
   std::vector<int> relax_n[2];
@@ -893,6 +900,11 @@ void drop_graph(bsam_hier h) {
   if (h->graph) cudaGraphDestroy(h->graph);
   if (h->wexec) cudaGraphExecDestroy(h->wexec);
   if (h->wgraph) cudaGraphDestroy(h->wgraph);
+  if (h->sexec) cudaGraphExecDestroy(h->sexec);
+  if (h->sgraph) cudaGraphDestroy(h->sgraph);
+  h->sexec = nullptr;
+  h->sgraph = nullptr;
+  h->solve_tried = false;
   h->gexec = nullptr;
   h->graph = nullptr;
   h->wexec = nullptr;
@@ -939,7 +951,7 @@ bool build_while_graph(bsam_hier h) {
       const int64_t before = h->launch_count;
       const int rc = launch_iteration(h, 1);
       h->kernels_per_cycle = h->launch_count - before;
-      launch_k(h, k_any_active, 1, kBlock, (const int *)h->active.p, h->ninst, cond);
+      launch_k(h, k_any_active, 1, kBlock, (const int *)h->active.p, h->ninst, cond, cond, 0);
       cudaGraph_t out = nullptr;
       ok = cudaStreamEndCapture(h->stream, &out) == cudaSuccess && rc == BSAM_OK;
       h->launch_count = before;
@@ -955,6 +967,102 @@ bool build_while_graph(bsam_hier h) {
   }
   h->wgraph = g;
   return true;
+}
+
+// a conditional node after the capturing stream's current dependencies,
+// whose body graph is captured from `body` (launches on the hierarchy's
+// stream, redirected to a helper stream); the capture continues after it
+bool add_conditional(bsam_hier h, cudaStream_t helper, cudaGraphConditionalHandle cond, cudaGraphConditionalNodeType ty,
+                     const std::function<int()> &body) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t cg = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  if (cudaStreamGetCaptureInfo(h->stream, &st, nullptr, &cg, &deps, nullptr, &nd) != cudaSuccess ||
+      st != cudaStreamCaptureStatusActive)
+    return false;
+  std::vector<cudaGraphNode_t> dv(deps, deps + nd);
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = cond;
+  np.conditional.type = ty;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, cg, dv.data(), nullptr, dv.size(), &np) != cudaSuccess) return false;
+  const cudaStream_t main = h->stream;
+  h->stream = helper;
+  bool ok = cudaStreamBeginCaptureToGraph(helper, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  int rc = BSAM_OK;
+  if (ok) {
+    rc = body();
+    cudaGraph_t out = nullptr;
+    ok = cudaStreamEndCapture(helper, &out) == cudaSuccess && rc == BSAM_OK;
+  }
+  h->stream = main;
+  return ok && cudaStreamUpdateCaptureDependencies(main, &node, nullptr, 1, cudaStreamSetCaptureDependencies) ==
+                   cudaSuccess;
+}
+
+// ebSolveCycles.m:8-70 as one graph: the preamble (F = FTrue, the ghost fill
+// of every level, the initial residual and stop test; in the mixed form,
+// while an instance iterates, the consistency step and the first
+// correction's right-hand side) and then the device-side loop, so a solve
+// is one graph launch and one read of the results.  Built once the smoother
+// is tuned; returns false (and the step-by-step path is used) when the
+// runtime cannot build it.
+bool build_solve_graph(bsam_hier h) {
+  if (h->sexec) return true;
+  if (h->solve_tried) return false;
+  h->solve_tried = true;
+  cudaStream_t helper = nullptr;
+  if (cudaStreamCreateWithFlags(&helper, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const int64_t before = h->launch_count;
+  bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  cudaGraphConditionalHandle wcond = 0, icond = 0;
+  if (ok) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cg = nullptr;
+    ok = cudaStreamGetCaptureInfo(h->stream, &st, nullptr, &cg, nullptr, nullptr, nullptr) == cudaSuccess &&
+         cudaGraphConditionalHandleCreate(&wcond, cg, 1, cudaGraphCondAssignDefault) == cudaSuccess &&
+         (!mixed(h) || cudaGraphConditionalHandleCreate(&icond, cg, 1, cudaGraphCondAssignDefault) == cudaSuccess);
+    if (ok) {
+      if (!mixed(h)) reset_force(h);
+      for (int k = 1; k <= h->nlev; ++k) launch_fill(h, k);
+      launch_residual(h, 0);
+      launch_k(h, k_any_active, 1, kBlock, (const int *)h->active.p, h->ninst, wcond, icond, mixed(h) ? 1 : 0);
+      h->preamble_kernels = h->launch_count - before;
+      if (mixed(h))
+        ok = add_conditional(h, helper, icond, cudaGraphCondTypeIf, [h]() {
+          launch_consistent(h);
+          launch_residual(h, 2);
+          return cudaGetLastError() == cudaSuccess ? BSAM_OK : BSAM_ERR_CUDA;
+        });
+      if (ok)
+        ok = add_conditional(h, helper, wcond, cudaGraphCondTypeWhile, [h, wcond]() {
+          const int rc = launch_iteration(h, 1);
+          launch_k(h, k_any_active, 1, kBlock, (const int *)h->active.p, h->ninst, wcond, wcond, 0);
+          return rc;
+        });
+    }
+    cudaGraph_t g = nullptr;
+    const bool ended = cudaStreamEndCapture(h->stream, &g) == cudaSuccess;
+    ok = ok && ended;
+    if (ok) ok = cudaGraphInstantiate(&h->sexec, g, 0) == cudaSuccess;
+    if (ok) h->sgraph = g;
+    else if (g) cudaGraphDestroy(g);
+  }
+  h->launch_count = before;
+  cudaStreamDestroy(helper);
+  cudaGetLastError();   // a refused build leaves no sticky error behind
+  if (!ok) {
+    if (h->sexec) cudaGraphExecDestroy(h->sexec);
+    h->sexec = nullptr;
+  }
+  return ok;
 }
 
 // per-instance residuals and active flags -> host (pinned); returns the
@@ -988,6 +1096,8 @@ int upload_stops(bsam_hier h) {
     h->hist_stride = stride;
     if ((rc = h->hist.alloc((size_t)h->ninst * stride))) return rc;
   }
+  // the graphs hold the reduction plan's and history's device addresses
+  drop_graph(h);
   h->instres.release();
   if ((rc = h->instres.upload(h->hir.data(), h->hir.size(), h->stream))) return rc;
   CK(cudaStreamSynchronize(h->stream));
@@ -2108,17 +2218,29 @@ int bsam_vcycle(bsam_hier h) {
   return BSAM_OK;
 }
 
+static int finish_solve(bsam_hier h, bool on_device, double *res_hist, int hist_cap, int *vcycles,
+                        double *final_rel, int64_t *visible_cells);
+
 int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles, double *final_rel,
                       int64_t *visible_cells) {
   if (!h) return fail(BSAM_ERR_ARG, "null hierarchy");
   int rc = set_device(h);
   if (rc) return rc;
   if ((rc = ensure_f32(h))) return rc;
+  int nactive = 0;
+  bool on_device = false;
+  if (h->tuned[mixed(h) ? 1 : 0] && !host_loop() && build_solve_graph(h)) {
+    // the whole solve in one graph launch (once the smoother is tuned)
+    CK(cudaGraphLaunch(h->sexec, h->stream));
+    h->solve_graphs++;
+    if ((rc = read_state(h, &nactive))) return rc;
+    on_device = true;
+    return finish_solve(h, on_device, res_hist, hist_cap, vcycles, final_rel, visible_cells);
+  }
   if (!mixed(h)) reset_force(h);
   for (int k = 1; k <= h->nlev; ++k) launch_fill(h, k);
   launch_residual(h, 0);
   CK(cudaGetLastError());
-  int nactive = 0;
   if ((rc = read_state(h, &nactive))) return rc;
   if (nactive && mixed(h)) {
     // the history starts with the reference's own initial residual; the
@@ -2130,7 +2252,6 @@ int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles,
   // instance of a batch is frozen (its stores are predicated off) while the
   // others continue.  The loop runs on the device when the runtime can build
   // its WHILE graph, else one graph launch per V-cycle with a host check.
-  bool on_device = false;
   if (nactive && (rc = autotune(h))) return rc;
   if (nactive && !host_loop() && build_while_graph(h)) {
     CK(cudaGraphLaunch(h->wexec, h->stream));
@@ -2143,6 +2264,13 @@ int bsam_solve_cycles(bsam_hier h, double *res_hist, int hist_cap, int *vcycles,
     h->graph_launches++;
     if ((rc = read_state(h, &nactive))) return rc;
   }
+  return finish_solve(h, on_device, res_hist, hist_cap, vcycles, final_rel, visible_cells);
+}
+
+// the results of a solve: residual histories and V-cycle counts to the host,
+// every instance active again for eager operations
+static int finish_solve(bsam_hier h, bool on_device, double *res_hist, int hist_cap, int *vcycles,
+                        double *final_rel, int64_t *visible_cells) {
   h->res_hist.resize((size_t)h->ninst * h->hist_stride);
   h->res_iters.resize(h->ninst);
   h->res_acc.assign(h->acc_host, h->acc_host + h->ninst);
@@ -2304,7 +2432,8 @@ int bsam_restore_state(bsam_hier h) {
 
 int bsam_launch_count(bsam_hier h, int64_t *count) {
   if (!h || !count) return fail(BSAM_ERR_ARG, "null argument");
-  *count = h->launch_count + h->graph_launches * h->kernels_per_cycle + h->while_bodies * (h->kernels_per_cycle + 1);
+  *count = h->launch_count + h->graph_launches * h->kernels_per_cycle + h->while_bodies * (h->kernels_per_cycle + 1) +
+           h->solve_graphs * h->preamble_kernels;
   return BSAM_OK;
 }
 

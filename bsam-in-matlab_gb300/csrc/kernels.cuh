@@ -1506,7 +1506,8 @@ __global__ void __launch_bounds__(kBlock) k_fp64_rate(double *out, int iters, do
 // still iterates (ebSolveCycles.m:22, per instance).  One block; a single
 // thread sets the condition.
 __global__ void __launch_bounds__(kBlock) k_any_active(const int *__restrict__ active, int ninst,
-                                                       cudaGraphConditionalHandle cond) {
+                                                       cudaGraphConditionalHandle cond,
+                                                       cudaGraphConditionalHandle cond2, int use2) {
   chain_in();
   __shared__ int any;
   if (threadIdx.x == 0) any = 0;
@@ -1514,7 +1515,10 @@ __global__ void __launch_bounds__(kBlock) k_any_active(const int *__restrict__ a
   for (int i = threadIdx.x; i < ninst; i += kBlock)
     if (active[i]) any = 1;   // benign: every writer stores 1
   __syncthreads();
-  if (threadIdx.x == 0) cudaGraphSetConditional(cond, any ? 1u : 0u);
+  if (threadIdx.x == 0) {
+    cudaGraphSetConditional(cond, any ? 1u : 0u);
+    if (use2) cudaGraphSetConditional(cond2, any ? 1u : 0u);
+  }
 }
 
 // ---------------------------------------------------------------------------
