@@ -1083,9 +1083,37 @@ __global__ void __launch_bounds__(kT) k_load(LevelD L, LevelD Lc, Decomp D, Fiel
 // writes its four fine cells.
 // kT threads per block: kBlock, or 64 on a level whose kBlock grid leaves
 // SMs idle (about 37 FP64 operations per coarse cell, two per clock per SM)
+// A parent-window operand of the prolongation fused with the parent level's
+// closing fill (k_fill_prolong): a code >= 0 is a cell of Q; a code < 0 is
+// the ghost cell that ghost item -1 - code fills in the same launch, whose
+// value the prolongation forms itself from the item's rule (the rule reads
+// interior cells and the level below, which the launch does not write) --
+// the value the fill stores, bit for bit.
+template <class T>
+struct WindowGhosts {
+  const int *win;              // window tables, ghost cells coded
+  GhostItems G;
+  const T *bcg;
+  T hx, hy;                    // cell size of the parent level (the ghosts' level)
+};
+
+template <class T>
+__device__ __forceinline__ T window_value(const T *Q, int code, const WindowGhosts<T> *W) {
+  if (W == nullptr || code >= 0) return Q[code];
+  const int i = -1 - code;
+  const GhostItems &G = W->G;
+  const int8_t ty = G.type[i];
+  if (ty == G_PHYS_CORNER) {
+    const T v1 = eval_rule<T>(G, G.a[i], Q, W->bcg, W->hx, W->hy);
+    const T v2 = eval_rule<T>(G, G.b[i], Q, W->bcg, W->hx, W->hy);
+    return (v1 + v2) - Q[G.c[i]];
+  }
+  return eval_rule<T>(G, i, Q, W->bcg, W->hx, W->hy);
+}
+
 template <class T, bool kChain>
 __device__ __forceinline__ void prolong_item(const LevelD &L, const Decomp &D, const FieldsT<T> &f, int correct,
-                                             int g) {
+                                             int g, const WindowGhosts<T> *W = nullptr) {
   if (g >= D.n) {
     if (kChain) chain_wait();
     return;
@@ -1100,7 +1128,7 @@ __device__ __forceinline__ void prolong_item(const LevelD &L, const Decomp &D, c
   const int s = g - __ldg(D.beg + p);
   const int b = s / cm, a = s - b * cm;
   const int ldw = cm + 2;
-  const int *win = f.win + P.win_off;
+  const int *win = (W ? W->win : f.win) + P.win_off;
   int src[3][3];
 #pragma unroll
   for (int dj = 0; dj < 3; ++dj)
@@ -1115,7 +1143,7 @@ __device__ __forceinline__ void prolong_item(const LevelD &L, const Decomp &D, c
 #pragma unroll
     for (int di = 0; di < 3; ++di) {
       const int w = (a + di) + (b + dj) * ldw;
-      const T wv = f.Q[src[dj][di]];
+      const T wv = window_value<T>(f.Q, src[dj][di], W);
       E[dj][di] = correct ? wv - QC[w] : wv;
     }
   const T C = E[1][1], Wm = E[1][0], Wp = E[1][2], Sm = E[0][1], Sp = E[2][1];
@@ -1142,6 +1170,32 @@ template <class T, int kT = kBlock>
 __global__ void __launch_bounds__(kT) k_prolong(LevelD L, Decomp D, FieldsT<T> f, int correct) {
   chain_trigger();
   prolong_item<T, true>(L, D, f, correct, blockIdx.x * kT + threadIdx.x);
+}
+
+// The closing ghost fill of level k-1 (the end of its V-cycle) and the
+// prolongation-correction of level k that follows it (ebVcycle.m:31-32) in
+// one launch: blocks [0, nb_g) fill level k-1, the rest prolong into level
+// k, forming any parent-window ghost from its rule (WindowGhosts), so no
+// item reads what another item of the launch writes.
+template <class T, int kT = kBlock>
+__global__ void __launch_bounds__(kT) k_fill_prolong(GhostItems G, int g_off, int g_n, int nb_g, LevelD L, Decomp D,
+                                                    FieldsT<T> f, int correct, WindowGhosts<T> W,
+                                                    const int *__restrict__ active,
+                                                    const int *__restrict__ inst_nlev) {
+  chain_trigger();
+  if ((int)blockIdx.x < nb_g) {
+    const int t = blockIdx.x * kT + threadIdx.x;
+    const int i = g_off + t;
+    const int inst = (t < g_n && G.inst) ? G.inst[i] : -1;
+    const bool skip = t >= g_n || (inst >= 0 && !active[inst]);
+    GhostPrep P;
+    if (!skip) P = ghost_prep(G, i, G.type[i], G.dst[i]);
+    chain_wait();
+    if (skip) return;
+    ghost_apply<T>(G, i, P, f.Q, f.QC, f.bcg, W.hx, W.hy);
+    return;
+  }
+  prolong_item<T, true>(L, D, f, correct, ((int)blockIdx.x - nb_g) * kT + threadIdx.x, &W);
 }
 
 // ---------------------------------------------------------------------------
