@@ -90,6 +90,7 @@ def lib():
         L.bsam_mass_check.argtypes = [P, P]
         L.bsam_stream.argtypes = [P, C.POINTER(P)]
         L.bsam_profile_vcycles.argtypes = [P, C.c_int, C.c_int, P, P, P]
+        L.bsam_time_relax.argtypes = [P, C.c_int, C.c_int, C.POINTER(D)]
         L.bsam_kernels_per_vcycle.argtypes = [P, C.POINTER(I64)]
         L.bsam_save_state.argtypes = [P]
         L.bsam_restore_state.argtypes = [P]
@@ -330,6 +331,13 @@ class DevHier:
         by = np.zeros(NKINDS)
         check(lib().bsam_profile_vcycles(self.h, int(ncycles), int(level), _ptr(ms), _ptr(nl), _ptr(by)))
         return {KIND_NAMES[i]: {'ms': ms[i], 'launches': int(nl[i]), 'bytes': by[i]} for i in range(NKINDS)}
+
+    def time_relax(self, level, reps=20):
+        """Microseconds per colour pass of `level`'s smoother, replayed as a
+        graph of chained launches (bsam_time_relax)."""
+        us = D(0)
+        check(lib().bsam_time_relax(self.h, int(level), int(reps), C.byref(us)))
+        return us.value
 
     def save_state(self):
         check(lib().bsam_save_state(self.h))

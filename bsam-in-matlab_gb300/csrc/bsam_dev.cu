@@ -2524,6 +2524,40 @@ int bsam_kernels_per_vcycle(bsam_hier h, int64_t *count) {
   return BSAM_OK;
 }
 
+int bsam_time_relax(bsam_hier h, int level, int reps, double *us) {
+  if (!h || !us || level < 2 || level > h->nlev || reps < 1) return fail(BSAM_ERR_ARG, "bad argument");
+  int rc = set_device(h);
+  if (rc || (rc = ensure_f32(h))) return rc;
+  if (!h->tuned[mixed(h) ? 1 : 0]) return fail(BSAM_ERR_STATE, "bsam_time_relax: the smoother is not tuned yet");
+  const int ns = std::max(h->opts.npre, 1);
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const int64_t before = h->launch_count;
+  if (mixed(h)) launch_relax<float>(h, level, ns, false, true);
+  else launch_relax<double>(h, level, ns, false, true);
+  h->launch_count = before;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamEndCapture(h->stream, &g));
+  cudaGraphExec_t ge = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = cudaGraphLaunch(ge, h->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(a, h->stream);
+  for (int i = 0; i < reps && e == cudaSuccess; ++i) e = cudaGraphLaunch(ge, h->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(b, h->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  float ms = 0;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (ge) cudaGraphExecDestroy(ge);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "bsam_time_relax");
+  *us = 1e3 * (double)ms / ((double)reps * 2 * ns);
+  return BSAM_OK;
+}
+
 int bsam_profile_vcycles(bsam_hier h, int ncycles, int level, double ms[BSAM_NKINDS], int64_t launches[BSAM_NKINDS],
                          double bytes[BSAM_NKINDS]) {
   if (!h || !ms || !launches || !bytes || ncycles < 1 || level < 0 || level > h->nlev)

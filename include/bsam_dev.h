@@ -238,6 +238,14 @@ int bsam_mass_check(bsam_hier h, double out[4]);
  * algorithmic bytes. */
 int bsam_stream(bsam_hier h, void **stream);
 #define BSAM_NKINDS 9
+/* Live cost of one colour pass of level `level`'s smoother in the solve's
+ * precision: the npre-sweep relaxation's colour passes (no closing fill)
+ * captured as one graph of programmatic-launch-chained kernels, as the
+ * solve's graph runs them, replayed `reps` times with CUDA events on the
+ * hierarchy's stream; *us = microseconds per pass.  Works on the live state
+ * (the caller restores it); the smoother must be tuned (a solve ran).  No
+ * counterpart in the reference: measurement. */
+int bsam_time_relax(bsam_hier h, int level, int reps, double *us);
 int bsam_profile_vcycles(bsam_hier h, int ncycles, int level, double ms[BSAM_NKINDS],
                          int64_t launches[BSAM_NKINDS], double bytes[BSAM_NKINDS]);
 

@@ -46,6 +46,7 @@ def test_native_line():
     assert r['bound'] == 'hbm' and r['unit'] == 'GB/s' and 0 < r['frac'] < 1.5
     assert abs(r['frac'] - r['achieved'] / r['peak']) < 1e-9 and r['traffic'] and r['traffic'] > 0
     assert 0 < r['fp64_pipe']['frac'] < 1.5
+    assert r['avg_launch_us'] > 0 and r['eager_avg_launch_us'] > 0 and 'graph' in r['timing']
     e = d['e2e']
     assert e['unit'] == 'solves/s' and e['h2d_bytes_per_step'] > 0 and e['d2h_bytes_per_step'] > 0
     assert d['gpu_launches'] > 1000
