@@ -112,6 +112,10 @@ struct LevelPlan {
   // corrections contributed by this (fine) level, targets in level k-1
   int ct_off = 0, ct_n = 0;
   int64_t ncells = 0;
+  // may this level's own closing fill join the launch of its restriction
+  // into the parent (k_restrict_fill): after the pre-smoothing (ring items
+  // left out), and with its ring items before the fill-down (set at upload)
+  bool fuse_pre = false, fuse_top = false;
 };
 
 }  // namespace
@@ -539,11 +543,17 @@ void launch_restrict(bsam_hier h, int k, int to_parent) {
 }
 
 // restriction of level k into QC and level k-1, then the ghost fill of
-// level k-1 (launch_restrict + launch_fill(k - 1, k)) in one launch
+// level k-1 (launch_restrict + launch_fill(k - 1, k)) in one launch.  With
+// fill_k, level k's own fill that precedes them (launch_fill(k)) joins the
+// launch too: FILL_PRE after the pre-smoothing (ring items left out), FILL_TOP
+// before the fill-down; the caller checks the level's fuse_pre / fuse_top.
+enum { FILL_NONE = 0, FILL_PRE = 1, FILL_TOP = 2 };
+
 template <class T = double>
-void launch_restrict_fill(bsam_hier h, int k) {
+void launch_restrict_fill(bsam_hier h, int k, int fill_k = FILL_NONE) {
   const LevelPlan &L = h->lev[k], &Lc = h->lev[k - 1];
   if (!Lc.g1_n) {
+    if (fill_k) launch_fill<T>(h, k);
     launch_restrict<T>(h, k, 1);
     return;
   }
@@ -551,14 +561,17 @@ void launch_restrict_fill(bsam_hier h, int k) {
   FieldsT<T> f = fields_t<T>(h);
   Launch l(h, K_RESTRICT, 12.0 * tscale<T>() * (double)L.ncells, k);
   const GhostAlt A{h->ga_a.p, h->ga_b.p, h->ga_c.p, h->ga_rt.p};
-  if (nblk(D.n) + nblk(Lc.g1_n) < spread_limit(h)) {
-    const int nb = (D.n + 63) / 64;
-    launch_k(h, k_restrict_fill<T, 64>, nb + (Lc.g1_n + 63) / 64, 64, leveld(h, k), D, f, 1, nb, ghost_items(h),
-             A, Lc.g1_off, Lc.g1_n, Lc.hx, Lc.hy, (const int *)h->active.p, (const int *)h->inst_nlev.p, k);
+  const int fn = fill_k ? L.g1_n : 0, fring = fill_k == FILL_TOP ? 1 : 0;
+  if (nblk(D.n) + nblk(Lc.g1_n) + nblk(fn) < spread_limit(h)) {
+    const int nb = (D.n + 63) / 64, nf = (fn + 63) / 64;
+    launch_k(h, k_restrict_fill<T, 64>, nb + nf + (Lc.g1_n + 63) / 64, 64, leveld(h, k), D, f, 1, nb,
+             ghost_items(h), A, Lc.g1_off, Lc.g1_n, Lc.hx, Lc.hy, (const int *)h->active.p,
+             (const int *)h->inst_nlev.p, k, L.g1_off, fn, nf, fring, L.hx, L.hy);
   } else {
-    const int nb = nblk(D.n);
-    launch_k(h, k_restrict_fill<T>, nb + nblk(Lc.g1_n), kBlock, leveld(h, k), D, f, 1, nb, ghost_items(h), A,
-             Lc.g1_off, Lc.g1_n, Lc.hx, Lc.hy, (const int *)h->active.p, (const int *)h->inst_nlev.p, k);
+    const int nb = nblk(D.n), nf = nblk(fn);
+    launch_k(h, k_restrict_fill<T>, nb + nf + nblk(Lc.g1_n), kBlock, leveld(h, k), D, f, 1, nb, ghost_items(h), A,
+             Lc.g1_off, Lc.g1_n, Lc.hx, Lc.hy, (const int *)h->active.p, (const int *)h->inst_nlev.p, k, L.g1_off,
+             fn, nf, fring, L.hx, L.hy);
   }
 }
 
@@ -626,12 +639,19 @@ void launch_fill_prolong(bsam_hier h, int k) {
 // prolongation items wait for the parent ghosts' rules on top of their FP64
 // work, and the starfish iteration measured 1.4% slower fused (the FP32
 // cycle 1% faster); both forms give the same bits.
+// the smoother's launch form of level k in the cycle's precision (1 before
+// the autotuner ran)
+template <class T>
+int relax_form(bsam_hier h, int k) {
+  const std::vector<int> &rn = h->relax_n[sizeof(T) == sizeof(float) ? 1 : 0];
+  return rn.empty() ? 1 : rn[k];
+}
+
 template <class T>
 bool fill_deferrable(bsam_hier h, int k) {
   if (sizeof(T) == sizeof(double)) return false;
   if (k == 1 || h->opts.npost <= 0) return true;
-  const std::vector<int> &rn = h->relax_n[sizeof(T) == sizeof(float) ? 1 : 0];
-  return rn.empty() || rn[k] != 0;
+  return relax_form<T>(h, k) != 0;
 }
 
 // the FP32 correction cycle solves a homogeneous problem: no boundary rhs
@@ -668,8 +688,11 @@ void launch_vcycle(bsam_hier h, int k, bool defer_fill = false) {
     launch_coarsest<T>(h, defer_fill);
     return;
   }
-  launch_relax<T>(h, k, h->opts.npre);
-  launch_restrict_fill<T>(h, k);
+  // the pre-smoothing's closing fill joins the restriction's launch (unless
+  // the relaxation runs as one cluster launch, which fills the level itself)
+  const bool pre_fused = h->opts.npre > 0 && relax_form<T>(h, k) != 0 && h->lev[k].fuse_pre;
+  launch_relax<T>(h, k, h->opts.npre, false, pre_fused);
+  launch_restrict_fill<T>(h, k, pre_fused ? FILL_PRE : FILL_NONE);
   launch_coarse_load<T>(h, k);
   const bool fused = fill_deferrable<T>(h, k - 1);
   launch_vcycle<T>(h, k - 1, fused);
@@ -686,8 +709,10 @@ void launch_vcycle(bsam_hier h, int k, bool defer_fill = false) {
   }
 }
 
-void launch_filldown(bsam_hier h) {
-  for (int kk = h->nlev; kk >= 2; --kk) launch_restrict_fill(h, kk);
+// ebTransfer 'filldown' (ebTransfer.m:73-79); top_fill: the finest level's
+// closing fill (left to it by launch_vcycle) joins the first launch
+void launch_filldown(bsam_hier h, bool top_fill = false) {
+  for (int kk = h->nlev; kk >= 2; --kk) launch_restrict_fill(h, kk, top_fill && kk == h->nlev ? FILL_TOP : FILL_NONE);
 }
 
 bool mixed(bsam_hier h) { return h->opts.precision == 1; }
@@ -764,8 +789,11 @@ int launch_iteration(bsam_hier h, int mode) {
     CK(cudaGetLastError());
     return BSAM_OK;
   }
-  launch_vcycle(h, h->nlev);
-  launch_filldown(h);
+  // the finest level's closing fill joins the fill-down's first launch
+  const bool top = h->nlev >= 2 && h->lev[h->nlev].fuse_top &&
+                   (h->opts.npost <= 0 || relax_form<double>(h, h->nlev) != 0);
+  launch_vcycle(h, h->nlev, top);
+  launch_filldown(h, top);
   launch_residual(h, mode);
   CK(cudaGetLastError());
   return BSAM_OK;
@@ -1160,6 +1188,26 @@ int apply_opts(bsam_hier h) {
 
 // ---------------------------------------------------------------------------
 // plan construction
+
+// the Q cells ghost item i reads (its rule's operands; a physical corner
+// reads those of its two face rules and an interior cell)
+template <class BT>
+void ghost_reads(const BT &B, int i, std::vector<int> &out) {
+  switch (B.gt[i]) {
+    case G_COPY: case G_NEUMANN: case G_RING: out.push_back(B.ga[i]); break;
+    case G_DIRICHLET: out.insert(out.end(), {B.ga[i], B.gb[i]}); break;
+    case G_LIF_CORNER: out.insert(out.end(), {B.ga[i], B.gc[i]}); break;
+    case G_QIF: case G_LIF: out.insert(out.end(), {B.ga[i], B.gb[i], B.gc[i]}); break;
+    case G_QIF_END: out.insert(out.end(), {B.ga[i], B.gb[i], B.gc[i], B.gd[i], B.ge[i]}); break;
+    case G_PHYS_CORNER:
+      ghost_reads(B, B.ga[i], out);
+      ghost_reads(B, B.gb[i], out);
+      out.push_back(B.gc[i]);
+      break;
+    default: break;
+  }
+}
+
 struct Builder {
   bsam_hier h;
   const bsam_hier_desc *d;
@@ -1788,6 +1836,37 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
         if (t == G_QIF || t == G_QIF_END || t == G_LIF || t == G_DIRICHLET) ab[i] = code(B.gb[i]);
         if (t == G_QIF || t == G_QIF_END || t == G_LIF || t == G_LIF_CORNER) ac[i] = code(B.gc[i]);
       }
+      // level k's own fill in the same launch (launch_restrict_fill with
+      // fill_k): allowed when no rule of it reads a cell the restriction or
+      // the parent's fill writes and the parent's fill reads no ghost cell of
+      // level k.  Its ring items read parent cells, which the restriction
+      // overwrites where a sibling patch covers them: after the
+      // pre-smoothing they are left out (the coarse load refreshes every
+      // ring cell of the level before anything reads one); before the
+      // fill-down they must run, so they must read no such cell.
+      std::unordered_map<int, int> pw, gw;   // Q cells the parent's / level k's fill writes
+      for (int i = Lc.g1_off; i < Lc.g1_off + Lc.g1_n; ++i)
+        if (B.gt[i] != G_RING) pw[B.gdst[i]] = i;
+      for (int i = L.g1_off; i < L.g1_off + L.g1_n; ++i)
+        if (B.gt[i] != G_RING) gw[B.gdst[i]] = i;
+      std::vector<int> rd;
+      bool ok = true, ring_ok = true;
+      for (int i = L.g1_off; i < L.g1_off + L.g1_n && ok; ++i) {
+        rd.clear();
+        ghost_reads(B, i, rd);
+        for (int q : rd) {
+          const bool hit = cov.count(q) || pw.count(q);
+          if (B.gt[i] == G_RING) ring_ok &= !hit;
+          else ok &= !hit;
+        }
+      }
+      for (int i = Lc.g1_off; i < Lc.g1_off + Lc.g1_n && ok; ++i) {
+        rd.clear();
+        ghost_reads(B, i, rd);
+        for (int q : rd) ok &= !gw.count(q);
+      }
+      h->lev[k].fuse_pre = ok;
+      h->lev[k].fuse_top = ok && ring_ok;
     }
     // windows: parent ghost cells -> the parent level's item filling them
     std::vector<int> walt(d->win, d->win + d->n_win);

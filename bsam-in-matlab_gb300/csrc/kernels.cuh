@@ -840,17 +840,39 @@ __global__ void __launch_bounds__(kT) k_restrict(LevelD L, Decomp D, FieldsT<T> 
 // fill level k-1 with the fused operands of GhostAlt (a fill operand under
 // level k's footprint is restricted by the item itself), so no item reads a
 // value another item of the launch writes.
+//
+// Optionally (f_n > 0) the launch also runs level k's own ghost fill that
+// precedes the restriction (the closing fill of its pre-smoothing, or of the
+// finest level's post-smoothing before the fill-down): blocks
+// [nb_r, nb_r + nb_f) run those items as k_ghost does, its ring items only
+// with f_ring.  The host allows it on a level whose fill reads no cell the
+// restriction or the parent's fill writes, and whose ghost cells the
+// parent's fill does not read.
 template <class T, int kT = kBlock>
 __global__ void __launch_bounds__(kT) k_restrict_fill(LevelD L, Decomp D, FieldsT<T> f, int to_parent, int nb_r,
                                                      GhostItems G, GhostAlt A, int g_off, int g_n, double hx_,
                                                      double hy_, const int *__restrict__ active,
-                                                     const int *__restrict__ inst_nlev, int need) {
+                                                     const int *__restrict__ inst_nlev, int need, int f_off, int f_n,
+                                                     int nb_f, int f_ring, double fhx, double fhy) {
   chain_trigger();
   if ((int)blockIdx.x < nb_r) {
     restrict_item<T, true>(L, D, f, to_parent, blockIdx.x * kT + threadIdx.x);
     return;
   }
-  const int t = ((int)blockIdx.x - nb_r) * kT + threadIdx.x;
+  if ((int)blockIdx.x < nb_r + nb_f) {
+    const int t = ((int)blockIdx.x - nb_r) * kT + threadIdx.x;
+    const int i = f_off + t;
+    const int inst = (t < f_n && G.inst) ? G.inst[i] : -1;
+    const int8_t ty = t < f_n ? G.type[i] : G_COPY;
+    const bool skip = t >= f_n || (inst >= 0 && !active[inst]) || (ty == G_RING && !f_ring);
+    GhostPrep P;
+    if (!skip) P = ghost_prep(G, i, ty, G.dst[i]);
+    chain_wait();
+    if (skip) return;
+    ghost_apply<T>(G, i, P, f.Q, f.QC, f.bcg, T(fhx), T(fhy));
+    return;
+  }
+  const int t = ((int)blockIdx.x - nb_r - nb_f) * kT + threadIdx.x;
   const int i = g_off + t;
   const int inst = (t < g_n && G.inst) ? G.inst[i] : -1;
   const bool skip = t >= g_n || (inst >= 0 && (!active[inst] || inst_nlev[inst] < need));
