@@ -116,6 +116,8 @@ struct LevelPlan {
   // into the parent (k_restrict_fill): after the pre-smoothing (ring items
   // left out), and with its ring items before the fill-down (set at upload)
   bool fuse_pre = false, fuse_top = false;
+  // does a ghost rule of this level read a ghost cell of the parent level
+  bool reads_pg = true;
 };
 
 }  // namespace
@@ -547,10 +549,13 @@ void launch_restrict(bsam_hier h, int k, int to_parent) {
 // fill_k, level k's own fill that precedes them (launch_fill(k)) joins the
 // launch too: FILL_PRE after the pre-smoothing (ring items left out), FILL_TOP
 // before the fill-down; the caller checks the level's fuse_pre / fuse_top.
+// The parent's fill skips the instances without level k (need = k) unless
+// need = 0 is given.
 enum { FILL_NONE = 0, FILL_PRE = 1, FILL_TOP = 2 };
 
 template <class T = double>
-void launch_restrict_fill(bsam_hier h, int k, int fill_k = FILL_NONE) {
+void launch_restrict_fill(bsam_hier h, int k, int fill_k = FILL_NONE, int need = -1) {
+  if (need < 0) need = k;
   const LevelPlan &L = h->lev[k], &Lc = h->lev[k - 1];
   if (!Lc.g1_n) {
     if (fill_k) launch_fill<T>(h, k);
@@ -566,12 +571,12 @@ void launch_restrict_fill(bsam_hier h, int k, int fill_k = FILL_NONE) {
     const int nb = (D.n + 63) / 64, nf = (fn + 63) / 64;
     launch_k(h, k_restrict_fill<T, 64>, nb + nf + (Lc.g1_n + 63) / 64, 64, leveld(h, k), D, f, 1, nb,
              ghost_items(h), A, Lc.g1_off, Lc.g1_n, Lc.hx, Lc.hy, (const int *)h->active.p,
-             (const int *)h->inst_nlev.p, k, L.g1_off, fn, nf, fring, L.hx, L.hy);
+             (const int *)h->inst_nlev.p, need, L.g1_off, fn, nf, fring, L.hx, L.hy);
   } else {
     const int nb = nblk(D.n), nf = nblk(fn);
     launch_k(h, k_restrict_fill<T>, nb + nf + nblk(Lc.g1_n), kBlock, leveld(h, k), D, f, 1, nb, ghost_items(h), A,
-             Lc.g1_off, Lc.g1_n, Lc.hx, Lc.hy, (const int *)h->active.p, (const int *)h->inst_nlev.p, k, L.g1_off,
-             fn, nf, fring, L.hx, L.hy);
+             Lc.g1_off, Lc.g1_n, Lc.hx, Lc.hy, (const int *)h->active.p, (const int *)h->inst_nlev.p, need,
+             L.g1_off, fn, nf, fring, L.hx, L.hy);
   }
 }
 
@@ -742,14 +747,75 @@ void launch_residual(bsam_hier h, int mode) {
            (const int *)h->crange.p, h->nlev, h->act_mode == kActChunk ? h->cact.p : nullptr);
 }
 
+// Ghost fills of several levels in one launch (k_ghost_spans); `lv` lists
+// the levels in increasing order, none reading a ghost cell another of them
+// writes.
+template <class T = double>
+void launch_fill_spans(bsam_hier h, const std::vector<int> &lv) {
+  GhostSpans S{};
+  int tot = 0, last = 0;
+  for (int k : lv) {
+    const LevelPlan &L = h->lev[k];
+    if (!L.g1_n) continue;
+    S.off[S.n] = L.g1_off;
+    S.beg[S.n] = tot;
+    S.hx[S.n] = L.hx;
+    S.hy[S.n] = L.hy;
+    tot += L.g1_n;
+    last = k;
+    ++S.n;
+  }
+  if (S.n == 0) return;
+  if (S.n == 1) {
+    launch_fill<T>(h, last);
+    return;
+  }
+  S.beg[S.n] = tot;
+  FieldsT<T> f = fields_t<T>(h);
+  Launch l(h, K_GHOST, 0, last);
+  if (nblk(tot) < spread_limit(h))
+    launch_k(h, k_ghost_spans<T, 64>, (tot + 63) / 64, 64, ghost_items(h), S, f.Q, f.QC, f.bcg,
+             (const int *)h->active.p);
+  else
+    launch_k(h, k_ghost_spans<T>, nblk(tot), kBlock, ghost_items(h), S, f.Q, f.QC, f.bcg, (const int *)h->active.p);
+}
+
 // Mixed form: after Q changed on every level at once (or before the first
 // correction, when a new level's parent still holds its old values under
 // the footprint), restrict finest first, then refill the ghosts coarsest
 // first, so every fill reads parent cells (ghosts included) that are up to
-// date and the composite residual sees a consistent hierarchy.
+// date and the composite residual sees a consistent hierarchy.  Launches:
+// the fill of level k-1 joins the restriction from level k (its operands
+// under level k's footprint restricted by the items, k_restrict_fill) where
+// level k-1 is the root or its rules read no cell that a later restriction
+// or fill writes (fuse_top); the other levels' fills follow the
+// restrictions, several levels per launch where none reads a ghost cell of
+// the level below it in the same launch.  The same values as one launch per
+// restriction and per level's fill.
 void launch_consistent(bsam_hier h) {
-  for (int kk = h->nlev; kk >= 2; --kk) launch_restrict(h, kk, 1);
-  for (int k = 1; k <= h->nlev; ++k) launch_fill(h, k);
+  std::vector<int> rest;   // levels filled after the restrictions
+  const bool top = h->nlev >= 2 && h->lev[h->nlev].fuse_top;
+  if (!top) rest.push_back(h->nlev);
+  for (int kk = h->nlev; kk >= 2; --kk) {
+    const int p = kk - 1, own = top && kk == h->nlev ? FILL_TOP : FILL_NONE;
+    if (p == 1 || h->lev[p].fuse_top) {
+      launch_restrict_fill(h, kk, own, 0);
+    } else {
+      if (own) launch_fill(h, kk);
+      launch_restrict(h, kk, 1);
+      rest.push_back(p);
+    }
+  }
+  std::sort(rest.begin(), rest.end());
+  std::vector<int> grp;
+  for (int k : rest) {
+    if (!grp.empty() && ((grp.back() == k - 1 && h->lev[k].reads_pg) || (int)grp.size() == kMaxSpans)) {
+      launch_fill_spans(h, grp);
+      grp.clear();
+    }
+    grp.push_back(k);
+  }
+  launch_fill_spans(h, grp);
 }
 
 // F = FTrue (ebSolveCycles.m:30-34), once before a run of FP64 V-cycles
@@ -777,7 +843,10 @@ void reset_force(bsam_hier h) {
 int launch_iteration(bsam_hier h, int mode) {
   if (mixed(h)) {
     CK(cudaMemsetAsync(h->E.p, 0, sizeof(float) * h->E.n, h->stream));
-    launch_vcycle<float>(h, h->nlev);
+    // the finest level's closing fill of E is left out: nothing reads the
+    // correction's ghosts after the cycle (the update reads cells, the next
+    // cycle starts from E = 0)
+    launch_vcycle<float>(h, h->nlev, true);
     {
       Decomp D = decomp(h, h->all_cells);
       Launch l(h, K_PROLONG, 20.0 * (double)h->n_cells);
@@ -1850,16 +1919,18 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
       for (int i = L.g1_off; i < L.g1_off + L.g1_n; ++i)
         if (B.gt[i] != G_RING) gw[B.gdst[i]] = i;
       std::vector<int> rd;
-      bool ok = true, ring_ok = true;
-      for (int i = L.g1_off; i < L.g1_off + L.g1_n && ok; ++i) {
+      bool ok = true, ring_ok = true, rpg = false;
+      for (int i = L.g1_off; i < L.g1_off + L.g1_n; ++i) {
         rd.clear();
         ghost_reads(B, i, rd);
         for (int q : rd) {
-          const bool hit = cov.count(q) || pw.count(q);
+          const bool g = pw.count(q) > 0, hit = g || cov.count(q);
+          rpg |= g;
           if (B.gt[i] == G_RING) ring_ok &= !hit;
           else ok &= !hit;
         }
       }
+      h->lev[k].reads_pg = rpg;
       for (int i = Lc.g1_off; i < Lc.g1_off + Lc.g1_n && ok; ++i) {
         rd.clear();
         ghost_reads(B, i, rd);

@@ -312,6 +312,47 @@ __global__ void __launch_bounds__(kT) k_ghost(GhostItems G, int off, int n, T *_
   ghost_apply<T>(G, i, P, Q, QC, bcg, T(hx_), T(hy_));
 }
 
+// Ghost fills of several levels in one launch: span s holds the items
+// [off[s], off[s] + beg[s+1] - beg[s]) of a level with cell sizes hx[s],
+// hy[s], and launch item t belongs to the span with beg[s] <= t < beg[s+1].
+// The host groups levels none of which reads a ghost cell that another level
+// of the launch writes.
+constexpr int kMaxSpans = 16;
+struct GhostSpans {
+  int off[kMaxSpans], beg[kMaxSpans + 1];
+  double hx[kMaxSpans], hy[kMaxSpans];
+  int n;
+};
+
+template <class T, int kT = kBlock>
+__global__ void __launch_bounds__(kT) k_ghost_spans(GhostItems G, GhostSpans S, T *__restrict__ Q,
+                                                    T *__restrict__ QC, const T *__restrict__ bcg,
+                                                    const int *__restrict__ active) {
+  chain_trigger();
+  const int t = blockIdx.x * kT + threadIdx.x;
+  int off = S.off[0], b = 0, tot = 0;
+  double hx = S.hx[0], hy = S.hy[0];
+#pragma unroll
+  for (int j = 1; j <= kMaxSpans; ++j) {
+    if (j == S.n) tot = S.beg[j];
+    if (j < kMaxSpans && j < S.n && t >= S.beg[j]) {
+      off = S.off[j];
+      b = S.beg[j];
+      hx = S.hx[j];
+      hy = S.hy[j];
+    }
+  }
+  const bool in = t < tot;
+  const int i = off + (t - b);
+  const int inst = (in && G.inst) ? G.inst[i] : -1;
+  const bool skip = !in || (inst >= 0 && !active[inst]);
+  GhostPrep P;
+  if (!skip) P = ghost_prep(G, i, G.type[i], G.dst[i]);
+  chain_wait();
+  if (skip) return;
+  ghost_apply<T>(G, i, P, Q, QC, bcg, T(hx), T(hy));
+}
+
 // ---------------------------------------------------------------------------
 // relax2d (EllipticBSAM/src/ebKernels.m:37-95): one colour of the red-black
 // Gauss-Seidel sweep over all patches of a level, one thread per cell of
