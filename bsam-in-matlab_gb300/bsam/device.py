@@ -352,7 +352,9 @@ class DevHier:
 
     def relax_tuning(self, precision=0):
         """Smoother launch form per level 1..nlev as tuned: colour cells per
-        thread (1, 2, 4), 0 for the single-cluster launch, -1 not yet run."""
+        thread (1, 2, 4), 3 persistent blocks, 0 the single-cluster launch, 5
+        the single-cluster launch with the level's solution in distributed
+        shared memory, -1 not yet run."""
         out = np.zeros(int(self.fl.nlev), np.int32)
         check(lib().bsam_relax_tuning(self.h, int(precision), out.ctypes.data, out.size))
         return out

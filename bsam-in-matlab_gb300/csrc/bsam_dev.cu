@@ -118,6 +118,8 @@ struct LevelPlan {
   bool fuse_pre = false, fuse_top = false;
   // does a ghost rule of this level read a ghost cell of the parent level
   bool reads_pg = true;
+  int64_t q_lo = 0, q_hi = 0;      // the level's patches' range of Q (ghosts included)
+  int dsm_shift[2] = {-1, -1};     // k_relax_dsm slice size 2^shift per precision (-1: not a candidate)
 };
 
 }  // namespace
@@ -451,6 +453,75 @@ void launch_cluster(bsam_hier h, int ctas, Args... args) {
   cudaLaunchKernelEx(&cfg, k_relax_cluster<T, kPow2>, args...);
 }
 
+// most shared memory per CTA of k_relax_dsm, and the amount for a slice of
+// 2^shift elements (the slice, then ten values per thread)
+constexpr int kDsmMaxBytes = 160 * 1024;
+template <class T>
+size_t dsm_smem(int shift) {
+  return (((size_t)1 << shift) + 10 * (size_t)DsmBlock<T>::value) * sizeof(T);
+}
+
+// can the device co-schedule one cluster of `ctas` CTAs of k_relax_dsm with
+// `smem` bytes of shared memory each (sets the kernel's attributes: any
+// slice up to kDsmMaxBytes may be launched afterwards)
+template <class T, bool kPow2>
+bool dsm_fits(int ctas, size_t smem) {
+  cudaFuncSetAttribute(k_relax_dsm<T, kPow2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaFuncSetAttribute(k_relax_dsm<T, kPow2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDsmMaxBytes);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)ctas);
+  cfg.blockDim = dim3(DsmBlock<T>::value);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)ctas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveClusters(&n, k_relax_dsm<T, kPow2>, &cfg);
+  cudaGetLastError();
+  return e == cudaSuccess && n >= 1;
+}
+
+// the slice size (log2, in elements) of k_relax_dsm on level k, or -1 where
+// the level's Q range does not fit one cluster's shared memory or its chunks
+// need more than one colour cell per thread
+template <class T>
+int dsm_shift_for(bsam_hier h, int k) {
+  const int C = cluster_ctas();
+  if (C <= 0) return -1;
+  const LevelPlan &L = h->lev[k];
+  if ((int64_t)L.rc_n * kChunk > (int64_t)C * DsmBlock<T>::value) return -1;
+  const int64_t n = L.q_hi - L.q_lo, per = (n + C - 1) / C;
+  int sh = 0;
+  while (((int64_t)1 << sh) < per) ++sh;
+  const size_t bytes = dsm_smem<T>(sh);
+  if (bytes > (size_t)kDsmMaxBytes) return -1;
+  const bool ok = L.pow2 ? dsm_fits<T, true>(C, bytes) : dsm_fits<T, false>(C, bytes);
+  return ok ? sh : -1;
+}
+
+template <class T, bool kPow2, class... Args>
+void launch_dsm(bsam_hier h, int ctas, size_t smem, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)ctas);
+  cfg.blockDim = dim3(DsmBlock<T>::value);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  at[1].id = cudaLaunchAttributeClusterDimension;
+  at[1].val.clusterDim.x = (unsigned)ctas;
+  at[1].val.clusterDim.y = 1;
+  at[1].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 2;
+  cudaLaunchKernelEx(&cfg, k_relax_dsm<T, kPow2>, args...);
+}
+
 // ebRelaxLevel (ebRelaxLevel.m:28-38): 2*nsweeps colour passes; the ghost
 // refill after every colour is folded into the next pass (k_relax `fresh`),
 // and one fill after the last pass leaves the ghost frame as the reference's.
@@ -471,6 +542,23 @@ void launch_relax(bsam_hier h, int k, int nsweeps, bool first_fresh = false, boo
   const int am = h->act_mode;
   const std::vector<int> &rn = h->relax_n[sizeof(T) == sizeof(float) ? 1 : 0];
   const int kn = rn.empty() ? 1 : rn[k];
+  if (kn == 5) {   // the whole relaxation (and its fill) in one cluster launch, solution in shared memory
+    const int sh = L.dsm_shift[sizeof(T) == sizeof(float) ? 1 : 0];
+    Launch l(h, K_RELAX, 24.0 * tscale<T>() * (double)L.ncells * 2 * nsweeps, k);
+    const int C = cluster_ctas();
+    const Rule *pr = (const Rule *)h->perim.p;
+    const T om = (T)h->opts.omega;
+    const int ff = first_fresh ? 1 : 0, gn = defer_fill ? 0 : L.g1_n;
+    const size_t smem = dsm_smem<T>(sh);
+    const int q0 = (int)L.q_lo, qn = (int)(L.q_hi - L.q_lo);
+    if (L.pow2)
+      launch_dsm<T, true>(h, C, smem, ld, ch, L.rc_n, f, pk, pr, om, unit, nsweeps, ff, ca, am, ghost_items(h),
+                          L.g1_off, gn, L.hx, L.hy, q0, qn, sh);
+    else
+      launch_dsm<T, false>(h, C, smem, ld, ch, L.rc_n, f, pk, pr, om, unit, nsweeps, ff, ca, am, ghost_items(h),
+                           L.g1_off, gn, L.hx, L.hy, q0, qn, sh);
+    return;
+  }
   if (kn == 0) {   // the whole relaxation and its fill in one cluster launch
     Launch l(h, K_RELAX, 24.0 * tscale<T>() * (double)L.ncells * 2 * nsweeps, k);
     const int C = cluster_ctas();
@@ -891,39 +979,65 @@ int tune_set(bsam_hier h, int k) {
   return 0;
 }
 
+// microseconds of one relaxation of level k (npre sweeps and the fill) in
+// launch form kn, replayed as a graph (as the solve runs it); a form the
+// runtime refuses is not a candidate (+inf)
+template <class T>
+float time_form(bsam_hier h, int k, int kn, int ns) {
+  std::vector<int> &rn = h->relax_n[sizeof(T) == sizeof(float) ? 1 : 0];
+  rn[k] = kn;
+  cudaGetLastError();
+  if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return 1e30f;
+  launch_relax<T>(h, k, ns);
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+  float t = 1e30f;
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  if (e == cudaSuccess) e = cudaGraphLaunch(ge, h->stream);   // warm-up
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  constexpr int kReps = 4;
+  for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+    cudaEventRecord(a, h->stream);
+    for (int i = 0; i < kReps; ++i) cudaGraphLaunch(ge, h->stream);
+    cudaEventRecord(b, h->stream);
+    e = cudaEventSynchronize(b);
+    float ms = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    if (e == cudaSuccess) t = std::min(t, 1000.0f * ms / kReps);
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (ge) cudaGraphExecDestroy(ge);
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();
+  return e == cudaSuccess ? t : 1e30f;
+}
+
 template <class T>
 int tune_level(bsam_hier h, int k, int set, int *best) {
-  std::vector<int> &rn = h->relax_n[sizeof(T) == sizeof(float) ? 1 : 0];
-  cudaEvent_t a, b;
-  CK(cudaEventCreate(&a));
-  CK(cudaEventCreate(&b));
+  const int p = sizeof(T) == sizeof(float) ? 1 : 0;
+  std::vector<int> &rn = h->relax_n[p];
   float bt = 1e30f;
   *best = 1;
   const int ns = std::max(h->opts.npre, 1);
-  const std::vector<int> cand = set == 1 ? std::vector<int>{1, 2, 4, 3} : std::vector<int>{1, 0};
+  std::vector<int> cand = set == 1 ? std::vector<int>{1, 2, 4, 3} : std::vector<int>{1};
+  if (set == 2) cand.push_back(0);
+  h->lev[k].dsm_shift[p] = dsm_shift_for<T>(h, k);
+  if (h->lev[k].dsm_shift[p] >= 0) cand.push_back(5);
   for (int kn : cand) {
-    rn[k] = kn;
-    launch_relax<T>(h, k, ns);         // warm-up
-    if (kn == 0 && cudaGetLastError() != cudaSuccess) continue;   // cluster launch refused: not a candidate
-    float t = 1e30f;
-    for (int rep = 0; rep < 3; ++rep) {
-      cudaEventRecord(a, h->stream);
-      launch_relax<T>(h, k, ns);
-      cudaEventRecord(b, h->stream);
-      CK(cudaEventSynchronize(b));
-      float ms = 0;
-      cudaEventElapsedTime(&ms, a, b);
-      t = std::min(t, ms);
-    }
+    const float t = time_form<T>(h, k, kn, ns);
     if (t < bt * 0.97f) {              // a change must win clearly
       bt = t;
       *best = kn;
     }
   }
   rn[k] = *best;
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
-  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->stream));
   return BSAM_OK;
 }
 
@@ -971,11 +1085,19 @@ int autotune(bsam_hier h) {
   h->tuned[p] = true;
   std::vector<int> &rn = h->relax_n[p];
   rn.assign(h->nlev + 1, 1);
+  // the shared-memory form only where the level's Q range fits one cluster
+  auto dsm_ok = [&](int k) {
+    const int sh = p ? dsm_shift_for<float>(h, k) : dsm_shift_for<double>(h, k);
+    h->lev[k].dsm_shift[p] = sh;
+    return sh >= 0;
+  };
   if (const char *env = getenv("BSAM_RELAX_N")) {
     int kn = atoi(env);
     if (kn == 0 && cluster_ctas() == 0) kn = 1;
-    rn.assign(h->nlev + 1, (kn >= 0 && kn <= 4) ? kn : 1);
+    rn.assign(h->nlev + 1, (kn >= 0 && kn <= 5) ? kn : 1);
     rn[1] = 1;
+    for (int k = 2; k <= h->nlev; ++k)
+      if (rn[k] == 5 && !dsm_ok(k)) rn[k] = 1;
     return BSAM_OK;
   }
   // levels already measured on this context (same precision, same h^2 form,
@@ -988,7 +1110,7 @@ int autotune(bsam_hier h) {
       const int set = tune_set(h, k);
       if (!set) continue;
       auto it = c->relax_tune.find(tune_key(p, h->lev[k].pow2, h->lev[k].rc_n, set));
-      if (it != c->relax_tune.end()) rn[k] = it->second;
+      if (it != c->relax_tune.end()) rn[k] = it->second == 5 && !dsm_ok(k) ? 1 : it->second;
       else todo.push_back(k);
     }
   }
@@ -1328,6 +1450,8 @@ struct Builder {
       qhi = std::max<int64_t>(qhi, (int64_t)r[PD_QOFF] + (int64_t)(r[PD_MX] + 2) * (r[PD_MY] + 2));
     }
     if (qlo < 0 || qhi > d->n_q || qhi <= qlo) return fail(BSAM_ERR_ARG, "patch Q range outside Q");
+    L.q_lo = qlo;
+    L.q_hi = qhi;
     std::vector<int> slot((size_t)(qhi - qlo), -1);
     bool outside = false;
     auto rule_at = [&](int dst) -> int {
@@ -2129,13 +2253,23 @@ int bsam_fp64_rate(bsam_ctx ctx, double *gops) {
   return BSAM_OK;
 }
 
-int bsam_ctx_destroy(bsam_ctx ctx) {
-  if (!ctx) return BSAM_OK;
+// drops one reference to the context (its creator's, or a hierarchy's) and
+// destroys it with the last one
+static void ctx_unref(bsam_ctx ctx) {
+  {
+    std::lock_guard<std::mutex> lk(ctx->ref_mu);
+    if (--ctx->refs > 0) return;
+  }
   cudaSetDevice(ctx->device);
   if (ctx->scratch) cudaFreeAsync(ctx->scratch, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
+}
+
+int bsam_ctx_destroy(bsam_ctx ctx) {
+  if (!ctx) return BSAM_OK;
+  ctx_unref(ctx);
   return BSAM_OK;
 }
 
@@ -2152,6 +2286,10 @@ int bsam_hier_upload(bsam_ctx ctx, const bsam_hier_desc *desc, const bsam_solve_
     delete h;
     return rc;
   }
+  {
+    std::lock_guard<std::mutex> lk(ctx->ref_mu);
+    ++ctx->refs;
+  }
   *out = h;
   return BSAM_OK;
 }
@@ -2161,7 +2299,9 @@ int bsam_hier_free(bsam_hier h) {
   set_device(h);
   cudaStreamSynchronize(h->stream);
   release(h);
+  bsam_ctx ctx = h->ctx;
   delete h;
+  ctx_unref(ctx);
   return BSAM_OK;
 }
 

@@ -20,6 +20,9 @@ struct bsam_ctx_s {
   size_t scratch_bytes = 0;
   std::mutex tune_mu;
   std::map<uint64_t, int> relax_tune;
+  // the context lives while it is open or a hierarchy made on it exists
+  std::mutex ref_mu;
+  int refs = 1;
 };
 
 // records the message of a failed call for bsam_last_error(); returns code

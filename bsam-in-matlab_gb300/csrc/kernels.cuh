@@ -250,6 +250,19 @@ __device__ __forceinline__ T ghost_operand(const T *Q, int code, const GhostAlt 
   return ld_sol<kCG>(Q + code);
 }
 
+// a ghost's value from its operands and boundary datum (eval_rule's
+// arithmetic, every kind but the ring refresh and the physical corner)
+template <class T>
+__device__ __forceinline__ T ghost_formula(int ty, T qa, T qb, T qc, T qd, T qe, T g, int nb, T hx, T hy) {
+  const T c23 = T(2.0 / 3.0), c13 = T(1.0 / 3.0), c83 = T(8.0 / 3.0);
+  switch (ty) {
+    case G_LIF_CORNER: return c23 * qc + c13 * qa;
+    case G_DIRICHLET: return (c83 * g - 2 * qa) + c13 * qb;
+    case G_NEUMANN: return qa + (nb ? hy : hx) * g;
+    default: return rule_value<T>(ty, qa, qb, qc, qd, qe);   // COPY, QIF, QIF_END, LIF
+  }
+}
+
 // the value of a prepared item that is not a ring refresh or a corner
 template <class T, bool kCG, bool kAlt>
 __device__ __forceinline__ T ghost_value(const GhostPrep &P, const T *Q, const T *bcg, T hx, T hy,
@@ -258,13 +271,7 @@ __device__ __forceinline__ T ghost_value(const GhostPrep &P, const T *Q, const T
   const T qc = ghost_operand<T, kCG, kAlt>(Q, P.c, A);
   const T qd = ld_sol<kCG>(Q + P.d), qe = ld_sol<kCG>(Q + P.e);
   const T g = P.g >= 0 ? bcg[P.g] : T(0);
-  const T c23 = T(2.0 / 3.0), c13 = T(1.0 / 3.0), c83 = T(8.0 / 3.0);
-  switch (P.ty) {
-    case G_LIF_CORNER: return c23 * qc + c13 * qa;
-    case G_DIRICHLET: return (c83 * g - 2 * qa) + c13 * qb;
-    case G_NEUMANN: return qa + (P.nb ? hy : hx) * g;
-    default: return rule_value<T>(P.ty, qa, qb, qc, qd, qe);   // COPY, QIF, QIF_END, LIF
-  }
+  return ghost_formula<T>(P.ty, qa, qb, qc, qd, qe, g, P.nb, hx, hy);
 }
 
 template <class T, bool kCG = false, bool kAlt = false>
@@ -830,6 +837,264 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
   }
 }
 
+
+// A small level's relaxation with its solution in distributed shared
+// memory.  One thread-block cluster copies the level's Q range [q0, q0 + qn)
+// into the shared memory of its CTAs (CTA r holds elements [r S, (r + 1) S),
+// S = 2^shift), runs every colour pass of the `nsweeps` sweeps with the
+// neighbour and ghost-rule loads and the stores going to the owning CTA's
+// shared memory, a cluster barrier between passes, then the level's ghost
+// fill (g_n > 0), and copies the range back.  Each thread owns one chunk
+// slot (the same colour-cell position of both colours) and loads its static
+// data once, before the passes: the packed operands, boundary data, force,
+// and its ghost rule with the rule's parent-cell operands (cells outside the
+// range do not change during the relaxation), so a pass waits only for the
+// shared-memory loads of the solution.  The arithmetic of every update and
+// ghost is relax_cell's and ghost_item's, so the results are the chained
+// passes' bit for bit.  The host uses it on levels with at most one colour
+// cell per thread and colour; the dynamic shared memory is the slice and
+// ten values per thread (the rules' parent-cell operands).
+template <class T>
+struct DsmBlock {
+  static constexpr int value = 512;
+};
+
+template <class T>
+struct DsmRange {
+  int q0, qn, shift;
+  uint32_t base;          // shared-window address of this CTA's slice
+};
+
+template <class T>
+__device__ __forceinline__ uint32_t dsm_addr(const DsmRange<T> &D, int rel) {
+  const uint32_t la = D.base + (uint32_t)(rel & ((1 << D.shift) - 1)) * (uint32_t)sizeof(T);
+  uint32_t ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(la), "r"((uint32_t)rel >> D.shift));
+  return ra;
+}
+__device__ __forceinline__ double dsm_ld(uint32_t a, double) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ float dsm_ld(uint32_t a, float) {
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ void dsm_st(uint32_t a, double v) {
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+__device__ __forceinline__ void dsm_st(uint32_t a, float v) {
+  asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+
+// a solution value: from the cluster's copy inside the range, else from
+// global memory (static while the kernel runs)
+template <class T>
+__device__ __forceinline__ T dsm_sol(const DsmRange<T> &D, const T *Q, int n) {
+  const int rel = n - D.q0;
+  if ((unsigned)rel < (unsigned)D.qn) return dsm_ld(dsm_addr(D, rel), T(0));
+  return __ldg(Q + n);
+}
+
+template <class T>
+__device__ __forceinline__ T dsm_rule(const DsmRange<T> &D, const Rule &R, const T *Q) {
+  const T qa = dsm_sol(D, Q, R.a), qb = dsm_sol(D, Q, R.b), qc = dsm_sol(D, Q, R.c);
+  const T qd = dsm_sol(D, Q, R.d), qe = dsm_sol(D, Q, R.e);
+  return rule_value<T>(R.type, qa, qb, qc, qd, qe);
+}
+
+// one colour cell's static data for k_relax_dsm; its ghost rule's operands
+// outside the range (static) wait in the CTA's shared memory at `ov`
+template <class T>
+struct DsmCell {
+  T dE, dW, dN, dS, idg, gx, gy, fv;
+  uint32_t oa[5];        // shared-window addresses of the rule's operands inside the range
+  int c, ldq, code, cc, rx, ry, rtype, omask;   // c relative to q0 after the bind; omask bit i: operand i inside
+  bool live;
+};
+
+// the static part, requested before the programmatic-launch wait
+template <class T>
+__device__ __forceinline__ void dsm_cell_static(const RelaxChunkD *__restrict__ chunks, int nchunks,
+                                                const T *__restrict__ pack, const FieldsT<T> &f,
+                                                const Rule *__restrict__ perim, const uint8_t *__restrict__ cact,
+                                                int amode, int ch, int tc, int m, DsmCell<T> &X) {
+  CellState<T> S;
+  cell_issue<T>(chunks, nchunks, pack, m, cact, amode, ch, tc, S);
+  cell_derive<T>(f, perim, m, 1, tc, S);
+  X.live = S.live;
+  X.dE = S.dE; X.dW = S.dW; X.dN = S.dN; X.dS = S.dS; X.idg = S.idg; X.gx = S.gx; X.gy = S.gy;
+  X.c = S.q_off + S.c;
+  X.ldq = S.ldq;
+  X.code = S.code;
+  X.cc = S.cc;
+  X.rx = S.rx;
+  X.ry = S.ry;
+  X.rtype = 0;
+  X.omask = 0;
+}
+
+// the dynamic part of the set-up, after the wait: force, and the rule's
+// operands (values outside the range into ov, addresses inside)
+template <class T>
+__device__ __forceinline__ void dsm_cell_bind(const FieldsT<T> &f, const Rule *__restrict__ perim,
+                                              const DsmRange<T> &D, T *ov, DsmCell<T> &X) {
+  if (!X.live) return;
+  X.fv = f.F[X.cc];
+  X.c -= D.q0;
+  const int kx = X.code & 3, ky = (X.code >> 2) & 3;
+  if (kx == 3 || ky == 3) {
+    const Rule R = perim[kx == 3 ? X.rx : X.ry];
+    X.rtype = R.type;
+    const int op[5] = {R.a, R.b, R.c, R.d, R.e};
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      const int rel = op[i] - D.q0;
+      if ((unsigned)rel < (unsigned)D.qn) {
+        X.omask |= 1 << i;
+        X.oa[i] = dsm_addr(D, rel);
+      } else {
+        X.oa[i] = 0;
+        ov[i] = f.Q[op[i]];
+      }
+    }
+  }
+}
+
+// cell_update from the static data and the cluster's copy of the solution
+template <class T, bool kPow2>
+__device__ __forceinline__ void dsm_cell_update(const LevelD &L, const FieldsT<T> &f, const Rule *__restrict__ perim,
+                                                T omega, int unit_omega, int fresh, const DsmCell<T> &X,
+                                                const T *ov, const DsmRange<T> &D) {
+  if (!X.live) return;
+  const T c83 = T(8.0 / 3.0), c13 = T(1.0 / 3.0);
+  const LevelH<T> H = level_h(L, T(0));
+  const int ldq = X.ldq, c = X.c;
+  int kx = X.code & 3, ky = (X.code >> 2) & 3;
+  const int sx = (X.code >> 4) & 1, sy = (X.code >> 5) & 1;
+  if (!fresh) {               // the stored ghosts, as the last fill left them
+    if (kx == 3) kx = 0;
+    if (ky == 3) ky = 0;
+  }
+  T qe = dsm_ld(dsm_addr(D, c + 1), T(0)), qw = dsm_ld(dsm_addr(D, c - 1), T(0));
+  T qn = dsm_ld(dsm_addr(D, c + ldq), T(0)), qs = dsm_ld(dsm_addr(D, c - ldq), T(0));
+  T t = X.fv;
+  const bool rx = kx == 3, ry = ky == 3;
+  T o[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i)
+    o[i] = (rx || ry) ? (((X.omask >> i) & 1) ? dsm_ld(X.oa[i], T(0)) : ov[i]) : T(0);
+  if (kx > 0) {
+    T v;
+    if (kx == 1) v = c83 * X.gx + c13 * (sx ? qw : qe);
+    else if (kx == 2) v = H.hx * X.gx;
+    else v = rule_value<T>(X.rtype, o[0], o[1], o[2], o[3], o[4]);
+    if (sx) qe = v; else qw = v;
+  }
+  if (ky > 0) {
+    T v;
+    if (ky == 1) v = c83 * X.gy + c13 * (sy ? qs : qn);
+    else if (ky == 2) v = H.hy * X.gy;
+    else if (rx) v = dsm_rule<T>(D, perim[X.ry], f.Q);
+    else v = rule_value<T>(X.rtype, o[0], o[1], o[2], o[3], o[4]);
+    if (sy) qn = v; else qs = v;
+  }
+  if (kPow2) {
+    t = t + qe * X.dE;
+    t = t + qw * X.dW;
+    t = t + qn * X.dN;
+    t = t + qs * X.dS;
+  } else {
+    t = t + (qe * X.dE) / H.hx2;
+    t = t + (qw * X.dW) / H.hx2;
+    t = t + (qn * X.dN) / H.hy2;
+    t = t + (qs * X.dS) / H.hy2;
+  }
+  t = t * X.idg;
+  const uint32_t ac = dsm_addr(D, c);
+  if (unit_omega) dsm_st(ac, t);
+  else dsm_st(ac, omega * t + (1 - omega) * dsm_ld(ac, T(0)));
+}
+
+// one ghost rule's value (eval_rule's arithmetic) from the cluster's copy
+template <class T>
+__device__ __forceinline__ T ghost_eval_dsm(const GhostItems &G, int i, const FieldsT<T> &f, T hx, T hy,
+                                            const DsmRange<T> &D) {
+  const GhostPrep P = ghost_prep(G, i, G.type[i], 0);
+  const T qa = dsm_sol(D, f.Q, P.a), qb = dsm_sol(D, f.Q, P.b), qc = dsm_sol(D, f.Q, P.c);
+  const T qd = dsm_sol(D, f.Q, P.d), qe = dsm_sol(D, f.Q, P.e);
+  const T g = P.g >= 0 ? f.bcg[P.g] : T(0);
+  return ghost_formula<T>(P.ty, qa, qb, qc, qd, qe, g, P.nb, hx, hy);
+}
+
+template <class T, bool kPow2>
+__global__ void __launch_bounds__(DsmBlock<T>::value, 1)
+    k_relax_dsm(LevelD L, const RelaxChunkD *__restrict__ chunks, int nchunks, FieldsT<T> f,
+                const T *__restrict__ pack, const Rule *__restrict__ perim, T omega, int unit_omega, int nsweeps,
+                int first_fresh, const uint8_t *__restrict__ cact, int amode, GhostItems G, int g_off, int g_n,
+                double hx_, double hy_, int q0, int qn, int shift) {
+  namespace cg = cooperative_groups;
+  constexpr int kB = DsmBlock<T>::value;
+  extern __shared__ __align__(16) unsigned char dsm_raw[];
+  T *slice = reinterpret_cast<T *>(dsm_raw);
+  chain_trigger();
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks(), r = (int)cl.block_rank();
+  const int S = 1 << shift;
+  const DsmRange<T> D{q0, qn, shift, (uint32_t)__cvta_generic_to_shared(slice)};
+  // this thread's chunk slot: CTA r takes a contiguous run of chunks
+  const int cpc = (nchunks + C - 1) / C;
+  const int w = r * cpc * kChunk + (int)threadIdx.x;
+  const bool mine = (int)threadIdx.x < cpc * kChunk && w < nchunks * kChunk;
+  // parent-cell operands of this thread's two rules, after the slice
+  T *ov0 = slice + S + 10 * (int)threadIdx.x, *ov1 = ov0 + 5;
+  DsmCell<T> X0, X1;
+  X0.live = X1.live = false;
+  if (mine) {
+    dsm_cell_static<T>(chunks, nchunks, pack, f, perim, cact, amode, w / kChunk, w % kChunk, 0, X0);
+    dsm_cell_static<T>(chunks, nchunks, pack, f, perim, cact, amode, w / kChunk, w % kChunk, 1, X1);
+  }
+  chain_wait();
+  const int e0 = r * S, e1 = min(qn, e0 + S);
+  for (int e = e0 + (int)threadIdx.x; e < e1; e += kB) slice[e - e0] = f.Q[q0 + e];
+  dsm_cell_bind<T>(f, perim, D, ov0, X0);
+  dsm_cell_bind<T>(f, perim, D, ov1, X1);
+  cl.sync();
+  for (int s = 0; s < nsweeps; ++s) {
+    dsm_cell_update<T, kPow2>(L, f, perim, omega, unit_omega, (first_fresh || s > 0) ? 1 : 0, X0, ov0, D);
+    cl.sync();
+    dsm_cell_update<T, kPow2>(L, f, perim, omega, unit_omega, 1, X1, ov1, D);
+    cl.sync();
+  }
+  if (g_n > 0) {
+    const int nth = C * kB, tid = r * kB + (int)threadIdx.x;
+    const T hx = T(hx_), hy = T(hy_);
+    for (int t = tid; t < g_n; t += nth) {
+      const int i = g_off + t;
+      const int inst = G.inst ? G.inst[i] : -1;
+      if (inst >= 0 && !f.active[inst]) continue;
+      const int8_t ty = G.type[i];
+      const int dst = G.dst[i];
+      if (ty == G_RING) {
+        f.QC[dst] = dsm_sol(D, f.Q, G.a[i]);
+        continue;
+      }
+      T v;
+      if (ty == G_PHYS_CORNER) {
+        const T v1 = ghost_eval_dsm<T>(G, G.a[i], f, hx, hy, D);
+        const T v2 = ghost_eval_dsm<T>(G, G.b[i], f, hx, hy, D);
+        v = (v1 + v2) - dsm_sol(D, f.Q, G.c[i]);
+      } else {
+        v = ghost_eval_dsm<T>(G, i, f, hx, hy, D);
+      }
+      dsm_st(dsm_addr(D, dst - q0), v);
+    }
+    cl.sync();
+  }
+  for (int e = e0 + (int)threadIdx.x; e < e1; e += kB) f.Q[q0 + e] = slice[e - e0];
+}
 
 // ---------------------------------------------------------------------------
 // restrict2 (ebKernels.m:98-102) of each patch interior into its QC interior

@@ -111,7 +111,9 @@ typedef struct {
 } bsam_solve_opts;
 
 /* Context: one device, one stream.  Replaces nothing in the reference (the
- * MATLAB session); created once by the gateway.                          */
+ * MATLAB session); created once by the gateway.  A hierarchy uploaded on a
+ * context keeps it alive: bsam_ctx_destroy and bsam_hier_free may come in
+ * either order, and the last of them releases the context's stream.      */
 int bsam_ctx_create(int device, bsam_ctx *out);
 int bsam_ctx_destroy(bsam_ctx ctx);
 
@@ -271,10 +273,12 @@ int bsam_launch_count(bsam_hier h, int64_t *count);
  * per pass of resident blocks that walk the level's chunks, the next
  * chunks' operands in flight during each update; 0 for the whole relaxation
  * (every pass and the closing ghost fill) in one launch of a single
- * thread-block cluster; -1 where that cycle has not run yet.  The choice
- * never changes a result bit; BSAM_RELAX_N=0|1|2|3|4 in the environment
- * forces one form.  No reference counterpart (ebRelaxLevel.m
- * has one loop order).                                                    */
+ * thread-block cluster; 5 for the same with the level's solution held in
+ * the cluster's distributed shared memory (levels whose Q range fits it);
+ * -1 where that cycle has not run yet.  The choice never changes a result
+ * bit; BSAM_RELAX_N=0|1|2|3|4|5 in the environment forces one form (5 where
+ * it fits, else 1).  No reference counterpart (ebRelaxLevel.m has one loop
+ * order).                                                                 */
 int bsam_relax_tuning(bsam_hier h, int precision, int32_t *cells_per_thread, int cap);
 
 /* Number of kernels one V-cycle (+ fill-down + residual) launches. */

@@ -108,12 +108,13 @@ def test_merge_rejects_different_spacing(parts):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize('form', [None, '0', '2', '3'])
+@pytest.mark.parametrize('form', [None, '0', '2', '3', '5'])
 def test_batch_equals_solo_bitwise(parts, form, monkeypatch):
     """form: the smoother's launch form forced on the batch (None: tuned; '0'
     one cluster launch per relaxation; '2' two colour cells per thread; '3'
-    persistent blocks), so frozen instances are skipped through the
-    per-chunk flags in every form."""
+    persistent blocks; '5' one cluster launch with the level's solution in
+    distributed shared memory, where it fits), so frozen instances are
+    skipped through the per-chunk flags in every form."""
     from bsam.device import DeviceBackend, DevHier, BSAM_FIELD_Q, BSAM_FIELD_QC, BSAM_FIELD_F
     ctx = DeviceBackend.get(0).ctx
     Hs = _instances()

@@ -115,3 +115,20 @@ def test_trace_file(tmp_path, monkeypatch):
     rec = [json.loads(l) for l in open(path)]
     assert rec[-1]['event'] == 'solve_cycles' and rec[-1]['vcycles'] == it
     assert rec[-1]['resHist'] == list(hist) and rec[-1]['finalRel'] == rel
+
+
+def test_context_destroyed_before_its_hierarchy():
+    """A hierarchy keeps its context alive: the context's handle may be
+    destroyed first (as at interpreter shutdown, where finaliser order is
+    arbitrary), and the hierarchy still solves and frees cleanly."""
+    from bsam.device import Context, DevHier, lib
+    fl, opts = _flat()
+    ctx = Context(0)
+    dh = DevHier(ctx, fl, opts)
+    ref = _upload(fl, opts).solve_cycles(opts.MaxVCycles + 2)
+    lib().bsam_ctx_destroy(ctx.h)
+    ctx.h = None                        # its finaliser then has nothing to free
+    it, hist, rel, vis = dh.solve_cycles(opts.MaxVCycles + 2)
+    assert it == ref[0] and rel == ref[2]
+    np.testing.assert_array_equal(hist, ref[1])
+    del dh

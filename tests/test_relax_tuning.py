@@ -1,8 +1,11 @@
 """Smoother autotuner: the launch form of each level's relaxation -- 1, 2 or
-4 colour cells updated per thread with one launch per colour pass, or every
-pass and the closing fill in one launch of a single thread-block cluster
-(form 0) -- is picked per level and precision at the first solve of a
-hierarchy, by timing the candidates on the live state.  The choice may
+4 colour cells updated per thread with one launch per colour pass,
+persistent blocks (form 3), or every pass and the closing fill in one launch
+of a single thread-block cluster, reading the solution from L2 (form 0) or
+holding the level's solution in the cluster's distributed shared memory
+(form 5, on levels whose Q range fits it) -- is picked per level and
+precision at the first solve of a hierarchy, by timing the candidates on the
+live state.  The choice may
 differ run to run, so it must never change a result bit: each forced form
 (BSAM_RELAX_N, on every level) and the tuned one give the same V-cycle
 count, residual history and solution, in the FP64 cycle
@@ -42,12 +45,16 @@ def test_every_coarsening_gives_the_same_bits(precision, monkeypatch):
     dh, it, hist, Q = _solve(fl, o)
     p = 1 if precision == 'mixed' else 0
     tuned = dh.relax_tuning(p)
-    assert set(tuned.tolist()) <= {0, 1, 2, 3, 4} and tuned[0] == 1
+    assert set(tuned.tolist()) <= {0, 1, 2, 3, 4, 5} and tuned[0] == 1
     assert np.all(dh.relax_tuning(1 - p) == -1)     # that cycle never ran
-    for kn in (0, 1, 2, 3, 4):
+    for kn in (0, 1, 2, 3, 4, 5):
         monkeypatch.setenv('BSAM_RELAX_N', str(kn))
         dk, itk, histk, Qk = _solve(fl, o)
-        assert np.all(dk.relax_tuning(p)[1:] == kn)
+        forms = dk.relax_tuning(p)[1:]
+        if kn == 5:     # where a level fits: here the coarser ones
+            assert set(forms.tolist()) <= {1, 5} and forms[0] == 5, forms
+        else:
+            assert np.all(forms == kn)
         assert itk == it
         np.testing.assert_array_equal(histk, hist)
         np.testing.assert_array_equal(Qk, Q)
