@@ -452,8 +452,9 @@ def main():
     ap.add_argument('--batch', type=int, default=256, help='instances of the batching form (0: skip)')
     ap.add_argument('--no-forms', action='store_true', help='skip the mixed, batching and serving forms')
     ap.add_argument('--serve-rates', default='5,10,20,50,100,200', help='offered request rates of the serving form')
-    ap.add_argument('--eager-vcycle', action='store_true',
-                    help='profiling aid: upload the starfish hierarchy, run one eager FP64 V-cycle (every kernel of '
+    ap.add_argument('--eager-vcycle', nargs='?', const='fp64', choices=['fp64', 'mixed'],
+                    help='profiling aid: upload the starfish hierarchy, solve it once (which tunes the smoother), '
+                         'put the initial state back and run one eager V-cycle in that precision (every kernel of '
                          'the V-cycle, fill-down and residual launched once, in order, between cudaProfilerStart and '
                          'cudaProfilerStop) and exit; for ncu --profile-from-start off')
     args = ap.parse_args()
@@ -490,14 +491,21 @@ def main():
     H, opts = starfish_hierarchy(backend)
     t_build = time.perf_counter()
     fl = flatten(H)
+    if args.eager_vcycle == 'mixed':
+        opts['Precision'] = 'mixed'
     dh = DevHier(backend.ctx, fl, opts)
     if args.eager_vcycle:
+        dh.save_state()
+        dh.solve_cycles(opts.MaxVCycles + 2)
+        dh.restore_state()
         torch.cuda.synchronize()
         torch.cuda.profiler.start()
         dh.vcycle()
         torch.cuda.synchronize()
         torch.cuda.profiler.stop()
-        print(json.dumps({'eager_vcycle': 'done', 'levels': H.nlev, 'kernels': dh.kernels_per_vcycle()}), flush=True)
+        print(json.dumps({'eager_vcycle': 'done', 'precision': args.eager_vcycle, 'levels': H.nlev,
+                          'kernels': dh.kernels_per_vcycle(), 'relax_forms': dh.relax_tuning(
+                              1 if args.eager_vcycle == 'mixed' else 0).tolist()}), flush=True)
         return
     dh.save_state()
     t_upload = time.perf_counter()

@@ -67,3 +67,4 @@ def test_eager_vcycle_mode():
     assert out.returncode == 0, out.stderr[-2000:]
     d = json.loads([l for l in out.stdout.splitlines() if l.startswith('{')][0])
     assert d['eager_vcycle'] == 'done' and d['levels'] == 7 and d['kernels'] > 50
+    assert d['precision'] == 'fp64' and d['relax_forms'][0] == 1
