@@ -725,13 +725,6 @@ void launch_fill_prolong(bsam_hier h, int k) {
   }
 }
 
-// can level k's V-cycle leave its closing fill to the prolongation of level
-// k + 1 (launch_fill_prolong): in the FP32 correction cycle, unless the
-// post-smoothing runs as one cluster launch, which fills the level itself.
-// The FP64 cycle keeps separate launches: there the fused launch's
-// prolongation items wait for the parent ghosts' rules on top of their FP64
-// work, and the starfish iteration measured 1.4% slower fused (the FP32
-// cycle 1% faster); both forms give the same bits.
 // the smoother's launch form of level k in the cycle's precision (1 before
 // the autotuner ran)
 template <class T>
@@ -740,6 +733,13 @@ int relax_form(bsam_hier h, int k) {
   return rn.empty() ? 1 : rn[k];
 }
 
+// can level k's V-cycle leave its closing fill to the prolongation of level
+// k + 1 (launch_fill_prolong): in the FP32 correction cycle, unless the
+// post-smoothing runs as one cluster launch, which fills the level itself.
+// The FP64 cycle keeps separate launches: there the fused launch's
+// prolongation items wait for the parent ghosts' rules on top of their FP64
+// work, and the starfish iteration measured no faster fused (the FP32 cycle
+// 1% faster); both forms give the same bits.
 template <class T>
 bool fill_deferrable(bsam_hier h, int k) {
   if (sizeof(T) == sizeof(double)) return false;
@@ -781,8 +781,9 @@ void launch_vcycle(bsam_hier h, int k, bool defer_fill = false) {
     launch_coarsest<T>(h, defer_fill);
     return;
   }
-  // the pre-smoothing's closing fill joins the restriction's launch (unless
-  // the relaxation runs as one cluster launch, which fills the level itself)
+  // the pre-smoothing's closing fill joins the restriction's launch where
+  // upload proved that exact (fuse_pre), unless the relaxation runs as
+  // k_relax_cluster, which fills the level itself
   const bool pre_fused = h->opts.npre > 0 && relax_form<T>(h, k) != 0 && h->lev[k].fuse_pre;
   launch_relax<T>(h, k, h->opts.npre, false, pre_fused);
   launch_restrict_fill<T>(h, k, pre_fused ? FILL_PRE : FILL_NONE);

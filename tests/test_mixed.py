@@ -81,7 +81,14 @@ def test_mixed_non_power_of_two_spacing():
     assert l2 <= TOL and mx <= TOL, (l2, mx)
 
 
-def test_mixed_batch_equals_solo():
+@pytest.mark.parametrize('form', [None, '5'])
+def test_mixed_batch_equals_solo(form, monkeypatch):
+    """Instances with different level counts merged into one mixed batch
+    give their solo results bit for bit (the consistency step's fills reach
+    an instance's finest level below the batch's); form '5' forces the
+    distributed-shared-memory smoother where a level fits it."""
+    if form is not None:
+        monkeypatch.setenv('BSAM_RELAX_N', form)
     from bsam.device import DeviceBackend, DevHier, BSAM_FIELD_Q
     from bsam.batch import merge_flats, split_field
     from bsam.flat import FIELD_Q
