@@ -458,7 +458,7 @@ void launch_cluster(bsam_hier h, int ctas, Args... args) {
 constexpr int kDsmMaxBytes = 160 * 1024;
 template <class T>
 size_t dsm_smem(int shift) {
-  return (((size_t)1 << shift) + 10 * (size_t)DsmBlock<T>::value) * sizeof(T);
+  return (((size_t)1 << shift) + 10 * (size_t)kDsmBlock) * sizeof(T);
 }
 
 // can the device co-schedule one cluster of `ctas` CTAs of k_relax_dsm with
@@ -470,7 +470,7 @@ bool dsm_fits(int ctas, size_t smem) {
   cudaFuncSetAttribute(k_relax_dsm<T, kPow2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDsmMaxBytes);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)ctas);
-  cfg.blockDim = dim3(DsmBlock<T>::value);
+  cfg.blockDim = dim3(kDsmBlock);
   cfg.dynamicSmemBytes = smem;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -493,7 +493,7 @@ int dsm_shift_for(bsam_hier h, int k) {
   const int C = cluster_ctas();
   if (C <= 0) return -1;
   const LevelPlan &L = h->lev[k];
-  if ((int64_t)L.rc_n * kChunk > (int64_t)C * DsmBlock<T>::value) return -1;
+  if ((int64_t)L.rc_n * kChunk > (int64_t)C * kDsmBlock) return -1;
   const int64_t n = L.q_hi - L.q_lo, per = (n + C - 1) / C;
   int sh = 0;
   while (((int64_t)1 << sh) < per) ++sh;
@@ -507,7 +507,7 @@ template <class T, bool kPow2, class... Args>
 void launch_dsm(bsam_hier h, int ctas, size_t smem, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)ctas);
-  cfg.blockDim = dim3(DsmBlock<T>::value);
+  cfg.blockDim = dim3(kDsmBlock);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = h->stream;
   cudaLaunchAttribute at[2];

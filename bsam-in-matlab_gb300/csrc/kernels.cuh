@@ -854,10 +854,7 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 // passes' bit for bit.  The host uses it on levels with at most one colour
 // cell per thread and colour; the dynamic shared memory is the slice and
 // ten values per thread (the rules' parent-cell operands).
-template <class T>
-struct DsmBlock {
-  static constexpr int value = 512;
-};
+constexpr int kDsmBlock = 512;   // threads per CTA of k_relax_dsm
 
 template <class T>
 struct DsmRange {
@@ -1030,13 +1027,13 @@ __device__ __forceinline__ T ghost_eval_dsm(const GhostItems &G, int i, const Fi
 }
 
 template <class T, bool kPow2>
-__global__ void __launch_bounds__(DsmBlock<T>::value, 1)
+__global__ void __launch_bounds__(kDsmBlock, 1)
     k_relax_dsm(LevelD L, const RelaxChunkD *__restrict__ chunks, int nchunks, FieldsT<T> f,
                 const T *__restrict__ pack, const Rule *__restrict__ perim, T omega, int unit_omega, int nsweeps,
                 int first_fresh, const uint8_t *__restrict__ cact, int amode, GhostItems G, int g_off, int g_n,
                 double hx_, double hy_, int q0, int qn, int shift) {
   namespace cg = cooperative_groups;
-  constexpr int kB = DsmBlock<T>::value;
+  constexpr int kB = kDsmBlock;
   extern __shared__ __align__(16) unsigned char dsm_raw[];
   T *slice = reinterpret_cast<T *>(dsm_raw);
   chain_trigger();
