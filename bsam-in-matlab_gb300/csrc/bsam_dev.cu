@@ -637,9 +637,11 @@ void launch_restrict(bsam_hier h, int k, int to_parent) {
 // fill_k, level k's own fill that precedes them (launch_fill(k)) joins the
 // launch too: FILL_PRE after the pre-smoothing (ring items left out), FILL_TOP
 // before the fill-down; the caller checks the level's fuse_pre / fuse_top.
+// FILL_ZERO: the FP32 correction cycle's pre-smoothing fill on any level,
+// its parent-level operands taken as the 0 they hold (k_restrict_fill).
 // The parent's fill skips the instances without level k (need = k) unless
 // need = 0 is given.
-enum { FILL_NONE = 0, FILL_PRE = 1, FILL_TOP = 2 };
+enum { FILL_NONE = 0, FILL_PRE = 1, FILL_TOP = 2, FILL_ZERO = 3 };
 
 template <class T = double>
 void launch_restrict_fill(bsam_hier h, int k, int fill_k = FILL_NONE, int need = -1) {
@@ -655,16 +657,18 @@ void launch_restrict_fill(bsam_hier h, int k, int fill_k = FILL_NONE, int need =
   Launch l(h, K_RESTRICT, 12.0 * tscale<T>() * (double)L.ncells, k);
   const GhostAlt A{h->ga_a.p, h->ga_b.p, h->ga_c.p, h->ga_rt.p};
   const int fn = fill_k ? L.g1_n : 0, fring = fill_k == FILL_TOP ? 1 : 0;
+  // FILL_ZERO: the zero-parent form of the FP32 correction cycle
+  const int zlo = fill_k == FILL_ZERO ? (int)L.q_lo : 0, zn = fill_k == FILL_ZERO ? (int)(L.q_hi - L.q_lo) : 0;
   if (nblk(D.n) + nblk(Lc.g1_n) + nblk(fn) < spread_limit(h)) {
     const int nb = (D.n + 63) / 64, nf = (fn + 63) / 64;
     launch_k(h, k_restrict_fill<T, 64>, nb + nf + (Lc.g1_n + 63) / 64, 64, leveld(h, k), D, f, 1, nb,
              ghost_items(h), A, Lc.g1_off, Lc.g1_n, Lc.hx, Lc.hy, (const int *)h->active.p,
-             (const int *)h->inst_nlev.p, need, L.g1_off, fn, nf, fring, L.hx, L.hy);
+             (const int *)h->inst_nlev.p, need, L.g1_off, fn, nf, fring, L.hx, L.hy, zlo, zn);
   } else {
     const int nb = nblk(D.n), nf = nblk(fn);
     launch_k(h, k_restrict_fill<T>, nb + nf + nblk(Lc.g1_n), kBlock, leveld(h, k), D, f, 1, nb, ghost_items(h), A,
              Lc.g1_off, Lc.g1_n, Lc.hx, Lc.hy, (const int *)h->active.p, (const int *)h->inst_nlev.p, need,
-             L.g1_off, fn, nf, fring, L.hx, L.hy);
+             L.g1_off, fn, nf, fring, L.hx, L.hy, zlo, zn);
   }
 }
 
@@ -782,11 +786,13 @@ void launch_vcycle(bsam_hier h, int k, bool defer_fill = false) {
     return;
   }
   // the pre-smoothing's closing fill joins the restriction's launch where
-  // upload proved that exact (fuse_pre), unless the relaxation runs as
-  // k_relax_cluster, which fills the level itself
-  const bool pre_fused = h->opts.npre > 0 && relax_form<T>(h, k) != 0 && h->lev[k].fuse_pre;
+  // upload proved that exact (fuse_pre) and on every level of the FP32
+  // cycle (FILL_ZERO), unless the relaxation runs as k_relax_cluster, which
+  // fills the level itself
+  const bool f32 = sizeof(T) == sizeof(float);
+  const bool pre_fused = h->opts.npre > 0 && relax_form<T>(h, k) != 0 && (f32 || h->lev[k].fuse_pre);
   launch_relax<T>(h, k, h->opts.npre, false, pre_fused);
-  launch_restrict_fill<T>(h, k, pre_fused ? FILL_PRE : FILL_NONE);
+  launch_restrict_fill<T>(h, k, !pre_fused ? FILL_NONE : f32 ? FILL_ZERO : FILL_PRE);
   launch_coarse_load<T>(h, k);
   const bool fused = fill_deferrable<T>(h, k - 1);
   launch_vcycle<T>(h, k - 1, fused);

@@ -1150,13 +1150,18 @@ __global__ void __launch_bounds__(kT) k_restrict(LevelD L, Decomp D, FieldsT<T> 
 // [nb_r, nb_r + nb_f) run those items as k_ghost does, its ring items only
 // with f_ring.  The host allows it on a level whose fill reads no cell the
 // restriction or the parent's fill writes, and whose ghost cells the
-// parent's fill does not read.
+// parent's fill does not read.  In the FP32 correction cycle it runs on
+// every level in the zero-parent form (z_n > 0): the correction starts at 0
+// and level k-1 is first written by this very launch, so every parent-level
+// operand of level k's pre-smoothing fill is 0, which the items use instead
+// of reading cells the launch may be writing.
 template <class T, int kT = kBlock>
 __global__ void __launch_bounds__(kT) k_restrict_fill(LevelD L, Decomp D, FieldsT<T> f, int to_parent, int nb_r,
                                                      GhostItems G, GhostAlt A, int g_off, int g_n, double hx_,
                                                      double hy_, const int *__restrict__ active,
                                                      const int *__restrict__ inst_nlev, int need, int f_off, int f_n,
-                                                     int nb_f, int f_ring, double fhx, double fhy) {
+                                                     int nb_f, int f_ring, double fhx, double fhy, int z_lo,
+                                                     int z_n) {
   chain_trigger();
   if ((int)blockIdx.x < nb_r) {
     restrict_item<T, true>(L, D, f, to_parent, blockIdx.x * kT + threadIdx.x);
@@ -1172,7 +1177,27 @@ __global__ void __launch_bounds__(kT) k_restrict_fill(LevelD L, Decomp D, Fields
     if (!skip) P = ghost_prep(G, i, ty, G.dst[i]);
     chain_wait();
     if (skip) return;
-    ghost_apply<T>(G, i, P, f.Q, f.QC, f.bcg, T(fhx), T(fhy));
+    if (z_n <= 0) {
+      ghost_apply<T>(G, i, P, f.Q, f.QC, f.bcg, T(fhx), T(fhy));
+      return;
+    }
+    // zero-parent form: an operand outside level k's range [z_lo, z_lo + z_n)
+    // is a parent-level cell, which holds 0 here (below) -- the value it had
+    // before this launch's restriction and parent fill wrote any of them
+    const T hx = T(fhx), hy = T(fhy);
+    auto op = [&](int n) -> T { return (unsigned)(n - z_lo) < (unsigned)z_n ? f.Q[n] : T(0); };
+    auto rule = [&](int j) -> T {
+      const GhostPrep R = ghost_prep(G, j, G.type[j], 0);
+      return ghost_formula<T>(R.ty, op(R.a), op(R.b), op(R.c), op(R.d), op(R.e), R.g >= 0 ? f.bcg[R.g] : T(0),
+                              R.nb, hx, hy);
+    };
+    if (P.ty == G_PHYS_CORNER) {
+      const T v1 = rule(G.a[i]), v2 = rule(G.b[i]);
+      f.Q[P.dst] = (v1 + v2) - op(G.c[i]);
+    } else {
+      f.Q[P.dst] = ghost_formula<T>(P.ty, op(P.a), op(P.b), op(P.c), op(P.d), op(P.e),
+                                    P.g >= 0 ? f.bcg[P.g] : T(0), P.nb, hx, hy);
+    }
     return;
   }
   const int t = ((int)blockIdx.x - nb_r - nb_f) * kT + threadIdx.x;
