@@ -160,6 +160,8 @@ struct bsam_hier_s {
   DBuf<double> Uo, Uoo, fsrc;      // parabolic history (cells) and f staging
   bool f32_dirty = true;
   DecompH all_cells;               // every cell of every level (batch force reset)
+  DecompH below_top;               // every cell of the levels below the finest
+  bool update_fold = false;        // mixed form: Q += E may join the finest restriction (k_restrict_update)
   std::vector<InstRes> hir;        // host copy of the per-instance reduction plan
   // results of the last solve, per instance
   std::vector<double> res_hist;    // [ninst][hist_stride]
@@ -887,7 +889,16 @@ void launch_fill_spans(bsam_hier h, const std::vector<int> &lv) {
 // restrictions, several levels per launch where none reads a ghost cell of
 // the level below it in the same launch.  The same values as one launch per
 // restriction and per level's fill.
-void launch_consistent(bsam_hier h) {
+// whether launch_consistent starts with a plain restriction of the finest
+// level (which k_restrict_update can run together with Q += E)
+bool consistent_starts_plain(bsam_hier h) {
+  const int n = h->nlev;
+  return n >= 2 && !h->lev[n].fuse_top && n - 1 != 1 && !h->lev[n - 1].fuse_top;
+}
+
+// top_restricted: the finest level's restriction already ran
+// (k_restrict_update; consistent_starts_plain holds)
+void launch_consistent(bsam_hier h, bool top_restricted = false) {
   std::vector<int> rest;   // levels filled after the restrictions
   const bool top = h->nlev >= 2 && h->lev[h->nlev].fuse_top;
   if (!top) rest.push_back(h->nlev);
@@ -897,7 +908,7 @@ void launch_consistent(bsam_hier h) {
       launch_restrict_fill(h, kk, own, 0);
     } else {
       if (own) launch_fill(h, kk);
-      launch_restrict(h, kk, 1);
+      if (!(top_restricted && kk == h->nlev)) launch_restrict(h, kk, 1);
       rest.push_back(p);
     }
   }
@@ -942,13 +953,27 @@ int launch_iteration(bsam_hier h, int mode) {
     // correction's ghosts after the cycle (the update reads cells, the next
     // cycle starts from E = 0)
     launch_vcycle<float>(h, h->nlev, true);
-    {
+    const bool fold = h->update_fold && consistent_starts_plain(h);
+    if (fold) {   // Q += E with the finest level's restriction
+      const LevelPlan &L = h->lev[h->nlev];
+      Decomp D = decomp(h, L.coarse), Du = decomp(h, h->below_top);
+      Launch l(h, K_RESTRICT, 20.0 * (double)h->n_cells);
+      if (nblk(D.n) + Du.nblocks < spread_limit(h)) {
+        const int nb = (D.n + 63) / 64;
+        launch_k(h, k_restrict_update<64>, nb + (Du.n + 63) / 64, 64, leveld(h, h->nlev), D, fields(h),
+                 (const float *)h->E.p, nb, Du, (const PatchD *)h->patches.p);
+      } else {
+        const int nb = nblk(D.n);
+        launch_k(h, k_restrict_update<>, nb + Du.nblocks, kBlock, leveld(h, h->nlev), D, fields(h),
+                 (const float *)h->E.p, nb, Du, (const PatchD *)h->patches.p);
+      }
+    } else {
       Decomp D = decomp(h, h->all_cells);
       Launch l(h, K_PROLONG, 20.0 * (double)h->n_cells);
       launch_k(h, k_update, D.nblocks, kBlock, D, (const PatchD *)h->patches.p, h->Q.p, (const float *)h->E.p,
                (const int *)h->active.p);
     }
-    launch_consistent(h);
+    launch_consistent(h, fold);
     launch_residual(h, mode);
     CK(cudaGetLastError());
     return BSAM_OK;
@@ -1997,6 +2022,25 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
     h->ncoarse_total = ro;
   }
   h->all_cells = B.make_decomp(0, d->npatch, 1);
+  h->below_top = B.make_decomp(0, h->lev[d->nlev].p0, 1);
+  // k_restrict_update skips the covered cells of the levels below the
+  // finest: exact where those are exactly the cells some restriction writes
+  {
+    std::vector<uint8_t> target((size_t)d->n_q, 0);
+    for (int64_t i = 0; i < d->n_fp; ++i) target[(size_t)d->fp[2 * i]] = 1;
+    bool same = d->nlev >= 2;
+    for (int p = 0; p < h->lev[d->nlev].p0 && same; ++p) {
+      const int32_t *r = B.P(p);
+      const int mx = r[PD_MX], my = r[PD_MY];
+      for (int lj = 0; lj < my && same; ++lj)
+        for (int lx = 0; lx < mx; ++lx) {
+          const bool cov = d->covered[r[PD_COFF] + lx + lj * mx] != 0;
+          const bool tgt = target[(size_t)r[PD_QOFF] + (lx + 1) + (lj + 1) * (mx + 2)] != 0;
+          if (cov != tgt) { same = false; break; }
+        }
+    }
+    h->update_fold = same;
+  }
   std::vector<int> rinst(std::max<int64_t>(d->n_ring, 1), 0);
   for (int p = 0; p < d->npatch; ++p)
     for (int t = B.P(p)[PD_RING0]; t < B.P(p)[PD_RING1]; ++t) rinst[t] = pinst[p];

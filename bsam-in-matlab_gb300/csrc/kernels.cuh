@@ -1972,6 +1972,68 @@ __global__ void __launch_bounds__(kBlock) k_update(Decomp D, const PatchD *__res
   Q[qi] = Q[qi] + (double)E[qi];
 }
 
+// Mixed form: Q += E of the correction cycle (k_update) and the restriction
+// of the finest level k (k_restrict) in one launch, where the consistency
+// step starts with that plain restriction: blocks [0, nb_r) restrict level
+// k, each item adding E to its four fine cells first (k_update's sum) and
+// restricting the sums (restrict_cell's order); the other blocks add E to
+// the cells of the levels below k that no finer level covers.  A covered
+// cell is rewritten by a restriction before anything reads it, and the ones
+// this launch's restriction writes must not be touched here, so skipping
+// them gives the values of k_update then k_restrict.
+template <int kT = kBlock>
+__global__ void __launch_bounds__(kT) k_restrict_update(LevelD L, Decomp D, Fields f, const float *__restrict__ E,
+                                                       int nb_r, Decomp Du, const PatchD *__restrict__ patches) {
+  chain_trigger();
+  if ((int)blockIdx.x < nb_r) {
+    const int g = blockIdx.x * kT + threadIdx.x;
+    if (g >= D.n) {
+      chain_wait();
+      return;
+    }
+    const int p = find_patch(D, g / kBlock, g);
+    const PatchD &P = L.patches[p];
+    if (!f.active[P.inst]) {
+      chain_wait();
+      return;
+    }
+    const int cmx = P.mx >> 1, ldq = P.mx + 2;
+    const int s = g - __ldg(D.beg + p);
+    const int cj = s / cmx, ci = s - cj * cmx;
+    const int dst = __ldg(f.fp + 2 * (P.fp_off + s));
+    chain_wait();
+    double *Q = f.Q + P.q_off;
+    const float *e = E + P.q_off;
+    const int c = (2 * ci + 1) + (2 * cj + 1) * ldq;
+    const double q0 = Q[c] + (double)e[c], q1 = Q[c + 1] + (double)e[c + 1];
+    const double q2 = Q[c + ldq] + (double)e[c + ldq], q3 = Q[c + ldq + 1] + (double)e[c + ldq + 1];
+    Q[c] = q0;
+    Q[c + 1] = q1;
+    Q[c + ldq] = q2;
+    Q[c + ldq + 1] = q3;
+    const double R = 0.25 * (((q0 + q1) + q2) + q3);
+    f.QC[P.qc_off + (ci + 1) + (cj + 1) * (cmx + 2)] = R;
+    f.Q[dst] = R;
+    return;
+  }
+  const int g = ((int)blockIdx.x - nb_r) * kT + threadIdx.x;
+  if (g >= Du.n) {
+    chain_wait();
+    return;
+  }
+  const int p = find_patch(Du, g / kBlock, g);
+  const PatchD &P = patches[p];
+  const int s = g - __ldg(Du.beg + p);
+  if (!f.active[P.inst] || (__ldg(f.flags + P.c_off + s) & 1)) {
+    chain_wait();
+    return;
+  }
+  const int lj = s / P.mx, lx = s - lj * P.mx;
+  const int qi = P.q_off + (lx + 1) + (lj + 1) * (P.mx + 2);
+  chain_wait();
+  f.Q[qi] = f.Q[qi] + (double)E[qi];
+}
+
 // Parabolic driver on the device.  k_history: Uoo = Uo, Uo = interior of Q
 // (ebpSolve.m:52-56); with rotate 0 only Uo = interior of Q (the new
 // hierarchy's Uo after a regrid, ebpRegrid.m:49).  k_prhs: FTrue of the step
