@@ -233,7 +233,7 @@ def mixed_form(backend, fl, opts, ref_Q, steps, warmup, flush, local):
     return {'value': steps / (ms.sum() / 1e3), 'unit': 'solves/s', 'ms_per_solve': float(ms.mean()),
             'p50_ms': float(np.percentile(ms, 50)), 'p99_ms': float(np.percentile(ms, 99)),
             'vcycles': r[0], 'final_rel': r[2], 'rel_l2_vs_fp64': l2, 'rel_max_vs_fp64': mx,
-            'relax_cells_per_thread': dh.relax_tuning(1).tolist(),
+            'relax_cells_per_thread': dh.relax_tuning(1).tolist(), 'kernels_per_vcycle': dh.kernels_per_vcycle(),
             'dtype': 'f32 smoothing / f64 defect correction',
             'note': 'error against the FP64 path, which equals the C oracle bit for bit'}
 
