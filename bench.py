@@ -97,12 +97,16 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples while the timed region runs."""
+    """nvidia-smi clock/throttle samples while the timed region runs: the
+    sampler starts before the region (it waits for its first sample, so the
+    tool's start-up falls outside), samples every 20 ms, and keeps the
+    samples that arrive between mark_start() and mark_end()."""
 
     def __init__(self, index=0):
         self.index = index
         self.rows = []
         self.proc = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         q = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
@@ -110,10 +114,13 @@ class ClockSampler:
              'clocks_event_reasons.sw_power_cap')
         try:
             self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), f'--query-gpu={q}',
-                                          '--format=csv,noheader,nounits', '-lms', '100'],
+                                          '--format=csv,noheader,nounits', '-lms', '20'],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            deadline = time.perf_counter() + 5.0
+            while not self.rows and time.perf_counter() < deadline and self.proc.poll() is None:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
@@ -122,7 +129,14 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [s.strip() for s in line.split(',')]
             if len(parts) == 7:
-                self.rows.append(parts)
+                self.rows.append((time.perf_counter(), parts))
+
+    def mark_start(self):
+        self.t0 = time.perf_counter()
+
+    def mark_end(self):
+        self.t1 = time.perf_counter()
+        time.sleep(0.05)          # the sample of the region's last moments
 
     def __exit__(self, *a):
         if self.proc:
@@ -135,12 +149,16 @@ class ClockSampler:
     def summary(self):
         if not self.rows:
             return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unsampled']}
-        sm = [float(r[0]) for r in self.rows if r[0].replace('.', '').isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace('.', '').isdigit()]
+        t0 = self.t0 if self.t0 is not None else -1e30
+        t1 = (self.t1 + 0.04) if self.t1 is not None else 1e30
+        inside = [r for t, r in self.rows if t0 <= t <= t1]
+        rows = inside or [r for _, r in self.rows]
+        sm = [float(r[0]) for r in rows if r[0].replace('.', '').isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
         names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == 'active'})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i].lower() == 'active'})
         return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': max(mx) if mx else None,
-                'reasons': reasons, 'samples': len(self.rows)}
+                'reasons': reasons, 'samples': len(rows), 'in_region': bool(inside)}
 
 
 def cpu_oracle_rate(H, opts, threads, budget_s):
@@ -532,6 +550,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
+        clk.mark_start()
         for s in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.zero_()
@@ -539,6 +558,7 @@ def main():
             it, hist, rel, vis = one_solve()
             ends[s].record(stream)
         torch.cuda.synchronize()
+        clk.mark_end()
     launches = dh.launch_count() - n0
     per = np.array([a.elapsed_time(b) for a, b in zip(starts, ends)])
     from bsam.replicas import job_rate

@@ -68,3 +68,21 @@ def test_eager_vcycle_mode():
     d = json.loads([l for l in out.stdout.splitlines() if l.startswith('{')][0])
     assert d['eager_vcycle'] == 'done' and d['levels'] == 7 and d['kernels'] > 50
     assert d['precision'] == 'fp64' and d['relax_forms'][0] == 1
+
+
+def test_clock_summary_keeps_the_timed_region():
+    """The clock record of the bench line comes from the samples taken
+    between the timed region's start and end marks; throttle reasons are read
+    from those samples only."""
+    sys.path.insert(0, ROOT)
+    import bench
+    c = bench.ClockSampler()
+    row = lambda mhz, hw: [str(mhz), '2070', '900.0', 'Active' if hw else 'Not Active', 'Not Active',
+                           'Not Active', 'Not Active']
+    c.rows = [(0.0, row(1000, True)), (1.0, row(2070, False)), (1.1, row(2060, False)), (5.0, row(500, True))]
+    c.t0, c.t1 = 0.9, 1.2
+    s = c.summary()
+    assert s['samples'] == 2 and s['in_region'] and s['sm_mhz'] == 2065.0 and s['reasons'] == []
+    c.t0, c.t1 = 10.0, 11.0             # nothing inside: every sample, flagged
+    s = c.summary()
+    assert s['samples'] == 4 and not s['in_region'] and s['reasons'] == ['hw_slowdown']
