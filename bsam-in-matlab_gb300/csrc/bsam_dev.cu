@@ -119,6 +119,7 @@ struct LevelPlan {
   // does a ghost rule of this level read a ghost cell of the parent level
   bool reads_pg = true;
   int64_t q_lo = 0, q_hi = 0;      // the level's patches' range of Q (ghosts included)
+  bool range_own = false;          // no other level's patch lies inside [q_lo, q_hi)
   int dsm_shift[2] = {-1, -1};     // k_relax_dsm slice size 2^shift per precision (-1: not a candidate)
 };
 
@@ -791,10 +792,10 @@ void launch_vcycle(bsam_hier h, int k, bool defer_fill = false) {
   // upload proved that exact (fuse_pre) and on every level of the FP32
   // cycle (FILL_ZERO), unless the relaxation runs as k_relax_cluster, which
   // fills the level itself
-  const bool f32 = sizeof(T) == sizeof(float);
-  const bool pre_fused = h->opts.npre > 0 && relax_form<T>(h, k) != 0 && (f32 || h->lev[k].fuse_pre);
+  const bool zero = sizeof(T) == sizeof(float) && h->lev[k].range_own;
+  const bool pre_fused = h->opts.npre > 0 && relax_form<T>(h, k) != 0 && (zero || h->lev[k].fuse_pre);
   launch_relax<T>(h, k, h->opts.npre, false, pre_fused);
-  launch_restrict_fill<T>(h, k, !pre_fused ? FILL_NONE : f32 ? FILL_ZERO : FILL_PRE);
+  launch_restrict_fill<T>(h, k, !pre_fused ? FILL_NONE : zero ? FILL_ZERO : FILL_PRE);
   launch_coarse_load<T>(h, k);
   const bool fused = fill_deferrable<T>(h, k - 1);
   launch_vcycle<T>(h, k - 1, fused);
@@ -2023,6 +2024,19 @@ int do_upload(bsam_hier h, const bsam_hier_desc *d) {
   }
   h->all_cells = B.make_decomp(0, d->npatch, 1);
   h->below_top = B.make_decomp(0, h->lev[d->nlev].p0, 1);
+  // a level whose Q range holds only its own patches (the FP32 cycle's
+  // zero-parent fill takes every operand outside the range for a parent cell)
+  for (int k = 1; k <= d->nlev; ++k) {
+    LevelPlan &L = h->lev[k];
+    bool own = true;
+    for (int p = 0; p < d->npatch && own; ++p) {
+      if (p >= L.p0 && p < L.p1) continue;
+      const int32_t *r = B.P(p);
+      const int64_t a = r[PD_QOFF], b = a + (int64_t)(r[PD_MX] + 2) * (r[PD_MY] + 2);
+      own = b <= L.q_lo || a >= L.q_hi;
+    }
+    L.range_own = own;
+  }
   // k_restrict_update skips the covered cells of the levels below the
   // finest: exact where those are exactly the cells some restriction writes
   {
