@@ -907,23 +907,27 @@ __device__ __forceinline__ T dsm_rule(const DsmRange<T> &D, const Rule &R, const
 template <class T>
 struct DsmCell {
   T dE, dW, dN, dS, idg, gx, gy, fv;
-  uint32_t oa[5];        // shared-window addresses of the rule's operands inside the range
-  int c, ldq, code, cc, rx, ry, rtype, omask;   // c relative to q0 after the bind; omask bit i: operand i inside
+  uint32_t oa[5];        // per rule operand: its shared-window address (inside the range) or global index
+  int c, ldq, code, cc, rx, ry, rtype, omask;   // c relative to q0; omask bit i: operand i inside the range
   bool live;
 };
 
-// the static part, requested before the programmatic-launch wait
+// the static part, before the programmatic-launch wait: the cell's packed
+// operands and boundary data, and its ghost rule -- kind, and per operand
+// the shared-window address (inside the range, mask bit set) or the global
+// index whose value the bind loads
 template <class T>
 __device__ __forceinline__ void dsm_cell_static(const RelaxChunkD *__restrict__ chunks, int nchunks,
                                                 const T *__restrict__ pack, const FieldsT<T> &f,
                                                 const Rule *__restrict__ perim, const uint8_t *__restrict__ cact,
-                                                int amode, int ch, int tc, int m, DsmCell<T> &X) {
+                                                int amode, int ch, int tc, int m, const DsmRange<T> &D,
+                                                DsmCell<T> &X) {
   CellState<T> S;
   cell_issue<T>(chunks, nchunks, pack, m, cact, amode, ch, tc, S);
   cell_derive<T>(f, perim, m, 1, tc, S);
   X.live = S.live;
   X.dE = S.dE; X.dW = S.dW; X.dN = S.dN; X.dS = S.dS; X.idg = S.idg; X.gx = S.gx; X.gy = S.gy;
-  X.c = S.q_off + S.c;
+  X.c = S.q_off + S.c - D.q0;
   X.ldq = S.ldq;
   X.code = S.code;
   X.cc = S.cc;
@@ -931,18 +935,8 @@ __device__ __forceinline__ void dsm_cell_static(const RelaxChunkD *__restrict__ 
   X.ry = S.ry;
   X.rtype = 0;
   X.omask = 0;
-}
-
-// the dynamic part of the set-up, after the wait: force, and the rule's
-// operands (values outside the range into ov, addresses inside)
-template <class T>
-__device__ __forceinline__ void dsm_cell_bind(const FieldsT<T> &f, const Rule *__restrict__ perim,
-                                              const DsmRange<T> &D, T *ov, DsmCell<T> &X) {
-  if (!X.live) return;
-  X.fv = f.F[X.cc];
-  X.c -= D.q0;
   const int kx = X.code & 3, ky = (X.code >> 2) & 3;
-  if (kx == 3 || ky == 3) {
+  if (X.live && (kx == 3 || ky == 3)) {
     const Rule R = perim[kx == 3 ? X.rx : X.ry];
     X.rtype = R.type;
     const int op[5] = {R.a, R.b, R.c, R.d, R.e};
@@ -953,10 +947,23 @@ __device__ __forceinline__ void dsm_cell_bind(const FieldsT<T> &f, const Rule *_
         X.omask |= 1 << i;
         X.oa[i] = dsm_addr(D, rel);
       } else {
-        X.oa[i] = 0;
-        ov[i] = f.Q[op[i]];
+        X.oa[i] = (uint32_t)op[i];
       }
     }
+  }
+}
+
+// the dynamic part of the set-up, after the wait: the force and the values
+// of the rule's operands outside the range (into ov)
+template <class T>
+__device__ __forceinline__ void dsm_cell_bind(const FieldsT<T> &f, T *ov, DsmCell<T> &X) {
+  if (!X.live) return;
+  X.fv = f.F[X.cc];
+  const int kx = X.code & 3, ky = (X.code >> 2) & 3;
+  if (kx == 3 || ky == 3) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+      if (!((X.omask >> i) & 1)) ov[i] = f.Q[(int)X.oa[i]];
   }
 }
 
@@ -1050,14 +1057,14 @@ __global__ void __launch_bounds__(kDsmBlock, 1)
   DsmCell<T> X0, X1;
   X0.live = X1.live = false;
   if (mine) {
-    dsm_cell_static<T>(chunks, nchunks, pack, f, perim, cact, amode, w / kChunk, w % kChunk, 0, X0);
-    dsm_cell_static<T>(chunks, nchunks, pack, f, perim, cact, amode, w / kChunk, w % kChunk, 1, X1);
+    dsm_cell_static<T>(chunks, nchunks, pack, f, perim, cact, amode, w / kChunk, w % kChunk, 0, D, X0);
+    dsm_cell_static<T>(chunks, nchunks, pack, f, perim, cact, amode, w / kChunk, w % kChunk, 1, D, X1);
   }
   chain_wait();
   const int e0 = r * S, e1 = min(qn, e0 + S);
   for (int e = e0 + (int)threadIdx.x; e < e1; e += kB) slice[e - e0] = f.Q[q0 + e];
-  dsm_cell_bind<T>(f, perim, D, ov0, X0);
-  dsm_cell_bind<T>(f, perim, D, ov1, X1);
+  dsm_cell_bind<T>(f, ov0, X0);
+  dsm_cell_bind<T>(f, ov1, X1);
   cl.sync();
   for (int s = 0; s < nsweeps; ++s) {
     dsm_cell_update<T, kPow2>(L, f, perim, omega, unit_omega, (first_fresh || s > 0) ? 1 : 0, X0, ov0, D);
