@@ -605,7 +605,11 @@ void launch_relax(bsam_hier h, int k, int nsweeps, bool first_fresh = false, boo
         }
         continue;
       }
-      if (grid < spread_limit(h)) {   // one chunk per block: the FP64 work over more SMs
+      // one chunk per block, the FP64 work over more SMs; the FP32 pass has
+      // little arithmetic, and fewer, larger blocks schedule faster once the
+      // level fills the SMs (starfish FP32 iteration 337 -> 326 us)
+      const int lim = sizeof(T) == sizeof(float) ? sm_count() : spread_limit(h);
+      if (grid < lim) {
         if (L.pow2)
           launch_k(h, k_relax<T, true, kChunk>, L.rc_n, kChunk, ld, ch, L.rc_n, f, pk, (const Rule *)h->perim.p, m,
                    (T)h->opts.omega, unit, fresh, ca, am);
