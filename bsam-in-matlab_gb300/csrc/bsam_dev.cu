@@ -1017,15 +1017,17 @@ int tune_set(bsam_hier h, int k) {
 }
 
 // microseconds of one relaxation of level k (npre sweeps and the fill) in
-// launch form kn, replayed as a graph (as the solve runs it); a form the
-// runtime refuses is not a candidate (+inf)
+// launch form kn, timed as the solve runs it: a graph of kRelax relaxations
+// in a row (a graph launch's own granularity then divides by kRelax); a
+// form the runtime refuses is not a candidate (+inf)
 template <class T>
 float time_form(bsam_hier h, int k, int kn, int ns) {
+  constexpr int kRelax = 8;
   std::vector<int> &rn = h->relax_n[sizeof(T) == sizeof(float) ? 1 : 0];
   rn[k] = kn;
   cudaGetLastError();
   if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return 1e30f;
-  launch_relax<T>(h, k, ns);
+  for (int r = 0; r < kRelax; ++r) launch_relax<T>(h, k, ns);
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ge = nullptr;
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
@@ -1037,15 +1039,14 @@ float time_form(bsam_hier h, int k, int kn, int ns) {
   if (e == cudaSuccess) e = cudaEventCreate(&b);
   if (e == cudaSuccess) e = cudaGraphLaunch(ge, h->stream);   // warm-up
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-  constexpr int kReps = 4;
   for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
     cudaEventRecord(a, h->stream);
-    for (int i = 0; i < kReps; ++i) cudaGraphLaunch(ge, h->stream);
+    cudaGraphLaunch(ge, h->stream);
     cudaEventRecord(b, h->stream);
     e = cudaEventSynchronize(b);
     float ms = 0;
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
-    if (e == cudaSuccess) t = std::min(t, 1000.0f * ms / kReps);
+    if (e == cudaSuccess) t = std::min(t, 1000.0f * ms / kRelax);
   }
   if (a) cudaEventDestroy(a);
   if (b) cudaEventDestroy(b);
